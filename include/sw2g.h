@@ -1,0 +1,143 @@
+/*
+ * sw2g: GB300 (sm_103a) implementation of the SW2 shallow-water time step,
+ * behind a plain C ABI (no CUDA or torch types in any signature).
+ *
+ * It replaces the reference's per-step hot path: the body of
+ *   void loop(char *bname, char *output_folder, sw *SW)          (core.c:22, sw.h:223)
+ * from core.c:134 to core.c:338, i.e. compute_Dt, solve_tracer, solve_cons_h,
+ * do_AdamsBashforth, do_eta_geofactor, solve_adv_u/v, solve_pres_u/v,
+ * dissipation_effect, laplacian_vels/laplacian_eta, solve_Coriolis_u/v,
+ * halo_update and do_channel (sw.h:230-292; laplacian.c; sppde_hupdate.c),
+ * together with the energy diagnostic calc_energy_balance (energy.c:25).
+ *
+ * Fields cross the boundary in the reference's own layout: padded
+ * (nx+4) x (ny+4) arrays of doubles, halo width 2, x fastest, cell (i,j) at
+ * (i+1) + (j+1)*(nx+4) for i in [-1,nx+2], j in [-1,ny+2] (sppde/sppde.h:131-142).
+ *
+ * Errors are returned, never raised: no call exits or aborts the process
+ * (the reference calls MPI_Abort through CRASH, sppde_core.c:163-190).
+ * A context is used by one host thread at a time; it owns its device memory
+ * and its CUDA stream. Calls on one context are not reentrant.
+ */
+#ifndef SW2G_H
+#define SW2G_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  SW2G_OK = 0,
+  SW2G_ERR_BAD_ARG = 1,   /* invalid case or argument (the reference CRASHes in init.c) */
+  SW2G_ERR_CFL = 2,       /* Dt > Dt_CFL at the start of a step (core.c:156-158) */
+  SW2G_ERR_NONFINITE = 3, /* field range check failed after a step (core.c:309-312) */
+  SW2G_ERR_TIMEOUT = 4,   /* a bounded device wait gave up */
+  SW2G_ERR_CUDA = 5,      /* a CUDA runtime call failed */
+  SW2G_ERR_NOMEM = 6,     /* device or host allocation failed */
+  SW2G_ERR_STATE = 7      /* call out of order (e.g. step before upload) */
+} sw2g_status;
+
+/* Arithmetic of the step. */
+typedef enum {
+  SW2G_FP64 = 0, /* plain FP64, bit-identical to the reference's single-rank run */
+  SW2G_FP32 = 1  /* FP32 stencils on height perturbation, FP64 state accumulation */
+} sw2g_precision;
+
+/* Behaviour flags (sw2g_case.flags). Zero reproduces the reference exactly. */
+#define SW2G_FLAG_VANLEER_SAFE 0x1u  /* Van Leer limiter gives 0 (its limit) at r = -1 instead of 0/0 */
+
+/* The parsed case, as the reference's initialize() stores it in the sw struct
+ * (init.c:48-161). Angles are in degrees, as in the .sw file. Polar 0 only. */
+typedef struct {
+  int nx, ny;                    /* interior cells; each >= 3 (sppde_core.c:431-459) */
+  int sch;                       /* limiter 0..9 (calc.c:262-273) */
+  double lon0, lon1, lat0, lat1; /* degrees */
+  double Omega, rE, rP, gE, depth;
+  double Dt;                     /* time step (s) */
+  double courant;                /* CFL: Dt must not exceed courant / max(|u|/dx + |v|/dy) */
+  double tau;                    /* Tau: sigma = 1/tau, 0 when tau > 1e10 (init.c:110-114) */
+  double tracer_dis;             /* TracerDis */
+  double hypernu[3];             /* Hypernu as entered: nu2, nu4 (positive), nu6 */
+  unsigned flags;                /* SW2G_FLAG_* */
+} sw2g_case;
+
+typedef struct sw2g_ctx sw2g_ctx;
+
+/* Upload modes. */
+#define SW2G_UPLOAD_RAW 0   /* every padded cell verbatim (state mid-run) */
+#define SW2G_UPLOAD_FRAME 1 /* interiors of eta/u/v/tracer, halos refreshed by the single-rank
+                               wrap (what load_binary_sw leaves, io.c:115-171); winds and hB verbatim */
+#define SW2G_UPLOAD_CONTINUE 2 /* as RAW, but the Adams-Bashforth history and the step count are
+                                  kept: a caller that holds the state on the host between steps */
+
+/* Returns a static description of a status code. */
+const char *sw2g_status_string(sw2g_status s);
+
+/* Creates a context on CUDA device `device` and builds the per-row geometry
+ * (coords.c:21-126, init.c:279-297). Replaces the allocation part of loop()
+ * (core.c:55-81) and the geometry part of initialize(). */
+sw2g_status sw2g_create(const sw2g_case *c, int precision, int device, sw2g_ctx **out);
+
+/* Copies the state in. Any pointer among tracer/windx/windy/hB may be NULL
+ * (read as zero). Resets the Adams-Bashforth start-up, as a reference restart
+ * does (core.c:133-134). Replaces load_binary_sw (io.c:115) and the pre-loop
+ * halo/channel set-up (core.c:88-101). */
+sw2g_status sw2g_upload(sw2g_ctx *ctx, const double *eta, const double *u, const double *v,
+                        const double *tracer, const double *windx, const double *windy,
+                        const double *hB, int mode);
+
+/* Advances nsteps time steps (the loop body, core.c:134-338). The
+ * Adams-Bashforth history is kept across calls. On SW2G_ERR_CFL or
+ * SW2G_ERR_NONFINITE, sw2g_error_step() gives the 0-based step (counted from
+ * the last upload) where the reference would have aborted; the device state
+ * is then unspecified. */
+sw2g_status sw2g_step(sw2g_ctx *ctx, int nsteps);
+
+/* Step index of the last CFL/range failure, -1 if none. */
+int sw2g_error_step(const sw2g_ctx *ctx);
+
+/* Copies the padded state out; NULL pointers are skipped. */
+sw2g_status sw2g_download(sw2g_ctx *ctx, double *eta, double *u, double *v, double *tracer);
+
+/* Kinetic and available potential energy as calc_energy_balance (energy.c:25-55)
+ * defines them, and mass = sum of H*DXC*DYC over the interior (same area element),
+ * each summed with compensated FP64 arithmetic. */
+sw2g_status sw2g_diag(sw2g_ctx *ctx, double *ke, double *ape, double *mass);
+
+/* Restarts the Adams-Bashforth sequence with an Euler step (as after LoadFrom). */
+sw2g_status sw2g_reset_ab(sw2g_ctx *ctx);
+
+/* Steps taken since the last upload. */
+long long sw2g_steps_done(const sw2g_ctx *ctx);
+
+/* Device pointer of a padded state field (0 eta, 1 u, 2 v, 3 tracer) for
+ * callers that keep data on the GPU; NULL on a bad index. */
+void *sw2g_device_field(sw2g_ctx *ctx, int which);
+
+/* CUDA stream the context launches on (as void*; cudaStream_t underneath). */
+void *sw2g_stream(sw2g_ctx *ctx);
+
+/* Number of kernel launches issued by the last sw2g_step call. */
+long long sw2g_last_launches(const sw2g_ctx *ctx);
+
+/* Device time (ms, CUDA events on the context's stream) from the first to the
+ * last launch of the last sw2g_step call. Replaces the reference's per-step
+ * wall-clock channel (core.c:143,333-336). */
+double sw2g_last_step_ms(const sw2g_ctx *ctx);
+
+/* Named per-kernel device timers, the counterpart of the reference's
+ * cr_start/cr_end channels (sppde/sppde_cr.c:38-217). While enabled, each
+ * launch is bracketed by CUDA events; times accumulate per kernel name until
+ * reset. Names are static strings owned by the library. */
+sw2g_status sw2g_timers_enable(sw2g_ctx *ctx, int on);
+void sw2g_timers_reset(sw2g_ctx *ctx);
+int sw2g_timers_count(const sw2g_ctx *ctx);
+sw2g_status sw2g_timer_read(const sw2g_ctx *ctx, int idx, const char **name, long long *launches,
+                            double *total_ms);
+
+void sw2g_destroy(sw2g_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

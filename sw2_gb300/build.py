@@ -1,0 +1,82 @@
+"""Builds libsw2g.so in-tree (sw2_gb300/_build/) for sm_103a.
+
+Translation units compile in parallel; the FP64 step is compiled with
+-fmad=false (no contraction, for bit-identity with the reference) and host
+code with -ffp-contract=off (gcc contracts by default on aarch64).
+
+    python -m sw2_gb300.build
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libsw2g.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+HOST = "-fPIC,-ffp-contract=off,-O2"
+
+# (source, extra nvcc flags)
+UNITS = [
+    ("api.cu", []),
+    ("step_fp64.cu", ["-fmad=false"]),
+    ("geometry.cpp", None),  # plain host C++
+]
+
+
+def nvcc() -> str:
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return p
+
+
+def _compile(src: str, extra) -> str:
+    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+    path = os.path.join(CSRC, src)
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    if extra is None:
+        cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", *inc, "-I", cuda_inc,
+               "-c", path, "-o", obj]
+    else:
+        cmd = [nvcc(), *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", HOST, "-Xptxas", "-v" if os.environ.get("SW2G_PTXAS_V") else "-O3",
+               *extra, *inc, "-c", path, "-o", obj]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if os.environ.get("SW2G_PTXAS_V"):
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def _stale() -> bool:
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "sw2g.h"), __file__]
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build(force: bool = False) -> str:
+    if not force and not _stale():
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        objs = list(ex.map(lambda u: _compile(*u), UNITS))
+    tmp = LIB + ".tmp"
+    cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,398 @@
+// C-ABI of the GB300 SW2 step (declared in include/sw2g.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "sw2g_internal.h"
+
+using namespace sw2g;
+
+namespace {
+
+constexpr int kChunk = 1024;  // steps per check read-back
+
+}  // namespace
+
+struct sw2g_ctx {
+  sw2g_case c{};
+  int precision = SW2G_FP64;
+  int device = 0;
+  int sch = 0;
+  DevState s{};
+  std::vector<double> rows;
+  double rest_mx = 0, rest_my = 0;
+  double* d_rows = nullptr;
+  Fp64Buffers b{};
+  std::vector<double*> allocs;
+  unsigned long long* d_cfl = nullptr;
+  int* d_bad = nullptr;
+  double* d_energy = nullptr;  // 3*ny row partials + 3 totals
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  double last_step_ms = 0;
+  Timers timers;
+  bool uploaded = false;
+  bool tracer_active = false;
+  int k = 0;  // Adams-Bashforth index n - nstart
+  long long steps = 0;
+  int err_step = -1;
+  long long last_launches = 0;
+};
+
+namespace {
+
+sw2g_status cuda_fail(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return SW2G_OK;
+  fprintf(stderr, "sw2g: %s: %s\n", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? SW2G_ERR_NOMEM : SW2G_ERR_CUDA;
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    sw2g_status _st = cuda_fail((call), #call);               \
+    if (_st != SW2G_OK) return _st;                           \
+  } while (0)
+
+bool case_ok(const sw2g_case* c) {
+  if (!c) return false;
+  if (c->nx < 3 || c->ny < 3 || c->sch < 0 || c->sch > 9) return false;
+  if ((long long)(c->nx + 4) * (c->ny + 4) > (1LL << 31) - 1) return false;
+  if (!(c->rE > 0) || !(c->rP > 0) || !(c->Dt > 0) || !(c->courant > 0)) return false;
+  if (!(c->lon1 > c->lon0) || !(c->lat1 > c->lat0)) return false;
+  if (!(c->lat0 > -90.0) || !(c->lat1 < 90.0)) return false;
+  // init.c:122: hyperviscosity coefficients are entered as non-negative
+  if (c->hypernu[0] < 0 || c->hypernu[1] < 0 || c->hypernu[2] < 0) return false;
+  if (c->flags & ~SW2G_FLAG_VANLEER_SAFE) return false;
+  return true;
+}
+
+sw2g_status dalloc(sw2g_ctx* x, double** p, size_t n) {
+  CK(cudaMalloc((void**)p, n * sizeof(double)));
+  CK(cudaMemsetAsync(*p, 0, n * sizeof(double), x->stream));
+  x->allocs.push_back(*p);
+  return SW2G_OK;
+}
+
+}  // namespace
+
+namespace sw2g {
+
+cudaEvent_t Timers::take() {
+  if (!free_.empty()) {
+    cudaEvent_t e = free_.back();
+    free_.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void Timers::begin(const char* tag, cudaStream_t st) {
+  int idx = -1;
+  for (size_t q = 0; q < entries_.size(); q++)
+    if (std::strcmp(entries_[q].name, tag) == 0) idx = (int)q;
+  if (idx < 0) {
+    entries_.push_back(Entry{tag, 0, 0.0});
+    idx = (int)entries_.size() - 1;
+  }
+  open_ = idx;
+  open_ev_ = take();
+  cudaEventRecord(open_ev_, st);
+}
+
+void Timers::end(cudaStream_t st) {
+  if (open_ < 0) return;
+  cudaEvent_t e = take();
+  cudaEventRecord(e, st);
+  pending_.push_back(Pending{open_, open_ev_, e});
+  open_ = -1;
+}
+
+void Timers::collect() {
+  for (const Pending& p : pending_) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      entries_[p.entry].ms += ms;
+      entries_[p.entry].launches += 1;
+    }
+    free_.push_back(p.a);
+    free_.push_back(p.b);
+  }
+  pending_.clear();
+}
+
+void Timers::reset() {
+  for (Entry& e : entries_) {
+    e.launches = 0;
+    e.ms = 0;
+  }
+}
+
+void Timers::release() {
+  collect();
+  for (cudaEvent_t e : free_) cudaEventDestroy(e);
+  free_.clear();
+  entries_.clear();
+}
+
+}  // namespace sw2g
+
+extern "C" {
+
+const char* sw2g_status_string(sw2g_status s) {
+  switch (s) {
+    case SW2G_OK: return "ok";
+    case SW2G_ERR_BAD_ARG: return "invalid argument";
+    case SW2G_ERR_CFL: return "time step exceeds the CFL limit";
+    case SW2G_ERR_NONFINITE: return "field out of range or not finite";
+    case SW2G_ERR_TIMEOUT: return "device wait timed out";
+    case SW2G_ERR_CUDA: return "CUDA error";
+    case SW2G_ERR_NOMEM: return "out of memory";
+    case SW2G_ERR_STATE: return "call out of order";
+  }
+  return "unknown status";
+}
+
+sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx** out) {
+  if (!out) return SW2G_ERR_BAD_ARG;
+  *out = nullptr;
+  if (!case_ok(c) || (precision != SW2G_FP64)) return SW2G_ERR_BAD_ARG;
+  sw2g_ctx* x = new (std::nothrow) sw2g_ctx();
+  if (!x) return SW2G_ERR_NOMEM;
+  x->c = *c;
+  x->precision = precision;
+  x->device = device;
+  x->sch = c->sch;
+  if (c->sch == 3 && (c->flags & SW2G_FLAG_VANLEER_SAFE)) x->sch = kVanLeerSafe;
+  sw2g_status st = SW2G_OK;
+  auto fail = [&](sw2g_status e) {
+    sw2g_destroy(x);
+    return e;
+  };
+  if ((st = cuda_fail(cudaSetDevice(device), "cudaSetDevice")) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking), "stream")) != SW2G_OK)
+    return fail(st);
+  for (int e = 0; e < 2; e++)
+    if ((st = cuda_fail(cudaEventCreate(&x->ev[e]), "event")) != SW2G_OK) return fail(st);
+  build_rows(*c, x->rows, &x->rest_mx, &x->rest_my);
+  DevState& s = x->s;
+  s.nx = c->nx;
+  s.ny = c->ny;
+  s.W = c->nx + 4;
+  s.H = c->ny + 4;
+  s.depth = c->depth;
+  s.Dt = c->Dt;
+  s.sigma = c->tau > 1e10 ? 0 : 1.0 / c->tau;  // init.c:110-114
+  s.sigma_tr = c->tracer_dis;
+  s.nu2 = c->hypernu[0];
+  s.nu4 = -c->hypernu[1];  // init.c:120
+  s.nu6 = c->hypernu[2];
+  const size_t S = (size_t)s.W * s.H;
+  if ((st = dalloc(x, &x->d_rows, x->rows.size())) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaMemcpyAsync(x->d_rows, x->rows.data(), x->rows.size() * sizeof(double),
+                                      cudaMemcpyHostToDevice, x->stream), "rows")) != SW2G_OK)
+    return fail(st);
+  s.rows = x->d_rows;
+  Fp64Buffers& b = x->b;
+  double** all[] = {&b.f[0], &b.f[1], &b.f[2], &b.f[3], &b.f[4], &b.f[5], &b.f[6],
+                    &b.deta[0], &b.deta[1], &b.deta[2], &b.du[0], &b.du[1], &b.du[2],
+                    &b.dv[0], &b.dv[1], &b.dv[2], &b.dtr[0], &b.dtr[1], &b.dtr[2],
+                    &b.detaAB, &b.duAB, &b.dvAB, &b.dtrAB, &b.duadv, &b.dvadv,
+                    &b.Le[0], &b.Le[1], &b.Le[2], &b.L[0], &b.L[1], &b.L[2], &b.L[3], &b.L[4], &b.L[5],
+                    &b.psi, &b.xi, &b.ze, &b.di};
+  for (double** p : all)
+    if ((st = dalloc(x, p, S)) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
+    return fail(st);
+  if ((st = cuda_fail(cudaMalloc((void**)&x->d_bad, sizeof(int) * kChunk), "bad")) != SW2G_OK) return fail(st);
+  if ((st = dalloc(x, &x->d_energy, 3 * (size_t)c->ny + 3)) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaStreamSynchronize(x->stream), "sync")) != SW2G_OK) return fail(st);
+  *out = x;
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_upload(sw2g_ctx* x, const double* eta, const double* u, const double* v, const double* tracer,
+                        const double* windx, const double* windy, const double* hB, int mode) {
+  if (!x || !eta || !u || !v) return SW2G_ERR_BAD_ARG;
+  if (mode != SW2G_UPLOAD_RAW && mode != SW2G_UPLOAD_FRAME && mode != SW2G_UPLOAD_CONTINUE) return SW2G_ERR_BAD_ARG;
+  const bool cont = (mode == SW2G_UPLOAD_CONTINUE);
+  if (cont && !x->uploaded) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  const DevState& s = x->s;
+  const size_t S = (size_t)s.W * s.H, bytes = S * sizeof(double);
+  const double* src[7] = {eta, u, v, tracer, windx, windy, hB};
+  for (int q = 0; q < 7; q++) {
+    if (src[q]) CK(cudaMemcpyAsync(x->b.f[q], src[q], bytes, cudaMemcpyHostToDevice, x->stream));
+    else if (!cont) CK(cudaMemsetAsync(x->b.f[q], 0, bytes, x->stream));  // CONTINUE: NULL keeps the field
+  }
+  if (mode == SW2G_UPLOAD_FRAME)
+    for (int q = 0; q < 4; q++) halo_wrap(x->b.f[q], s.nx, s.ny, x->stream);
+  if (cont) {
+    // history, step count and the tracer decision carry over (unless a tracer is given)
+    if (tracer) x->tracer_active = true;
+    CK(cudaStreamSynchronize(x->stream));
+    return SW2G_OK;
+  }
+  // The tracer step is skipped while the tracer is +0.0 in every cell it can
+  // read: with no source the reference's tracer update then provably leaves it +0.
+  bool active = false;
+  if (tracer) {
+    for (int j = -1; j <= s.ny + 2 && !active; j++)
+      for (int i = -1; i <= s.nx + 2; i++) {
+        const bool inner = (i >= 1 && i <= s.nx && j >= 1 && j <= s.ny);
+        if (mode == SW2G_UPLOAD_FRAME && !inner) continue;
+        uint64_t bits;
+        std::memcpy(&bits, &tracer[(i + 1) + (size_t)(j + 1) * s.W], sizeof(bits));
+        if (bits != 0) { active = true; break; }
+      }
+  }
+  x->tracer_active = active;
+  x->k = 0;
+  x->steps = 0;
+  x->err_step = -1;
+  x->uploaded = true;
+  CK(cudaStreamSynchronize(x->stream));
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
+  if (!x || nsteps < 0) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  x->last_launches = 0;
+  std::vector<unsigned long long> cfl(2 * kChunk);
+  std::vector<int> bad(kChunk);
+  int done = 0;
+  x->last_step_ms = 0;
+  while (done < nsteps) {
+    const int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
+    CK(cudaMemsetAsync(x->d_cfl, 0, sizeof(unsigned long long) * 2 * n, x->stream));
+    CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int) * n, x->stream));
+    StepChecks chk{x->d_cfl, x->d_bad};
+    CK(cudaEventRecord(x->ev[0], x->stream));
+    for (int t = 0; t < n; t++) {
+      x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers);
+      x->k++;
+    }
+    CK(cudaEventRecord(x->ev[1], x->stream));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cfl.data(), x->d_cfl, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost, x->stream));
+    CK(cudaMemcpyAsync(bad.data(), x->d_bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+    CK(cudaStreamSynchronize(x->stream));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
+    x->last_step_ms += ms;
+    if (x->timers.on) x->timers.collect();
+    for (int t = 0; t < n; t++) {
+      // compute_Dt (calc.c:701-738) and its check (core.c:158)
+      double mx, my;
+      std::memcpy(&mx, &cfl[2 * t], sizeof(double));
+      std::memcpy(&my, &cfl[2 * t + 1], sizeof(double));
+      if (mx + my == 0) { mx = x->rest_mx; my = x->rest_my; }
+      const double dt_cfl = (x->c.courant / (mx + my));
+      if (x->c.Dt > dt_cfl) {
+        x->err_step = (int)(x->steps + t);
+        x->steps += t;
+        return SW2G_ERR_CFL;
+      }
+      if (bad[t]) {
+        x->err_step = (int)(x->steps + t);
+        x->steps += t + 1;
+        return SW2G_ERR_NONFINITE;
+      }
+    }
+    x->steps += n;
+    done += n;
+  }
+  return SW2G_OK;
+}
+
+int sw2g_error_step(const sw2g_ctx* x) { return x ? x->err_step : -1; }
+long long sw2g_steps_done(const sw2g_ctx* x) { return x ? x->steps : 0; }
+long long sw2g_last_launches(const sw2g_ctx* x) { return x ? x->last_launches : 0; }
+
+sw2g_status sw2g_download(sw2g_ctx* x, double* eta, double* u, double* v, double* tracer) {
+  if (!x) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  const size_t bytes = sizeof(double) * (size_t)x->s.W * x->s.H;
+  double* dst[4] = {eta, u, v, tracer};
+  for (int q = 0; q < 4; q++)
+    if (dst[q]) CK(cudaMemcpyAsync(dst[q], x->b.f[q], bytes, cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_diag(sw2g_ctx* x, double* ke, double* ape, double* mass) {
+  if (!x) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  const double* f[7];
+  for (int q = 0; q < 7; q++) f[q] = x->b.f[q];
+  energy_rows(x->s, f, x->d_energy, x->stream);
+  energy_sum(x->d_energy, x->s.ny, x->d_energy + 3 * (size_t)x->s.ny, x->stream);
+  double h[3];
+  CK(cudaMemcpyAsync(h, x->d_energy + 3 * (size_t)x->s.ny, sizeof(h), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  if (ke) *ke = h[0];
+  if (ape) *ape = h[1];
+  if (mass) *mass = h[2];
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_reset_ab(sw2g_ctx* x) {
+  if (!x) return SW2G_ERR_BAD_ARG;
+  x->k = 0;
+  return SW2G_OK;
+}
+
+void* sw2g_device_field(sw2g_ctx* x, int which) {
+  if (!x || which < 0 || which > 3) return nullptr;
+  return x->b.f[which];
+}
+
+void* sw2g_stream(sw2g_ctx* x) { return x ? (void*)x->stream : nullptr; }
+
+void sw2g_destroy(sw2g_ctx* x) {
+  if (!x) return;
+  cudaSetDevice(x->device);
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  for (double* p : x->allocs) cudaFree(p);
+  if (x->d_cfl) cudaFree(x->d_cfl);
+  if (x->d_bad) cudaFree(x->d_bad);
+  x->timers.release();
+  for (int e = 0; e < 2; e++)
+    if (x->ev[e]) cudaEventDestroy(x->ev[e]);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete x;
+}
+
+double sw2g_last_step_ms(const sw2g_ctx* x) { return x ? x->last_step_ms : 0.0; }
+
+sw2g_status sw2g_timers_enable(sw2g_ctx* x, int on) {
+  if (!x) return SW2G_ERR_BAD_ARG;
+  x->timers.on = (on != 0);
+  return SW2G_OK;
+}
+
+void sw2g_timers_reset(sw2g_ctx* x) {
+  if (x) x->timers.reset();
+}
+
+int sw2g_timers_count(const sw2g_ctx* x) { return x ? (int)x->timers.entries().size() : 0; }
+
+sw2g_status sw2g_timer_read(const sw2g_ctx* x, int idx, const char** name, long long* launches, double* total_ms) {
+  if (!x || idx < 0 || idx >= (int)x->timers.entries().size()) return SW2G_ERR_BAD_ARG;
+  const Timers::Entry& e = x->timers.entries()[idx];
+  if (name) *name = e.name;
+  if (launches) *launches = e.launches;
+  if (total_ms) *total_ms = e.ms;
+  return SW2G_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+// Host geometry for a polar-0 case. Every expression keeps the operand order of
+// the reference macro it restates, and this file is compiled with
+// -ffp-contract=off, so the tables are bit-identical to the values the
+// reference computes per cell.
+#include <cmath>
+
+#include "sw2g_internal.h"
+
+namespace sw2g {
+namespace {
+
+struct Planet {
+  double rE, rP, eps2, gE, Omega;
+};
+
+double ref_pi() { return 4.0 * std::atan(1.0); }                                   // sw.h:16
+double deg2rad(double a) { return a * (ref_pi() / 180.0); }                        // sw.h:108
+double linspace_val(int i, double x0, double x1, int n) {                          // tools.c:256-273
+  return x0 + (double)i * (x1 - x0) / ((double)n);
+}
+double rZ(const Planet& p, double lat) {                                           // sw.h:174
+  return p.rE / std::sqrt(1.0 + (std::tan(lat) * std::tan(lat)) / p.eps2);
+}
+double rM(const Planet& p, double lat) {                                           // sw.h:175
+  double q = rZ(p, lat) / (p.rE * std::cos(lat));
+  return p.rE / p.eps2 * (q * q * q);
+}
+double lat2pclat(const Planet& p, double lat) { return std::atan(1.0 / p.eps2 * std::tan(lat)); }  // sw.h:170
+double radius(const Planet& p, double pc) {                                        // sw.h:172
+  double a = p.rE * std::sin(pc), b = p.rP * std::cos(pc);
+  return p.rE * p.rP / std::sqrt(a * a + b * b);
+}
+double g_eff(const Planet& p, double pc) {                                         // sw.h:178-179
+  double r = radius(p, pc);
+  double g0 = (p.gE + p.Omega * p.Omega * p.rE) * ((p.rE / r) * (p.rE / r));
+  return g0 - p.Omega * p.Omega * r * std::cos(pc);
+}
+double fcor(const Planet& p, double lat) { return 2.0 * p.Omega * std::sin(lat); }  // sw.h:193
+
+}  // namespace
+
+void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, double* rest_my) {
+  const int ny = c.ny, H = c.ny + 4;
+  Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};  // init.c:150
+  const double lon0 = deg2rad(c.lon0), lon1 = deg2rad(c.lon1);
+  const double lat0 = deg2rad(c.lat0), lat1 = deg2rad(c.lat1);
+  const double dlon = (lon1 - lon0) / ((double)c.nx);                    // coords.c:36
+  const double dlat = (lat1 - lat0) / ((double)ny);
+  auto latn = [&](int j) { return linspace_val(j, lat0, lat1, ny); };    // sw.h:116
+  auto latc = [&](int j) { return (latn(j) + latn(j - 1)) / 2.; };       // sw.h:117
+  rows.assign((size_t)R_NUM * H, 0.0);
+  auto R = [&](int t, int j) -> double& { return rows[(size_t)t * H + (j + 1)]; };
+  const double Dt = c.Dt;
+  for (int j = -1; j <= ny + 2; j++) {
+    const double lc = latc(j), ln = latn(j);
+    R(R_DXE, j) = dlon * rZ(p, lc);                                      // coords.c:60-65
+    R(R_DXC, j) = dlon * rZ(p, lc);
+    R(R_DXV, j) = dlon * rZ(p, ln);
+    R(R_DYN, j) = dlat * rM(p, lc);
+    R(R_DYC, j) = dlat * rM(p, latn(j - 1));
+    R(R_DYV, j) = dlat * rM(p, lc);
+    R(R_GE, j) = g_eff(p, lat2pclat(p, lc));                             // init.c:287-290
+    R(R_GN, j) = g_eff(p, lat2pclat(p, ln));
+    R(R_GC, j) = g_eff(p, lat2pclat(p, lc));
+    R(R_FE, j) = fcor(p, lc);                                            // init.c:292-295
+    R(R_FN, j) = fcor(p, ln);
+    R(R_RMC, j) = rM(p, lc);
+    R(R_RZC, j) = rZ(p, lc);
+    R(R_RMN, j) = rM(p, ln);
+    R(R_RZN, j) = rZ(p, ln);
+    R(R_SINC, j) = std::sin(lc);
+    R(R_SINN, j) = std::sin(ln);
+  }
+  for (int j = -1; j <= ny + 2; j++) {
+    R(R_KX, j) = R(R_RMC, j) / R(R_RZC, j);
+    R(R_KY, j) = R(R_RZN, j) / R(R_RMN, j);
+    R(R_KC, j) = 1.0 / (R(R_RMC, j) * R(R_RZC, j));
+    R(R_GEO, j) = Dt * R(R_SINC, j) / R(R_RZC, j);
+    R(R_IDXE, j) = 1.0 / R(R_DXE, j);
+    R(R_IDXC, j) = 1.0 / R(R_DXC, j);
+    R(R_IDXV, j) = 1.0 / R(R_DXV, j);
+    R(R_IDYN, j) = 1.0 / R(R_DYN, j);
+    R(R_IDYC, j) = 1.0 / R(R_DYC, j);
+    R(R_DTFE, j) = Dt * R(R_FE, j);
+    R(R_DTFN, j) = Dt * R(R_FN, j);
+    R(R_MGEDT, j) = -R(R_GE, j) * Dt;
+    R(R_MGNDT, j) = -R(R_GN, j) * Dt;
+    R(R_DXE2, j) = R(R_DXE, j) + R(R_DXE, j);
+    R(R_DYNS, j) = (j + 1 <= ny + 2) ? R(R_DYN, j) + R(R_DYN, j + 1) : 0.0;
+    R(R_SURF, j) = R(R_DXC, j) * R(R_DYC, j);
+  }
+  // compute_Dt fallback for a flow at rest (calc.c:715-725): depends on geometry only
+  double mx = 0, my = 0;
+  for (int j = 1; j <= ny; j++) {
+    double cx = std::sqrt((c.depth) * (R(R_GE, j))), cy = std::sqrt((c.depth) * (R(R_GN, j)));
+    if (std::fabs(cx / R(R_DXE, j)) > mx) mx = std::fabs(cx) / R(R_DXE, j);
+    if (std::fabs(cy / R(R_DYN, j)) > my) my = std::fabs(cy) / R(R_DYN, j);
+  }
+  *rest_mx = mx;
+  *rest_my = my;
+}
+
+}  // namespace sw2g

@@ -1,0 +1,572 @@
+// Reference-exact FP64 step: one kernel per reference routine, in core.c's
+// order (core.c:134-338). Compiled with -fmad=false so that no a*b+c is fused:
+// every expression below keeps the association of the reference expression it
+// restates, which makes the results bit-identical to the reference's own
+// single-rank run (divisions and square roots are IEEE-rounded by default).
+#include <cuda_runtime.h>
+
+#include "sw2g_internal.h"
+
+namespace sw2g {
+namespace {
+
+constexpr int TX = 128;
+
+__device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
+__device__ __forceinline__ double RW(const DevState& s, int t, int j) { return s.rows[t * s.H + j + 1]; }
+
+// calc.c:54-63 with sw.h:104-105 MIN/MAX as ternaries (NaN order as written).
+template <int SCH>
+__device__ __forceinline__ double limiter(double r) {
+#define MN(a, b) (((a) < (b)) ? (a) : (b))
+#define MX(a, b) (((a) > (b)) ? (a) : (b))
+  if constexpr (SCH == 0) return MX(0.0, MN(MN((1 + r) / 2.0, 2.0 * r), 2.0));
+  else if constexpr (SCH == 1) return MX(MX(0.0, MN(2.0 * r, 1.0)), MX(0.0, MN(r, 2.0)));
+  else if constexpr (SCH == 2) return MN(r, 1.0);
+  else if constexpr (SCH == 3) return (r + fabs(r)) / (1.0 + r);
+  else if constexpr (SCH == 4) return MX(0.0, MN(2.0 * r, MN((1 + 2.0 * r) / 3.0, 2.0)));
+  else if constexpr (SCH == 5) return (1.5 * (r * r + r)) / (r * r + r + 1.0);
+  else if constexpr (SCH == 6) return (r * r + r) / (r * r + 1.0);
+  else if constexpr (SCH == 7) return MX(0.0, MN(MN(2.0, 2.0 * r), MN(0.25 + 0.75 * r, 0.75 + 0.25 * r)));
+  else if constexpr (SCH == 8) return 0.0;
+  else if constexpr (SCH == 9) return 1.0;
+  else return (r == -1.0) ? 0.0 : (r + fabs(r)) / (1.0 + r);
+#undef MN
+#undef MX
+}
+
+// One face q0|q1 with outer neighbours qm, q2 (calc.c:41-49).
+template <int SCH>
+__device__ __forceinline__ void tvd_face(double qm, double q0, double q1, double q2, double cP, double cM,
+                                         double& BP, double& BM) {
+  const double d = q1 - q0;
+  const double rP = (d != 0) ? ((q0 - qm) / d) : 0.0;
+  const double rM = (d != 0) ? ((q2 - q1) / d) : 0.0;
+  BP = q0 + limiter<SCH>(rP) * 0.5 * (1 - cP) * d;
+  BM = q1 - limiter<SCH>(rM) * 0.5 * (1 + cM) * d;
+}
+
+// Sum C*B over the four faces in the reference's order (calc.c:100).
+template <int SCH>
+__device__ __forceinline__ double tvd_sum(const double* qx, const double* qy, double cwP, double cwM, double ceP,
+                                          double ceM, double csP, double csM, double cnP, double cnM) {
+  double wP, wM, eP, eM, sP, sM, nP, nM;
+  tvd_face<SCH>(qx[0], qx[1], qx[2], qx[3], cwP, cwM, wP, wM);
+  tvd_face<SCH>(qx[1], qx[2], qx[3], qx[4], ceP, ceM, eP, eM);
+  tvd_face<SCH>(qy[0], qy[1], qy[2], qy[3], csP, csM, sP, sM);
+  tvd_face<SCH>(qy[1], qy[2], qy[3], qy[4], cnP, cnM, nP, nM);
+  return cwP * wP + cwM * wM - ceP * eP - ceM * eM + csP * sP + csM * sM - cnP * nP - cnM * nM;
+}
+
+__device__ __forceinline__ double cpos(double a, double dt, double dx) { return 0.5 * (a + fabs(a)) * dt / dx; }
+__device__ __forceinline__ double cneg(double a, double dt, double dx) { return 0.5 * (a - fabs(a)) * dt / dx; }
+__device__ __forceinline__ double cpos2(double a, double b, double dt, double dx) {
+  return 0.5 * (0.5 * (a + fabs(a)) + 0.5 * (b + fabs(b))) * dt / dx;
+}
+__device__ __forceinline__ double cneg2(double a, double b, double dt, double dx) {
+  return 0.5 * (0.5 * (a - fabs(a)) + 0.5 * (b - fabs(b))) * dt / dx;
+}
+
+struct F7 {
+  const double *eta, *u, *v, *tr, *wx, *wy, *hb;
+};
+
+#define UW(i, j) (f.u[IX(W, i, j)] + f.wx[IX(W, i, j)])                   /* sw.h:216 */
+#define VW(i, j) (f.v[IX(W, i, j)] + f.wy[IX(W, i, j)])                   /* sw.h:217 */
+#define HH(i, j) (f.eta[IX(W, i, j)] + s.depth - f.hb[IX(W, i, j)])       /* sw.h:213 */
+
+#define INTERIOR_IJ                                   \
+  const int W = s.W;                                  \
+  const int i = blockIdx.x * TX + threadIdx.x + 1;    \
+  const int j = blockIdx.y + 1;                       \
+  if (i > s.nx) return;
+
+// BODYH + damping (calc.c:70-113)
+template <int SCH>
+__global__ void k_mass(DevState s, F7 f, double* out) {
+  INTERIOR_IJ
+  const double Dt = s.Dt, dxe = RW(s, R_DXE, j), dyn = RW(s, R_DYN, j);
+  double qx[5], qy[5];
+#pragma unroll
+  for (int o = -2; o <= 2; o++) { qx[o + 2] = HH(i + o, j); qy[o + 2] = HH(i, j + o); }
+  const double a = UW(i - 1, j), b = UW(i, j), c = VW(i, j - 1), d = VW(i, j);
+  double acc = tvd_sum<SCH>(qx, qy, cpos(a, Dt, dxe), cneg(a, Dt, dxe), cpos(b, Dt, dxe), cneg(b, Dt, dxe),
+                            cpos(c, Dt, dyn), cneg(c, Dt, dyn), cpos(d, Dt, dyn), cneg(d, Dt, dyn));
+  acc -= 2.0 * Dt * (s.sigma) * f.eta[IX(W, i, j)];
+  out[IX(W, i, j)] = acc;
+}
+
+// BODYTRACER (calc.c:117-163)
+template <int SCH>
+__global__ void k_tracer(DevState s, F7 f, double* out) {
+  INTERIOR_IJ
+  const double Dt = s.Dt, dxe = RW(s, R_DXE, j), dyn = RW(s, R_DYN, j);
+  double qx[5], qy[5];
+#pragma unroll
+  for (int o = -2; o <= 2; o++) { qx[o + 2] = f.tr[IX(W, i + o, j)]; qy[o + 2] = f.tr[IX(W, i, j + o)]; }
+  const double a = UW(i - 1, j), b = UW(i, j), c = VW(i, j - 1), d = VW(i, j);
+  const double pv1 = tvd_sum<SCH>(qx, qy, cpos(a, Dt, dxe), cneg(a, Dt, dxe), cpos(b, Dt, dxe), cneg(b, Dt, dxe),
+                                  cpos(c, Dt, dyn), cneg(c, Dt, dyn), cpos(d, Dt, dyn), cneg(d, Dt, dyn));
+  const double t = qx[2];
+  double pv2 = Dt * t * (b - a) / dxe;
+  pv2 += Dt * t * (d - c) / dyn;
+  double acc = pv1 + pv2;
+  acc -= 2.0 * Dt * (s.sigma_tr) * t;
+  out[IX(W, i, j)] = acc;
+}
+
+// BODYU (calc.c:168-200)
+template <int SCH>
+__global__ void k_adv_u(DevState s, F7 f, double* out) {
+  INTERIOR_IJ
+  const double Dt = s.Dt, dxc = RW(s, R_DXC, j), dyv = RW(s, R_DYV, j);
+  double qx[5], qy[5];
+#pragma unroll
+  for (int o = -2; o <= 2; o++) { qx[o + 2] = UW(i + o, j); qy[o + 2] = UW(i, j + o); }
+  const double uwm = qx[1], u0 = qx[2], uep = qx[3];
+  const double vs0 = VW(i, j - 1), vs1 = VW(i + 1, j - 1), vn0 = VW(i, j), vn1 = VW(i + 1, j);
+  const double p1 = tvd_sum<SCH>(qx, qy, cpos2(uwm, u0, Dt, dxc), cneg2(uwm, u0, Dt, dxc), cpos2(u0, uep, Dt, dxc),
+                                 cneg2(u0, uep, Dt, dxc), cpos2(vs0, vs1, Dt, dyv), cneg2(vs0, vs1, Dt, dyv),
+                                 cpos2(vn0, vn1, Dt, dyv), cneg2(vn0, vn1, Dt, dyv));
+  const double p2 = Dt * (u0 * (uep - uwm) / RW(s, R_DXE2, j) + u0 * ((vn0 + vn1) / 2. - (vs0 + vs1) / 2.) / dyv);
+  out[IX(W, i, j)] = p1 + p2;
+}
+
+// BODYV (calc.c:205-237)
+template <int SCH>
+__global__ void k_adv_v(DevState s, F7 f, double* out) {
+  INTERIOR_IJ
+  const double Dt = s.Dt, dxv = RW(s, R_DXV, j), dyc = RW(s, R_DYC, j);
+  double qx[5], qy[5];
+#pragma unroll
+  for (int o = -2; o <= 2; o++) { qx[o + 2] = VW(i + o, j); qy[o + 2] = VW(i, j + o); }
+  const double vsm = qy[1], v0 = qy[2], vnp = qy[3];
+  const double uw1 = UW(i - 1, j + 1), uw0 = UW(i - 1, j), ue1 = UW(i, j + 1), ue0 = UW(i, j);
+  const double p1 = tvd_sum<SCH>(qx, qy, cpos2(uw1, uw0, Dt, dxv), cneg2(uw1, uw0, Dt, dxv), cpos2(ue1, ue0, Dt, dxv),
+                                 cneg2(ue1, ue0, Dt, dxv), cpos2(vsm, v0, Dt, dyc), cneg2(vsm, v0, Dt, dyc),
+                                 cpos2(v0, vnp, Dt, dyc), cneg2(v0, vnp, Dt, dyc));
+  const double p2 = Dt * (v0 * ((ue0 + ue1) / 2. - (uw0 + uw1) / 2.) / dxv + v0 * (vnp - vsm) / RW(s, R_DYNS, j));
+  out[IX(W, i, j)] = p1 + p2;
+}
+
+// do_AdamsBashforth (calc.c:651-699) via copy_scaf/linop_scaf (sppde_core.c:247-298)
+__global__ void k_ab(DevState s, int k, double* ab, const double* dn, const double* dm1, const double* dm2) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  if (k == 0) {
+    ab[q] = dn[q];
+  } else if (k == 1) {
+    ab[q] = (3.0 / 2.0) * dn[q] + -(1.0 / 2.0) * dm1[q];
+  } else {
+    const double t = -(4.0 / 3.0) * dm1[q] + +(5.0 / 12.0) * dm2[q];
+    ab[q] = (23.0 / 12.0) * dn[q] + 1.0 * t;
+  }
+}
+
+// forall x += dx (core.c:175-177, 203-205)
+__global__ void k_add(DevState s, double* x, const double* dx) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  x[q] = x[q] + dx[q];
+}
+
+// laplacian_eta first pass (laplacian.c:120-123)
+__global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* xi) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  psi[q] = RW(s, R_KX, j) * (e[IX(W, i + 1, j)] - e[q]) / (RW(s, R_DXC, j));
+  xi[q] = RW(s, R_KY, j) * (e[IX(W, i, j + 1)] - e[q]) / (RW(s, R_DYC, j));
+}
+
+// laplacian_eta second pass (laplacian.c:125-127)
+__global__ void k_lape_pass2(DevState s, const double* psi, const double* xi, double* eo) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  eo[q] = RW(s, R_KC, j) * ((psi[q] - psi[IX(W, i - 1, j)]) / (RW(s, R_DXE, j)) +
+                            (xi[q] - xi[IX(W, i, j - 1)]) / (RW(s, R_DYN, j)));
+}
+
+// laplacian_eta wall rows after its halo update (laplacian.c:131-146)
+__global__ void k_lape_fix(int nx, int ny, double* eo) {
+  const int W = nx + 4;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > nx) return;
+  eo[IX(W, i, ny + 1)] = eo[IX(W, i, ny)];
+  eo[IX(W, i, ny + 2)] = eo[IX(W, i, ny + 1)];
+  eo[IX(W, i, 0)] = eo[IX(W, i, 1)];
+}
+
+// Deta_n += nu*Dt*L (calc.c:346-350); Du/Dv the same (core.c:258-266)
+__global__ void k_hyper_add(DevState s, double* d, const double* l2, const double* l4, const double* l6) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  double x = d[q];
+  x += (s.nu2) * (s.Dt) * l2[q];
+  x += (s.nu4) * (s.Dt) * l4[q];
+  x += (s.nu6) * (s.Dt) * l6[q];
+  d[q] = x;
+}
+
+// do_eta_geofactor (calc.c:403-422)
+__global__ void k_geofactor(DevState s, F7 f, double* ab) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  ab[q] -= (RW(s, R_GEO, j) * HH(i, j) * 0.5 * (VW(i, j) + VW(i, j - 1)));
+}
+
+// solve_pres_u/v + new_vels + dissipation_effect (core.c:217-231; calc.c:500-540, 357-400)
+__global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* dvadv, double* dun, double* dvn) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  const double* e = f.eta;
+  const double dup = RW(s, R_MGEDT, j) * (e[IX(W, i + 1, j)] - e[q]) / RW(s, R_DXC, j);
+  const double dvp = RW(s, R_MGNDT, j) * (e[IX(W, i, j + 1)] - e[q]) / RW(s, R_DYC, j + 1);
+  double a = duadv[q] + dup;
+  double b = dvadv[q] + dvp;
+  a -= f.u[q] * s.sigma * s.Dt;
+  b -= f.v[q] * s.sigma * s.Dt;
+  dun[q] = a;
+  dvn[q] = b;
+}
+
+// laplacian_vels first pass (laplacian.c:59-65)
+__global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, double* ze, double* di) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  double a = RW(s, R_IDXV, j), b = -RW(s, R_IDYC, j + 1);
+  ze[q] = a * ((vv[IX(W, i + 1, j)] - vv[q]) + b * (RW(s, R_DXC, j + 1) * uu[IX(W, i, j + 1)] - RW(s, R_DXC, j) * uu[q]));
+  a = RW(s, R_IDXE, j);
+  b = RW(s, R_IDYN, j);
+  di[q] = a * ((uu[q] - uu[IX(W, i - 1, j)]) + b * (RW(s, R_DXV, j) * vv[q] - RW(s, R_DXV, j - 1) * vv[IX(W, i, j - 1)]));
+}
+
+// laplacian_vels wall fix after the halo update of dseta/div (laplacian.c:70-81)
+__global__ void k_lapv_fix1(DevState s, const double* uu, double* ze, double* di) {
+  const int W = s.W, ny = s.ny;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > s.nx) return;
+  di[IX(W, i, ny + 1)] = (uu[IX(W, i, ny)] - uu[IX(W, i - 1, ny)]) / RW(s, R_DXE, ny);
+  ze[IX(W, i, 0)] = 0;
+}
+
+// laplacian_vels second pass (laplacian.c:83-89)
+__global__ void k_lapv_pass2(DevState s, const double* ze, const double* di, double* lu, double* lv) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  double a = -RW(s, R_IDYN, j), b = RW(s, R_IDXC, j);
+  lu[q] = a * (ze[q] - ze[IX(W, i, j - 1)]) + b * (di[IX(W, i + 1, j)] - di[q]);
+  a = RW(s, R_IDXV, j);
+  b = RW(s, R_IDYC, j + 1);
+  lv[q] = a * (ze[q] - ze[IX(W, i - 1, j)]) + b * (di[IX(W, i, j + 1)] - di[q]);
+}
+
+// laplacian_vels wall fix of the outputs (laplacian.c:94-107)
+__global__ void k_lapv_fix2(int nx, int ny, double* lu, double* lv) {
+  const int W = nx + 4;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > nx) return;
+  lu[IX(W, i, ny + 1)] = lu[IX(W, i, ny)];
+  lv[IX(W, i, ny + 1)] = 0;
+  lu[IX(W, i, 0)] = lu[IX(W, i, 1)];
+  lv[IX(W, i, 0)] = 0;
+}
+
+// solve_Coriolis_u (calc.c:542-569), in place
+__global__ void k_coriolis_u(DevState s, double* u, const double* v, const double* duab) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
+  const double al = RW(s, R_DTFE, j) + (s.Dt * u[q] * RW(s, R_SINC, j)) / RW(s, R_RZC, j);
+  const double be = 0.25 * al * al;
+  u[q] = (u[q] + duab[q] - be * u[q] + al * semi) / (1.0 + be);
+}
+
+// solve_Coriolis_v (calc.c:571-598), in place, reading the new u interior
+__global__ void k_coriolis_v(DevState s, const double* u, double* v, const double* dvab) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
+  const double al = RW(s, R_DTFN, j) + (s.Dt * semi * RW(s, R_SINN, j)) / RW(s, R_RZN, j);
+  const double be = 0.25 * al * al;
+  v[q] = (v[q] + dvab[q] - be * v[q] - al * semi) / (1.0 + be);
+}
+
+// Single-rank halo update (sppde_hupdate.c:274-342). The y pass then the x pass
+// compose to: every halo cell copies the interior cell (wrapx(i), wrapy(j)).
+__global__ void k_halo(double* x, int nx, int ny) {
+  const int W = nx + 4;
+  const int nh = 4 * W + 4 * ny;  // 4 full halo rows + 4 halo columns over interior rows
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nh) return;
+  int i, j;
+  if (t < 4 * W) {
+    const int r = t / W;
+    i = t - r * W - 1;
+    j = (r < 2) ? r - 1 : ny + r - 1;  // rows -1, 0, ny+1, ny+2
+  } else {
+    const int u = t - 4 * W;
+    const int c = u / ny;
+    j = u - c * ny + 1;
+    i = (c < 2) ? c - 1 : nx + c - 1;  // columns -1, 0, nx+1, nx+2
+  }
+  const int si = (i < 1) ? i + nx : ((i > nx) ? i - nx : i);
+  const int sj = (j < 1) ? j + ny : ((j > ny) ? j - ny : j);
+  x[IX(W, i, j)] = x[IX(W, si, sj)];
+}
+
+// do_channel (calc.c:600-649), polar 0: interior columns of the wall rows
+__global__ void k_channel(int nx, int ny, double* u, double* v, double* wx, double* wy) {
+  const int W = nx + 4;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (i > nx) return;
+  v[IX(W, i, 0)] = 0; v[IX(W, i, -1)] = 0;
+  wy[IX(W, i, 0)] = 0; wy[IX(W, i, -1)] = 0;
+  u[IX(W, i, 0)] = u[IX(W, i, 1)]; u[IX(W, i, -1)] = u[IX(W, i, 0)];
+  wx[IX(W, i, 0)] = wx[IX(W, i, 1)]; wx[IX(W, i, -1)] = wx[IX(W, i, 0)];
+  v[IX(W, i, ny)] = 0; v[IX(W, i, ny + 1)] = 0; v[IX(W, i, ny + 2)] = 0;
+  wy[IX(W, i, ny)] = 0; wy[IX(W, i, ny + 1)] = 0; wy[IX(W, i, ny + 2)] = 0;
+  u[IX(W, i, ny + 1)] = u[IX(W, i, ny)]; u[IX(W, i, ny + 2)] = u[IX(W, i, ny + 1)];
+  wx[IX(W, i, ny + 1)] = wx[IX(W, i, ny)]; wx[IX(W, i, ny + 2)] = wx[IX(W, i, ny + 1)];
+}
+
+// compute_Dt maxima (calc.c:705-712): max |u+wx|/DXE and |v+wy|/DYN over the
+// interior; NaNs never win the comparison, as in the reference's loop.
+__global__ void k_cfl(DevState s, F7 f, unsigned long long* out) {
+  const int W = s.W;
+  const int i = blockIdx.x * TX + threadIdx.x + 1;
+  const int j = blockIdx.y + 1;
+  double mx = 0, my = 0;
+  if (i <= s.nx) {
+    const double ax = fabs(UW(i, j)) / RW(s, R_DXE, j);
+    const double ay = fabs(VW(i, j)) / RW(s, R_DYN, j);
+    mx = (ax > mx) ? ax : mx;
+    my = (ay > my) ? ay : my;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ox = __shfl_xor_sync(0xffffffffu, mx, o), oy = __shfl_xor_sync(0xffffffffu, my, o);
+    mx = (ox > mx) ? ox : mx;
+    my = (oy > my) ? oy : my;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
+    if (my > 0) atomicMax(out + 1, (unsigned long long)__double_as_longlong(my));
+  }
+}
+
+// check_stats_scaf (sppde_core.c:346-395) as the reference evaluates it: min and
+// max start from the first interior value and skip NaNs after it, so the step
+// aborts iff the first value is not finite or some value lies outside +-1e10.
+__global__ void k_range(DevState s, const double* x, int* bad) {
+  INTERIOR_IJ
+  const double r = x[IX(W, i, j)];
+  bool b = (r < -1e10) || (r > 1e10);
+  if (i == 1 && j == 1) b = b || !isfinite(r);
+  if (b) atomicOr(bad, 1);
+}
+
+#undef UW
+#undef VW
+#undef HH
+
+template <int SCH>
+void launch_bodies(int which, dim3 g, cudaStream_t st, const DevState& s, const F7& f, double* out) {
+  if (which == 0) k_mass<SCH><<<g, TX, 0, st>>>(s, f, out);
+  else if (which == 1) k_tracer<SCH><<<g, TX, 0, st>>>(s, f, out);
+  else if (which == 2) k_adv_u<SCH><<<g, TX, 0, st>>>(s, f, out);
+  else k_adv_v<SCH><<<g, TX, 0, st>>>(s, f, out);
+}
+
+void body(int which, int sch, dim3 g, cudaStream_t st, const DevState& s, const F7& f, double* out) {
+  switch (sch) {
+    case 0: launch_bodies<0>(which, g, st, s, f, out); break;
+    case 1: launch_bodies<1>(which, g, st, s, f, out); break;
+    case 2: launch_bodies<2>(which, g, st, s, f, out); break;
+    case 3: launch_bodies<3>(which, g, st, s, f, out); break;
+    case 4: launch_bodies<4>(which, g, st, s, f, out); break;
+    case 5: launch_bodies<5>(which, g, st, s, f, out); break;
+    case 6: launch_bodies<6>(which, g, st, s, f, out); break;
+    case 7: launch_bodies<7>(which, g, st, s, f, out); break;
+    case 8: launch_bodies<8>(which, g, st, s, f, out); break;
+    case 9: launch_bodies<9>(which, g, st, s, f, out); break;
+    default: launch_bodies<kVanLeerSafe>(which, g, st, s, f, out); break;
+  }
+}
+
+void rotate3(double** h) {
+  double* t = h[2];
+  h[2] = h[1];
+  h[1] = h[0];
+  h[0] = t;
+}
+
+}  // namespace
+
+void halo_wrap(double* x, int nx, int ny, cudaStream_t st) {
+  const int nh = 4 * (nx + 4) + 4 * ny;
+  k_halo<<<(nh + 255) / 256, 256, 0, st>>>(x, nx, ny);
+}
+
+// One reference time step; returns the number of kernels launched.
+int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
+              cudaStream_t st, Timers* tm) {
+#define LAUNCH(tag, ...)                          \
+  do {                                            \
+    if (tm && tm->on) tm->begin(tag, st);         \
+    __VA_ARGS__;                                  \
+    if (tm && tm->on) tm->end(st);                \
+    nl++;                                         \
+  } while (0)
+  const dim3 g((s.nx + TX - 1) / TX, s.ny);
+  const int gw = (s.nx + 127) / 128;
+  const size_t bytes = sizeof(double) * (size_t)s.W * s.H;
+  int nl = 0;
+  auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
+  const bool hyper = (s.nu2 != 0 || s.nu4 != 0 || s.nu6 != 0);
+
+  // compute_Dt (core.c:155-159): maxima at the start of the step
+  LAUNCH("cfl", k_cfl<<<g, TX, 0, st>>>(s, F(), chk.cfl + 2 * slot));
+
+  // tracer (core.c:161-182); skipped while the tracer is identically +0, which
+  // the step then provably leaves unchanged
+  if (tracer) {
+    LAUNCH("tracer", body(1, sch, g, st, s, F(), b.dtr[0]));
+    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.dtrAB, b.dtr[0], b.dtr[1], b.dtr[2]));
+    rotate3(b.dtr);
+    LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[3], b.dtrAB));
+    LAUNCH("halo", halo_wrap(b.f[3], s.nx, s.ny, st));
+  }
+
+  // mass (core.c:184-210; calc.c:289-355)
+  LAUNCH("mass", body(0, sch, g, st, s, F(), b.deta[0]));
+  if (hyper) {
+    const double* src = b.f[1];  // the reference passes u, not eta (calc.c:332)
+    for (int q = 0; q < 3; q++) cudaMemsetAsync(b.Le[q], 0, bytes, st);
+    const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
+    for (int q = 0; q < nlap; q++) {
+      cudaMemsetAsync(b.psi, 0, bytes, st);
+      cudaMemsetAsync(b.xi, 0, bytes, st);
+      LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
+      LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
+      LAUNCH("halo", halo_wrap(b.Le[q], s.nx, s.ny, st));
+      LAUNCH("lape_fix", k_lape_fix<<<gw, 128, 0, st>>>(s.nx, s.ny, b.Le[q]));
+    }
+    LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
+  }
+  LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
+  LAUNCH("geofactor", k_geofactor<<<g, TX, 0, st>>>(s, F(), b.detaAB));
+  rotate3(b.deta);
+  LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[0], b.detaAB));
+  LAUNCH("halo", halo_wrap(b.f[0], s.nx, s.ny, st));
+
+  // momentum (core.c:212-280)
+  LAUNCH("adv_u", body(2, sch, g, st, s, F(), b.duadv));
+  LAUNCH("adv_v", body(3, sch, g, st, s, F(), b.dvadv));
+  LAUNCH("pres_sum", k_pres_sum<<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
+  if (hyper) {
+    for (int q = 0; q < 6; q++) cudaMemsetAsync(b.L[q], 0, bytes, st);
+    const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
+    for (int q = 0; q < nlap; q++) {
+      const double* uu = q == 0 ? b.f[1] : b.L[2 * q - 2];
+      const double* vv = q == 0 ? b.f[2] : b.L[2 * q - 1];
+      cudaMemsetAsync(b.ze, 0, bytes, st);
+      cudaMemsetAsync(b.di, 0, bytes, st);
+      LAUNCH("lapv_pass1", k_lapv_pass1<<<g, TX, 0, st>>>(s, uu, vv, b.ze, b.di));
+      LAUNCH("halo", halo_wrap(b.ze, s.nx, s.ny, st));
+      LAUNCH("halo", halo_wrap(b.di, s.nx, s.ny, st));
+      LAUNCH("lapv_fix1", k_lapv_fix1<<<gw, 128, 0, st>>>(s, uu, b.ze, b.di));
+      LAUNCH("lapv_pass2", k_lapv_pass2<<<g, TX, 0, st>>>(s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
+      LAUNCH("halo", halo_wrap(b.L[2 * q], s.nx, s.ny, st));
+      LAUNCH("halo", halo_wrap(b.L[2 * q + 1], s.nx, s.ny, st));
+      LAUNCH("lapv_fix2", k_lapv_fix2<<<gw, 128, 0, st>>>(s.nx, s.ny, b.L[2 * q], b.L[2 * q + 1]));
+    }
+    LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.du[0], b.L[0], b.L[2], b.L[4]));
+    LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.dv[0], b.L[1], b.L[3], b.L[5]));
+  }
+  LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.duAB, b.du[0], b.du[1], b.du[2]));
+  LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.dvAB, b.dv[0], b.dv[1], b.dv[2]));
+  rotate3(b.du);
+  rotate3(b.dv);
+
+  // Coriolis (core.c:282-285)
+  LAUNCH("coriolis_u", k_coriolis_u<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.duAB));
+  LAUNCH("coriolis_v", k_coriolis_v<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dvAB));
+
+  // halos and walls (core.c:287-307); the tracer and eta refresh is idempotent
+  LAUNCH("halo", halo_wrap(b.f[1], s.nx, s.ny, st));
+  LAUNCH("halo", halo_wrap(b.f[2], s.nx, s.ny, st));
+  LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
+
+  // range checks of tracer, eta, u, v (core.c:309-312)
+  const int order[4] = {3, 0, 1, 2};
+  for (int q = 0; q < 4; q++) {
+    if (order[q] == 3 && !tracer) continue;  // an all-zero tracer passes trivially
+    LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, b.f[order[q]], chk.bad + slot));
+  }
+  return nl;
+#undef LAUNCH
+}
+
+// Energy per interior row (energy.c:36-41), compensated (Neumaier) over i.
+__global__ void k_energy_rows(DevState s, F7 f, double* out) {
+  const int W = s.W;
+  const int j = blockIdx.x + 1;
+  double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+  const double surf = RW(s, R_SURF, j), gc = RW(s, R_GC, j), depth = s.depth;
+  for (int i = threadIdx.x + 1; i <= s.nx; i += blockDim.x) {
+#define UW(i, j) (f.u[IX(W, i, j)] + f.wx[IX(W, i, j)])
+#define VW(i, j) (f.v[IX(W, i, j)] + f.wy[IX(W, i, j)])
+#define HH(i, j) (f.eta[IX(W, i, j)] + s.depth - f.hb[IX(W, i, j)])
+    const double uc = 0.5 * (UW(i, j) + UW(i - 1, j));
+    const double vc = 0.5 * (VW(i, j) + VW(i, j - 1));
+    const double w0 = f.wx[IX(W, i, j)], w1 = f.wy[IX(W, i, j)];
+    const double h = HH(i, j);
+    const double term[3] = {0.5 * h * (uc * uc + vc * vc) * surf - 0.5 * ((w0 * w0) + (w1 * w1)) * surf,
+                            0.5 * gc * (h * h) * surf - 0.5 * gc * (depth * depth) * surf, h * surf};
+#undef UW
+#undef VW
+#undef HH
+    for (int c = 0; c < 3; c++) {
+      const double t = acc[c] + term[c];
+      cmp[c] += (fabs(acc[c]) >= fabs(term[c])) ? ((acc[c] - t) + term[c]) : ((term[c] - t) + acc[c]);
+      acc[c] = t;
+    }
+  }
+  __shared__ double sh[3][2][256];
+  for (int c = 0; c < 3; c++) { sh[c][0][threadIdx.x] = acc[c]; sh[c][1][threadIdx.x] = cmp[c]; }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int c = threadIdx.x;
+    double a = 0, e = 0;
+    for (int t = 0; t < (int)blockDim.x; t++) {
+      const double term = sh[c][0][t];
+      const double u = a + term;
+      e += (fabs(a) >= fabs(term)) ? ((a - u) + term) : ((term - u) + a);
+      a = u;
+      e += sh[c][1][t];
+    }
+    out[3 * (j - 1) + c] = a + e;
+  }
+}
+
+__global__ void k_energy_sum(const double* rows, int ny, double* out) {
+  const int c = threadIdx.x;
+  if (c >= 3) return;
+  double a = 0, e = 0;
+  for (int j = 0; j < ny; j++) {
+    const double term = rows[3 * j + c];
+    const double u = a + term;
+    e += (fabs(a) >= fabs(term)) ? ((a - u) + term) : ((term - u) + a);
+    a = u;
+  }
+  out[c] = a + e;
+}
+
+void energy_rows(const DevState& s, const double* const* f, double* row_out, cudaStream_t st) {
+  k_energy_rows<<<s.ny, 256, 0, st>>>(s, F7{f[0], f[1], f[2], f[3], f[4], f[5], f[6]}, row_out);
+}
+
+void energy_sum(const double* row_in, int ny, double* out3, cudaStream_t st) {
+  k_energy_sum<<<1, 32, 0, st>>>(row_in, ny, out3);
+}
+
+}  // namespace sw2g

@@ -1,0 +1,105 @@
+// Internal declarations shared by the sw2g translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "sw2g.h"
+
+namespace sw2g {
+
+// Per-row tables (one value per latitude row j = -1..ny+2, stored at j+1).
+// The first group restates the reference's metric and physics fields, which
+// for polar 0 depend on j only (coords.c:35-96, init.c:279-297, sw.h:174-193);
+// the second holds per-row subexpressions that the reference evaluates per
+// cell with identical operands, precomputed here with the same operations.
+enum Row {
+  R_DXE, R_DXC, R_DXV, R_DYN, R_DYC, R_DYV,
+  R_GE, R_GN, R_GC, R_FE, R_FN,
+  R_RMC, R_RZC, R_RMN, R_RZN, R_SINC, R_SINN,
+  R_KX,    // rM(latc)/rZ(latc)            laplacian.c:121
+  R_KY,    // rZ(latn)/rM(latn)            laplacian.c:122
+  R_KC,    // 1.0/(rM(latc)*rZ(latc))      laplacian.c:126
+  R_GEO,   // Dt*sin(latc)/rZ(latc)        calc.c:419
+  R_IDXE, R_IDXC, R_IDXV, R_IDYN, R_IDYC,  // 1.0/x   laplacian.c:60-87
+  R_DTFE,  // Dt*FE                        calc.c:563
+  R_DTFN,  // Dt*FN                        calc.c:592
+  R_MGEDT, // -GE*Dt                       calc.c:517
+  R_MGNDT, // -GN*Dt                       calc.c:538
+  R_DXE2,  // DXE+DXE                      calc.c:197
+  R_DYNS,  // DYN(j)+DYN(j+1)              calc.c:234
+  R_SURF,  // DXC*DYC                      energy.c:40
+  R_NUM
+};
+
+// Internal limiter index: 0..9 as the reference, 10 = Van Leer made safe at r = -1.
+constexpr int kVanLeerSafe = 10;
+
+struct DevState {
+  int nx, ny, W, H;  // W = nx+4 (row pitch), H = ny+4
+  const double* rows;  // R_NUM * H
+  double depth, Dt, sigma, sigma_tr, nu2, nu4, nu6;
+};
+
+struct Ctx;
+
+// Host geometry (geometry.cpp): fills rows[R_NUM*H]; returns the at-rest CFL
+// maxima used by compute_Dt when the flow is at rest (calc.c:715-725).
+void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, double* rest_my);
+
+// FP64 reference-exact step (step_fp64.cu).
+struct Fp64Buffers {
+  double* f[7];  // eta u v tracer windx windy hB (padded)
+  double* deta[3]; double* du[3]; double* dv[3]; double* dtr[3];
+  double* detaAB; double* duAB; double* dvAB; double* dtrAB;
+  double* duadv; double* dvadv;
+  double* Le[3]; double* L[6];
+  double* psi; double* xi; double* ze; double* di;
+};
+
+struct StepChecks {
+  unsigned long long* cfl;  // 2 per step: bit patterns of max|u|/dx, max|v|/dy
+  int* bad;                 // 1 per step: range check failed
+};
+
+// Named device timers (the role of the reference's cr_start/cr_end channels,
+// sppde_cr.c:38-217): while enabled, every tagged launch is bracketed by a
+// pair of CUDA events on the launching stream; collect() (after the stream has
+// been synchronised) adds the elapsed times per tag.
+class Timers {
+ public:
+  struct Entry {
+    const char* name;
+    long long launches;
+    double ms;
+  };
+  bool on = false;
+  void begin(const char* tag, cudaStream_t st);
+  void end(cudaStream_t st);
+  void collect();
+  void reset();
+  void release();
+  const std::vector<Entry>& entries() const { return entries_; }
+
+ private:
+  struct Pending {
+    int entry;
+    cudaEvent_t a, b;
+  };
+  cudaEvent_t take();
+  std::vector<cudaEvent_t> free_;
+  std::vector<Pending> pending_;
+  std::vector<Entry> entries_;
+  int open_ = -1;
+  cudaEvent_t open_ev_ = nullptr;
+};
+
+int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int step_slot,
+              cudaStream_t st, Timers* tm);
+void halo_wrap(double* x, int nx, int ny, cudaStream_t st);
+void energy_rows(const DevState& s, const double* const* f, double* row_out, cudaStream_t st);
+void energy_sum(const double* row_in, int ny, double* out3, cudaStream_t st);
+
+}  // namespace sw2g

@@ -1,0 +1,204 @@
+"""ctypes binding of libsw2g.so (the C ABI in include/sw2g.h).
+
+There is no fallback: if the library is missing or no GPU is present, every
+call raises. `Solver` mirrors the reference's step interface: create from the
+parsed case, upload the fields in the reference's padded layout, step, read
+back, and query the energy diagnostic.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .formats import CaseParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsw2g.so")
+
+OK, ERR_BAD_ARG, ERR_CFL, ERR_NONFINITE, ERR_TIMEOUT, ERR_CUDA, ERR_NOMEM, ERR_STATE = range(8)
+FP64, FP32 = 0, 1
+FLAG_VANLEER_SAFE = 0x1
+UPLOAD_RAW, UPLOAD_FRAME, UPLOAD_CONTINUE = 0, 1, 2
+
+SYMBOLS = [
+    "sw2g_status_string", "sw2g_create", "sw2g_upload", "sw2g_step", "sw2g_error_step", "sw2g_download",
+    "sw2g_diag", "sw2g_reset_ab", "sw2g_steps_done", "sw2g_device_field", "sw2g_stream", "sw2g_last_launches",
+    "sw2g_destroy", "sw2g_last_step_ms", "sw2g_timers_enable", "sw2g_timers_reset", "sw2g_timers_count",
+    "sw2g_timer_read",
+]
+
+
+class Case(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("sch", ctypes.c_int),
+                ("lon0", ctypes.c_double), ("lon1", ctypes.c_double),
+                ("lat0", ctypes.c_double), ("lat1", ctypes.c_double),
+                ("Omega", ctypes.c_double), ("rE", ctypes.c_double), ("rP", ctypes.c_double),
+                ("gE", ctypes.c_double), ("depth", ctypes.c_double),
+                ("Dt", ctypes.c_double), ("courant", ctypes.c_double),
+                ("tau", ctypes.c_double), ("tracer_dis", ctypes.c_double),
+                ("hypernu", ctypes.c_double * 3), ("flags", ctypes.c_uint)]
+
+
+class SW2GError(RuntimeError):
+    def __init__(self, code, what, step=-1):
+        super().__init__(f"{what}: {status_string(code)} (status {code}, step {step})")
+        self.code = code
+        self.step = step
+
+
+_lib = None
+
+
+def load():
+    """Load the library (no rebuild, no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} not built: run `python -m sw2_gb300.build`")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+        L.sw2g_status_string.restype = ctypes.c_char_p
+        L.sw2g_status_string.argtypes = [ctypes.c_int]
+        L.sw2g_create.argtypes = [ctypes.POINTER(Case), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.sw2g_upload.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int]
+        L.sw2g_step.argtypes = [vp, ctypes.c_int]
+        L.sw2g_error_step.argtypes = [vp]
+        L.sw2g_download.argtypes = [vp, dp, dp, dp, dp]
+        L.sw2g_diag.argtypes = [vp, dp, dp, dp]
+        L.sw2g_reset_ab.argtypes = [vp]
+        L.sw2g_steps_done.restype = ctypes.c_longlong
+        L.sw2g_steps_done.argtypes = [vp]
+        L.sw2g_device_field.restype = vp
+        L.sw2g_device_field.argtypes = [vp, ctypes.c_int]
+        L.sw2g_stream.restype = vp
+        L.sw2g_stream.argtypes = [vp]
+        L.sw2g_last_launches.restype = ctypes.c_longlong
+        L.sw2g_last_launches.argtypes = [vp]
+        L.sw2g_destroy.argtypes = [vp]
+        L.sw2g_last_step_ms.restype = ctypes.c_double
+        L.sw2g_last_step_ms.argtypes = [vp]
+        L.sw2g_timers_enable.argtypes = [vp, ctypes.c_int]
+        L.sw2g_timers_reset.argtypes = [vp]
+        L.sw2g_timers_reset.restype = None
+        L.sw2g_timers_count.argtypes = [vp]
+        L.sw2g_timer_read.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                      ctypes.POINTER(ctypes.c_longlong), dp]
+        _lib = L
+    return _lib
+
+
+def status_string(code: int) -> str:
+    return load().sw2g_status_string(int(code)).decode()
+
+
+def case_struct(p: CaseParams, flags: int = 0) -> Case:
+    c = Case()
+    c.nx, c.ny, c.sch = p.nx, p.ny, p.sch
+    c.lon0, c.lon1, c.lat0, c.lat1 = p.lon0, p.lon1, p.lat0, p.lat1
+    c.Omega, c.rE, c.rP, c.gE, c.depth = p.Omega, p.rE, p.rP, p.gE, p.depth
+    c.Dt, c.courant, c.tau, c.tracer_dis = p.Dt, p.CFL, p.Tau, p.TracerDis
+    for k in range(3):
+        c.hypernu[k] = p.hypernu[k]
+    c.flags = flags
+    return c
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Solver:
+    """One GPU run of a case (a sw2g context)."""
+
+    def __init__(self, params: CaseParams, precision: int = FP64, device: int = 0, flags: int = 0):
+        self.params = params
+        self.nx, self.ny = params.nx, params.ny
+        self._c = case_struct(params, flags)
+        h = ctypes.c_void_p()
+        rc = load().sw2g_create(ctypes.byref(self._c), precision, device, ctypes.byref(h))
+        if rc != OK:
+            raise SW2GError(rc, "sw2g_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sw2g_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc, what):
+        if rc != OK:
+            raise SW2GError(rc, what, load().sw2g_error_step(self.h))
+
+    def _arr(self, a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.shape != (self.ny + 4, self.nx + 4):
+            raise ValueError(f"field shape {a.shape} != {(self.ny + 4, self.nx + 4)}")
+        return a
+
+    def upload(self, eta, u, v, tracer=None, windx=None, windy=None, hB=None, mode=UPLOAD_FRAME):
+        arrs = [self._arr(a) for a in (eta, u, v, tracer, windx, windy, hB)]
+        self._keep = arrs
+        self._check(load().sw2g_upload(self.h, *[_ptr(a) for a in arrs], mode), "sw2g_upload")
+
+    def step(self, n: int):
+        """Advance n steps; returns the status code (raises only on CUDA/argument errors)."""
+        rc = load().sw2g_step(self.h, int(n))
+        if rc in (OK, ERR_CFL, ERR_NONFINITE):
+            return rc
+        self._check(rc, "sw2g_step")
+
+    def error_step(self) -> int:
+        return load().sw2g_error_step(self.h)
+
+    def steps_done(self) -> int:
+        return load().sw2g_steps_done(self.h)
+
+    def last_launches(self) -> int:
+        return load().sw2g_last_launches(self.h)
+
+    def download(self):
+        out = [np.empty((self.ny + 4, self.nx + 4)) for _ in range(4)]
+        self._check(load().sw2g_download(self.h, *[_ptr(a) for a in out]), "sw2g_download")
+        return dict(zip(("eta", "u", "v", "tracer"), out))
+
+    def diag(self):
+        k, a, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(load().sw2g_diag(self.h, ctypes.byref(k), ctypes.byref(a), ctypes.byref(m)), "sw2g_diag")
+        return k.value, a.value, m.value
+
+    def reset_ab(self):
+        self._check(load().sw2g_reset_ab(self.h), "sw2g_reset_ab")
+
+    def last_step_ms(self) -> float:
+        return load().sw2g_last_step_ms(self.h)
+
+    def timers(self, on: bool = True):
+        self._check(load().sw2g_timers_enable(self.h, 1 if on else 0), "sw2g_timers_enable")
+
+    def timers_reset(self):
+        load().sw2g_timers_reset(self.h)
+
+    def timer_table(self):
+        """{kernel name: (launches, total ms)} accumulated while timers were on."""
+        out = {}
+        for i in range(load().sw2g_timers_count(self.h)):
+            nm, n, ms = ctypes.c_char_p(), ctypes.c_longlong(), ctypes.c_double()
+            self._check(load().sw2g_timer_read(self.h, i, ctypes.byref(nm), ctypes.byref(n), ctypes.byref(ms)),
+                        "sw2g_timer_read")
+            out[nm.value.decode()] = (n.value, ms.value)
+        return out
+
+    def device_field(self, which: int) -> int:
+        return load().sw2g_device_field(self.h, which)
+
+    def stream(self) -> int:
+        return load().sw2g_stream(self.h)

@@ -1,0 +1,166 @@
+"""Parity of the FP64 CUDA step (through the C ABI) with the reference.
+
+Bar: bit-identical. Every padded cell of eta, u, v and tracer (halos included)
+must equal the CPU oracle's, and the interiors must equal the frames the
+reference itself wrote (tests/golden). Energy diagnostics use compensated
+sums instead of the reference's sequential ones: relative tolerance 1e-12.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from sw2_gb300 import cases, lib
+from tests import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("eta", "u", "v", "tracer")
+
+
+def same(a, b):
+    """Bitwise-equal up to the sign of zero (NaNs equal to NaNs)."""
+    return np.array_equal(a, b, equal_nan=True)
+
+
+def run_both(case, nsteps, flags=0, chunk=None):
+    s = lib.Solver(case.params, flags=flags)
+    s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    o = orc.Oracle(case.params)
+    o.load(case.fields())
+    chunk = chunk or nsteps
+    done = 0
+    while done < nsteps:
+        n = min(chunk, nsteps - done)
+        assert s.step(n) == lib.OK
+        rc, bad = o.step(n)
+        assert rc == 0, (rc, bad)
+        done += n
+    return s, o
+
+
+@pytest.mark.parametrize("name", gc.array_cases())
+def test_gpu_matches_reference_frames(name):
+    entry, case, frames = gc.load_case(name)
+    s = lib.Solver(case.params)
+    s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    for fr in frames:
+        assert s.step(entry["save_every"]) == lib.OK
+        got = s.download()
+        for k in FIELDS:
+            g = got[k][2:-2, 2:-2]
+            assert np.array_equal(g, fr[k]), f"{k}: max|d|={np.max(np.abs(g - fr[k]))}"
+
+
+@pytest.mark.parametrize("sch", range(10))
+def test_gpu_matches_oracle_all_cells(sch):
+    flags = lib.FLAG_VANLEER_SAFE if sch == 3 else 0
+    case = cases.make_case(nx=61, ny=29, sch=sch, seed=100 + sch, bumps=2, tracer=(sch % 2 == 0),
+                           TracerDis=1e-6, Tau=2e6 if sch % 3 == 0 else 1e20)
+    if sch == 3:
+        pytest.skip("reference Van Leer aborts; safe variant is covered separately")
+    s, o = run_both(case, 25, flags=flags, chunk=7)
+    got = s.download()
+    for k in FIELDS:
+        assert same(got[k], o.field(k)), k
+
+
+@pytest.mark.parametrize("nx,ny", [(3, 3), (4, 5), (129, 7), (257, 33)])
+def test_gpu_matches_oracle_odd_sizes(nx, ny):
+    case = cases.make_case(nx=nx, ny=ny, sch=1, seed=7, bumps=1, sigma_km=(8000.0, 8000.0))
+    nu4 = case.params.hypernu[1]
+    case.params.hypernu = (1e-3 * nu4 ** 0.5, nu4, 1e-4 * nu4 ** 1.5)
+    s, o = run_both(case, 12, chunk=5)
+    got = s.download()
+    for k in FIELDS:
+        assert same(got[k], o.field(k)), k
+
+
+def test_gpu_wind_tracer():
+    wind = np.stack([np.arange(-180.0, 181.0), 30 * np.cos(np.deg2rad(np.arange(-180.0, 181.0)) * 3)], axis=1)
+    case = cases.make_case(nx=48, ny=20, sch=7, seed=5, wind=wind, tracer=True, TracerDis=3e-6)
+    s, o = run_both(case, 20)
+    got = s.download()
+    for k in FIELDS:
+        assert same(got[k], o.field(k)), k
+
+
+def test_gpu_vanleer_aborts_where_reference_aborts():
+    entry = gc.manifest()["c01_vanleer_nan"]
+    p = gc.params_of(entry)
+    z = np.load(f"{gc.GOLDEN}/c01_vanleer_nan.npz")
+    f = [gc.padded(z["init_" + k]) for k in FIELDS]
+    s = lib.Solver(p)
+    s.upload(*f)
+    assert s.step(entry["nsteps"]) == lib.ERR_NONFINITE
+    assert s.error_step() + 1 == entry["abort_step"]
+    # the safe variant runs through
+    s2 = lib.Solver(p, flags=lib.FLAG_VANLEER_SAFE)
+    s2.upload(*f)
+    assert s2.step(entry["nsteps"]) == lib.OK
+    assert all(np.isfinite(a).all() for a in s2.download().values())
+
+
+def test_gpu_cfl_abort_step_matches_oracle():
+    case = cases.make_case(nx=40, ny=20, sch=2, seed=22, cfl=0.4, nsteps=200)
+    s = lib.Solver(case.params)
+    s.upload(*case.fields())
+    o = orc.Oracle(case.params)
+    o.load(case.fields())
+    rc, bad = o.step(200)
+    assert rc == 1
+    assert s.step(200) == lib.ERR_CFL
+    assert s.error_step() == bad
+    # an oversized Dt fails on the first step
+    case.params.Dt *= 100
+    s3 = lib.Solver(case.params)
+    s3.upload(*case.fields())
+    assert s3.step(3) == lib.ERR_CFL and s3.error_step() == 0
+
+
+def test_gpu_energy_matches_oracle():
+    case = cases.make_case(nx=96, ny=48, sch=2, seed=3, bumps=3)
+    s, o = run_both(case, 30)
+    ke, ape, m = s.diag()
+    oke, oape, om = o.energy()
+    for a, b in ((ke, oke), (ape, oape), (m, om)):
+        assert abs(a - b) <= 1e-12 * abs(b), (a, b)
+
+
+def test_gpu_raw_upload_round_trip_and_resume():
+    case = cases.make_case(nx=32, ny=16, sch=2, seed=9)
+    s = lib.Solver(case.params)
+    s.upload(*case.fields(), mode=lib.UPLOAD_RAW)
+    back = s.download()
+    for k in FIELDS:
+        assert np.array_equal(back[k], getattr(case, k))
+    # stepping 10 then 10 equals stepping 20 (history kept across calls)
+    s.step(10)
+    s.step(10)
+    a = s.download()
+    s2 = lib.Solver(case.params)
+    s2.upload(*case.fields(), mode=lib.UPLOAD_RAW)
+    s2.step(20)
+    b = s2.download()
+    for k in FIELDS:
+        assert same(a[k], b[k])
+
+
+def test_gpu_rest_state_stays_at_rest():
+    case = cases.make_case(nx=64, ny=32, sch=1, seed=1, jet="none", bumps=0)
+    s = lib.Solver(case.params)
+    s.upload(*case.fields())
+    assert s.step(50) == lib.OK
+    got = s.download()
+    assert np.all(got["u"] == 0) and np.all(got["v"] == 0)
+    assert np.all(got["eta"][2:-2, 2:-2] == case.eta[2:-2, 2:-2])
+
+
+@pytest.mark.slow
+def test_gpu_band2048_matches_oracle():
+    """Full drop-in size (2048x1024 minmod with nu4), bit-identical to the oracle
+    after 40 steps."""
+    case = cases.config_case("band2048")
+    s, o = run_both(case, 40, chunk=20)
+    got = s.download()
+    for k in ("eta", "u", "v"):
+        assert same(got[k], o.field(k)), k
