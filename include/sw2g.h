@@ -137,6 +137,39 @@ sw2g_status sw2g_timer_read(const sw2g_ctx *ctx, int idx, const char **name, lon
 
 void sw2g_destroy(sw2g_ctx *ctx);
 
+/* Largest ny accepted by sw2g_energy_noalloc. */
+#define SW2G_NOALLOC_MAX_ROWS 8192
+
+/* Energy diagnostic that allocates nothing. This entry point has no
+ * counterpart in the reference.
+ *
+ * sw2g_diag needs a context, whose creation allocates device memory. Some
+ * callers hold fields on the GPU but cannot let a library allocate: a host
+ * loop whose device memory is already reserved by its own pool allocator, a
+ * time loop in which a cudaMalloc/cudaFree would synchronise the device in
+ * the middle of a step, or a post-processing tool that owns its field buffers
+ * and never creates a context. This call gives them the same three sums as
+ * sw2g_diag (kinetic and available potential energy as energy.c:25-55
+ * defines them, and mass), without any cudaMalloc, cudaFree or other
+ * allocating routine.
+ *
+ * All field pointers are device pointers on the current CUDA device, in the
+ * padded layout; windx, windy and hB may be NULL (read as zero). out3 is a
+ * device pointer to three doubles (ke, ape, mass). Work is queued on `stream`
+ * (a cudaStream_t; NULL is the default stream); out3 is valid once it is done.
+ *
+ * Limits and sharing: ny must not exceed SW2G_NOALLOC_MAX_ROWS (otherwise
+ * SW2G_ERR_BAD_ARG and a message on stderr). The scratch is one fixed 320 KiB
+ * array in device memory that every GPU loading the library holds until the
+ * process exits, and that all calls share: each call rewrites the rows it
+ * reads, but calls that overlap on the GPU (other streams, other host
+ * threads) race on it and must be serialised by the caller. The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress); make
+ * that first call before any stream capture. */
+sw2g_status sw2g_energy_noalloc(const sw2g_case *c, const double *eta, const double *u, const double *v,
+                                const double *windx, const double *windy, const double *hB, double *out3,
+                                void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,6 +27,7 @@ HOST = "-fPIC,-ffp-contract=off,-O2"
 UNITS = [
     ("api.cu", []),
     ("step_fp64.cu", ["-fmad=false"]),
+    ("noalloc.cu", ["-fmad=false"]),
     ("geometry.cpp", None),  # plain host C++
 ]
 

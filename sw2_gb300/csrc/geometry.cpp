@@ -100,4 +100,23 @@ void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, 
   *rest_my = my;
 }
 
+// Area element DXC*DYC and gravity GC of interior rows j0..j0+n-1 (the two
+// per-row values the energy sum needs), into caller-owned arrays; uses the
+// same expressions as build_rows and allocates nothing.
+void energy_row_geometry(const sw2g_case& c, int j0, int n, double* surf, double* gc) {
+  Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};
+  const double lon0 = deg2rad(c.lon0), lon1 = deg2rad(c.lon1);
+  const double lat0 = deg2rad(c.lat0), lat1 = deg2rad(c.lat1);
+  const double dlon = (lon1 - lon0) / ((double)c.nx);
+  const double dlat = (lat1 - lat0) / ((double)c.ny);
+  for (int q = 0; q < n; q++) {
+    const int j = j0 + q;
+    const double ln1 = linspace_val(j - 1, lat0, lat1, c.ny), ln = linspace_val(j, lat0, lat1, c.ny);
+    const double lc = (ln + ln1) / 2.;
+    const double dxc = dlon * rZ(p, lc), dyc = dlat * rM(p, ln1);
+    surf[q] = dxc * dyc;
+    gc[q] = g_eff(p, lat2pclat(p, lc));
+  }
+}
+
 }  // namespace sw2g
