@@ -62,6 +62,10 @@ KERNEL_BYTES = {
     "add": 8 * (2 + 1),
     "cfl": 8 * 2,
     "range": 8 * 1,
+    # FP32 form: FP64 state (8 B), FP32 histories and intermediates (4 B)
+    "f32_lap1": 8 * 2 + 4 * 2,                      # u v -> Lu Lv
+    "f32_main1": 8 * 3 + 4 * 2 + 4 * 2 + 8 + 4 + 4 * 2,  # eta u v, L, 2 hist -> eta, hist, partial Du Dv
+    "f32_main2": 8 * 3 + 4 * 2 + 4 * 4 + 8 * 2 + 4 * 2,  # eta u v, partials, 4 hist -> u v, 2 hist
 }
 # The whole step: read eta u v, write eta u v, read two history levels of
 # three tendencies, write one (SURVEY-style count for the FP64 form).
@@ -121,11 +125,14 @@ class ClockSampler:
                     rows.append(p)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        sm = [int(r[1]) for r in rows]
+        # samples with the "GPU idle" event bit (0x1) were taken outside kernel work
+        busy = [r for r in rows if not (int(r[4], 16) & 0x1)]
+        use = busy or rows
+        sm = [int(r[1]) for r in use]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        reasons = sorted({names[k] for r in use for k in range(4) if r[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]), "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(rows), "samples_under_load": len(busy)}
 
 
 def dist_env():
@@ -196,6 +203,64 @@ def run_reference_arm(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def measure(lib, case, precision, steps, warmup, local, barrier, flags=0):
+    """Timed region of one form: K steps with inputs resident; then a second
+    pass with per-kernel timers. Returns a dict of measurements."""
+    p = case.params
+    cells = p.nx * p.ny
+    s = lib.Solver(p, precision=precision, device=local, flags=flags)
+    s.upload(*case.fields())
+    assert s.step(warmup) == lib.OK
+    barrier()
+    rc = s.step(steps)
+    barrier()
+    if rc != lib.OK:
+        raise RuntimeError(f"step failed: {lib.status_string(rc)} at step {s.error_step()}")
+    ms = s.last_step_ms()
+    launches = s.last_launches()
+    s.timers(True)
+    s.timers_reset()
+    assert s.step(steps) == lib.OK
+    table = s.timer_table()
+    s.timers(False)
+    name, (nl, kms) = max(table.items(), key=lambda kv: kv[1][1])
+    per_launch = kms / nl
+    kb = KERNEL_BYTES.get(name)
+    total_k = sum(v[1] for v in table.values())
+    return {"solver": s, "ms": ms, "launches": launches, "value": cells * steps / (ms * 1e-3),
+            "kernel": name, "per_launch_ms": per_launch, "bytes_per_cell": kb,
+            "achieved_gbs": (kb * cells / (per_launch * 1e-3) / 1e9) if kb else None,
+            "kernel_share": kms / total_k,
+            "kernels_ms_per_step": {k: v[1] / steps for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}}
+
+
+def accuracy(lib, case, nsteps, local):
+    """FP32 form against the FP64 reference-exact step after nsteps: relative
+    L2 over the interior of h = eta + depth, u, v, and the relative drift of
+    mass and energy of each form."""
+    d = case.params.depth
+    out = {"steps": nsteps}
+    res = {}
+    for nm, prec in (("fp64", lib.FP64), ("fp32", lib.FP32)):
+        s = lib.Solver(case.params, precision=prec, device=local)
+        s.upload(*case.fields())
+        k0, a0, m0 = s.diag()
+        rc = s.step(nsteps)
+        if rc != lib.OK:
+            return {"steps": nsteps, "error": f"{nm}: {lib.status_string(rc)} at step {s.error_step()}"}
+        k1, a1, m1 = s.diag()
+        res[nm] = s.download()
+        out[f"mass_drift_{nm}"] = (m1 - m0) / m0
+        out[f"energy_drift_{nm}"] = ((k1 + a1) - (k0 + a0)) / (k0 + a0)
+        s.close()
+    a, b = res["fp32"], res["fp64"]
+    I = (slice(2, -2), slice(2, -2))
+    out["h_rel_l2"] = float(np.linalg.norm((a["eta"] - b["eta"])[I]) / np.linalg.norm((b["eta"] + d)[I]))
+    for k in ("u", "v"):
+        out[f"{k}_rel_l2"] = float(np.linalg.norm((a[k] - b[k])[I]) / np.linalg.norm(b[k][I]))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -203,6 +268,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="band2048")
+    ap.add_argument("--fp32-config", default="saturn4096", help="workload of the FP32-form throughput line")
+    ap.add_argument("--accuracy-steps", type=int, default=2000)
     ap.add_argument("--cpu-steps", type=int, default=None, help="oracle steps for the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -227,44 +294,25 @@ def main():
     case, desc = make_workload(args.config, seed=1 + rank)
     p = case.params
     cells = p.nx * p.ny
-    s = lib.Solver(p, device=local)
-    s.upload(*case.fields())
 
     def barrier():
         torch.cuda.synchronize(local)
         if pg:
             pg.barrier()
 
-    # warm-up
-    assert s.step(args.warmup) == lib.OK
-
-    # timed region: K steps, device time by CUDA events on the library's stream
-    barrier()
-    with ClockSampler(local) as clk:
-        rc = s.step(args.steps)
-        barrier()
-    if rc != lib.OK:
-        raise RuntimeError(f"step failed: {lib.status_string(rc)} at step {s.error_step()}")
-    ms = s.last_step_ms()
-    launches = s.last_launches()
-    if pg:
-        t = torch.tensor([ms], device=f"cuda:{local}")
+    def max_over_ranks(x):
+        if not pg:
+            return x
+        t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cells * args.steps * ws / (ms * 1e-3)
+        return float(t.item())
 
-    # per-kernel device times (second timed pass, timers on)
-    s.timers(True)
-    s.timers_reset()
-    assert s.step(args.steps) == lib.OK
-    table = s.timer_table()
-    s.timers(False)
-    name, (nl, kms) = max(table.items(), key=lambda kv: kv[1][1])
-    per_launch_ms = kms / nl
-    kb = KERNEL_BYTES.get(name)
-    peak, peak_kind = load_peaks()
-    achieved = (kb * cells / (per_launch_ms * 1e-3) / 1e9) if kb else None
-    total_kernel_ms = sum(v[1] for v in table.values())
+    # headline: the FP64 reference-exact step on the drop-in configuration
+    clk = ClockSampler(local).__enter__()
+    m64 = measure(lib, case, lib.FP64, args.steps, args.warmup, local, barrier)
+    ms = max_over_ranks(m64["ms"])
+    value = cells * args.steps * ws / (ms * 1e-3)
+    s = m64["solver"]
 
     # end to end through the C ABI: every step uploads the state from pinned
     # host memory, steps once, and downloads it again
@@ -281,13 +329,19 @@ def main():
             raise RuntimeError("e2e step failed")
         lib.load().sw2g_download(s.h, *[lib._ptr(h) for h in host], None)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], device=f"cuda:{local}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = cells * args.steps * ws / e2e_s
     bytes_io = 3 * W * H * 8
+    s.close()
+
+    # the FP32 precision form, same workload and the larger precision-form workload
+    m32 = measure(lib, case, lib.FP32, args.steps, args.warmup, local, barrier)
+    m32["solver"].close()
+    c32, desc32 = make_workload(args.fp32_config, seed=1 + rank)
+    m32b = measure(lib, c32, lib.FP32, args.steps, args.warmup, local, barrier)
+    m32b["solver"].close()
+    clk.__exit__(None, None, None)
+    acc = accuracy(lib, case, args.accuracy_steps, local) if args.accuracy_steps > 0 else None
 
     if rank != 0:
         pg.destroy_process_group()
@@ -295,11 +349,21 @@ def main():
 
     cpu = None
     if not args.no_cpu:
-        n_cpu = args.cpu_steps or max(2, int(round(15.0 / (cells / 40e6))))  # ~15 s at ~40 M cell/s
+        n_cpu = args.cpu_steps or max(2, int(round(15.0 / (cells / 30e6))))  # ~15 s at ~30 M cell/s
         v_cpu, thr, secs = time_cpu_oracle(case, n_cpu)
         cpu = {"value": v_cpu, "unit": UNIT, "cores": thr, "kind": "port",
                "sample": f"{args.config}: {n_cpu} full-grid steps ({secs:.1f} s) of the C restatement of the "
                          f"reference step, OpenMP over rows"}
+
+    peak, peak_kind = load_peaks()
+
+    def form_line(m, cfg, nxy):
+        return {"config": cfg, "cells": nxy, "value": m["value"], "unit": UNIT,
+                "ms_per_step": m["ms"] / args.steps, "gpu_launches": m["launches"],
+                "dominant_kernel": m["kernel"], "kernel_per_launch_ms": m["per_launch_ms"],
+                "kernel_bytes_per_cell": m["bytes_per_cell"], "kernel_achieved_gbs": m["achieved_gbs"],
+                "kernel_frac_of_measured_hbm": (m["achieved_gbs"] / peak) if m["achieved_gbs"] else None,
+                "kernels_ms_per_step": m["kernels_ms_per_step"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -307,17 +371,25 @@ def main():
         "dtype": "f64", "data": "synthetic (seeded balanced jet + Gaussian; no dataset)",
         "config": {"workload": f"{args.config}: {desc}", "nx": p.nx, "ny": p.ny, "form": "fp64-exact",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                   "l2": "no flush: the step streams ~38 padded FP64 fields (>0.6 GB) per step, far above L2"},
+                   "l2": "no flush: each step streams >0.6 GB of fields, far above L2"},
         "hbm_gbs_step": STEP_BYTES * value / 1e9,
-        "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "peak_kind": peak_kind, "bytes_per_cell": kb,
-                     "per_launch_ms": per_launch_ms, "kernel_share": kms / total_kernel_ms},
-        "kernels_ms_per_step": {k: v[1] / args.steps for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])},
-        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": m64["kernel"], "achieved": m64["achieved_gbs"], "peak": peak,
+                     "unit": "GB/s", "frac": (m64["achieved_gbs"] / peak) if m64["achieved_gbs"] else None,
+                     "traffic": None, "peak_kind": peak_kind, "bytes_per_cell": m64["bytes_per_cell"],
+                     "per_launch_ms": m64["per_launch_ms"], "kernel_share": m64["kernel_share"],
+                     "note": "the FP64 form is FP64-issue bound on GB300 (~0.5 T FP64 op/s)"},
+        "kernels_ms_per_step": m64["kernels_ms_per_step"],
+        "gpu_launches": m64["launches"],
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
+        "forms": {
+            "fp64": form_line(m64, args.config, cells),
+            "fp32": form_line(m32, args.config, cells),
+            "fp32_large": form_line(m32b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
+        },
+        "fp32_over_fp64": m32["value"] / m64["value"],
+        "accuracy_fp32_vs_fp64": acc,
     }
     print(json.dumps(line), flush=True)
     if pg:

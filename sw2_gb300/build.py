@@ -28,6 +28,7 @@ UNITS = [
     ("api.cu", []),
     ("step_fp64.cu", ["-fmad=false"]),
     ("noalloc.cu", ["-fmad=false"]),
+    ("step_fp32.cu", []),
     ("geometry.cpp", None),  # plain host C++
 ]
 

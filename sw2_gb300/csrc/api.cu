@@ -41,6 +41,16 @@ struct sw2g_ctx {
   long long steps = 0;
   int err_step = -1;
   long long last_launches = 0;
+  // FP32 precision form
+  Fp32Engine e32;
+  Fp32Ctx c32{};
+  std::vector<void*> allocs32;
+  float* d_q32 = nullptr;
+  double* d_ref = nullptr;         // eta_ref(j), ny+4 rows
+  std::vector<double> ref;         // host copy
+  double* d_aux64[3] = {nullptr, nullptr, nullptr};  // windx, windy, hB (FP64) for the diagnostic
+  float* d_aux32[3] = {nullptr, nullptr, nullptr};   // the same in FP32 for the stencils
+  double* d_tmp = nullptr;         // full eta for download and diagnostics
 };
 
 namespace {
@@ -74,6 +84,163 @@ sw2g_status dalloc(sw2g_ctx* x, double** p, size_t n) {
   CK(cudaMalloc((void**)p, n * sizeof(double)));
   CK(cudaMemsetAsync(*p, 0, n * sizeof(double), x->stream));
   x->allocs.push_back(*p);
+  return SW2G_OK;
+}
+
+template <typename T>
+sw2g_status dalloc32(sw2g_ctx* x, T** p, size_t n) {
+  CK(cudaMalloc((void**)p, n * sizeof(T)));
+  CK(cudaMemsetAsync(*p, 0, n * sizeof(T), x->stream));
+  x->allocs32.push_back(*p);
+  return SW2G_OK;
+}
+
+// Buffers of the FP32 form: FP64 state (double-buffered, eta as a perturbation),
+// FP32 histories and intermediates.
+sw2g_status alloc_fp32(sw2g_ctx* x) {
+  const size_t S = (size_t)x->s.W * x->s.H;
+  Fp32Engine& e = x->e32;
+  sw2g_status st;
+  for (int q = 0; q < 2; q++) {
+    if ((st = dalloc(x, &e.eta[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc(x, &e.u[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc(x, &e.v[q], S)) != SW2G_OK) return st;
+  }
+  for (int q = 0; q < 3; q++) {
+    if ((st = dalloc32(x, &e.heta[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.hu[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.hv[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc(x, &x->d_aux64[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &x->d_aux32[q], S)) != SW2G_OK) return st;
+  }
+  if ((st = dalloc32(x, &e.Lu, S)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.Lv, S)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.dup, S)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.dvp, S)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.cfl, 2 * (size_t)kChunk)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.bad, (size_t)kChunk)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &x->d_q32, (size_t)Q_NUM * x->s.H)) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->d_ref, (size_t)x->s.H)) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->d_tmp, S)) != SW2G_OK) return st;
+  return SW2G_OK;
+}
+
+// Per-row FP32 constants of the FP32 form, from the FP64 geometry and the
+// reference profile eta_ref(j) (all arithmetic in FP64, rounded once).
+void build_q32(const sw2g_ctx* x, std::vector<float>& q) {
+  const int ny = x->s.ny, H = x->s.H;
+  const double Dt = x->c.Dt;
+  q.assign((size_t)Q_NUM * H, 0.f);
+  auto R = [&](int t, int j) { return x->rows[(size_t)t * H + (j + 1)]; };
+  auto ref = [&](int j) { return x->ref[j + 1]; };
+  for (int j = -1; j <= ny + 2; j++) {
+    auto set = [&](int t, double v) { q[(size_t)t * H + (j + 1)] = (float)v; };
+    const bool up = (j + 1 <= ny + 2), up2 = (j + 2 <= ny + 2), dn2 = (j - 2 >= -1);
+    set(Q_KXE, Dt / R(R_DXE, j));
+    set(Q_KYN, Dt / R(R_DYN, j));
+    set(Q_KXC, Dt / R(R_DXC, j));
+    set(Q_KYV, Dt / R(R_DYV, j));
+    set(Q_KXV, Dt / R(R_DXV, j));
+    set(Q_KYC, Dt / R(R_DYC, j));
+    set(Q_K2XE, Dt / (R(R_DXE, j) + R(R_DXE, j)));
+    set(Q_KDYNS, up ? Dt / (R(R_DYN, j) + R(R_DYN, j + 1)) : 0.0);
+    set(Q_GEX, -R(R_GE, j) * Dt / R(R_DXC, j));
+    set(Q_GNY, up ? -R(R_GN, j) * Dt / R(R_DYC, j + 1) : 0.0);
+    set(Q_GEO, R(R_GEO, j));
+    set(Q_CV, Dt * R(R_SINN, j) / R(R_RZN, j));
+    set(Q_DTFE, R(R_DTFE, j));
+    set(Q_DTFN, R(R_DTFN, j));
+    set(Q_HB, ref(j) + x->c.depth);
+    set(Q_EREF, ref(j));
+    set(Q_DHBM2, dn2 ? ref(j - 2) - ref(j) : 0.0);
+    set(Q_DHBM1, j - 1 >= -1 ? ref(j - 1) - ref(j) : 0.0);
+    set(Q_DHBP1, up ? ref(j + 1) - ref(j) : 0.0);
+    set(Q_DHBP2, up2 ? ref(j + 2) - ref(j) : 0.0);
+    set(Q_IDXV, 1.0 / R(R_DXV, j));
+    set(Q_IDYC, 1.0 / R(R_DYC, j));
+    set(Q_DXC, R(R_DXC, j));
+    set(Q_IDXE, 1.0 / R(R_DXE, j));
+    set(Q_IDYN, 1.0 / R(R_DYN, j));
+    set(Q_DXV, R(R_DXV, j));
+    set(Q_IDXC, 1.0 / R(R_DXC, j));
+  }
+}
+
+bool all_zero(const double* a, size_t n) {
+  if (!a) return true;
+  for (size_t t = 0; t < n; t++)
+    if (a[t] != 0.0) return false;
+  return true;
+}
+
+// Upload for the FP32 form: eta is stored as eta - eta_ref(j), with eta_ref
+// the zonal mean of the uploaded interior (halo rows take the wrapped rows).
+sw2g_status upload_fp32(sw2g_ctx* x, const double* eta, const double* u, const double* v, const double* tracer,
+                        const double* windx, const double* windy, const double* hB, int mode) {
+  const DevState& s = x->s;
+  const int W = s.W, H = s.H, nx = s.nx, ny = s.ny;
+  const size_t S = (size_t)W * H, bytes = S * sizeof(double);
+  const bool cont = (mode == SW2G_UPLOAD_CONTINUE);
+  if (tracer && !all_zero(tracer, S)) {
+    fprintf(stderr, "sw2g: the FP32 form does not advect a tracer; upload an all-zero tracer or NULL\n");
+    return SW2G_ERR_BAD_ARG;
+  }
+  if (!cont) {
+    x->ref.assign(H, 0.0);
+    for (int j = 1; j <= ny; j++) {
+      double acc = 0, cmp = 0;
+      for (int i = 1; i <= nx; i++) {  // compensated zonal sum
+        const double t = eta[(i + 1) + (size_t)(j + 1) * W], a = acc + t;
+        cmp += (std::fabs(acc) >= std::fabs(t)) ? ((acc - a) + t) : ((t - a) + acc);
+        acc = a;
+      }
+      x->ref[j + 1] = (acc + cmp) / nx;
+    }
+    x->ref[0] = x->ref[ny];  // j = -1 <- ny - 1
+    x->ref[1] = x->ref[ny + 1];
+    x->ref[ny + 2] = x->ref[2];
+    x->ref[ny + 3] = x->ref[3];
+    CK(cudaMemcpyAsync(x->d_ref, x->ref.data(), H * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+    std::vector<float> q;
+    build_q32(x, q);
+    CK(cudaMemcpyAsync(x->d_q32, q.data(), q.size() * sizeof(float), cudaMemcpyHostToDevice, x->stream));
+    CK(cudaStreamSynchronize(x->stream));
+  }
+  Fp32Engine& e = x->e32;
+  std::vector<double> ep(S);
+  for (int j = -1; j <= ny + 2; j++)
+    for (int i = -1; i <= nx + 2; i++) {
+      const size_t t = (i + 1) + (size_t)(j + 1) * W;
+      ep[t] = eta[t] - x->ref[j + 1];
+    }
+  CK(cudaMemcpyAsync(e.eta[e.cur], ep.data(), bytes, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(e.u[e.cur], u, bytes, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(e.v[e.cur], v, bytes, cudaMemcpyHostToDevice, x->stream));
+  if (mode == SW2G_UPLOAD_FRAME) {
+    halo_wrap(e.eta[e.cur], nx, ny, x->stream);
+    halo_wrap(e.u[e.cur], nx, ny, x->stream);
+    halo_wrap(e.v[e.cur], nx, ny, x->stream);
+  }
+  const double* aux[3] = {windx, windy, hB};
+  if (!cont || windx || windy || hB) {
+    int extra = 0;
+    std::vector<float> f32(S);
+    for (int q = 0; q < 3; q++) {
+      if (aux[q]) {
+        CK(cudaMemcpyAsync(x->d_aux64[q], aux[q], bytes, cudaMemcpyHostToDevice, x->stream));
+        for (size_t t = 0; t < S; t++) f32[t] = (float)aux[q][t];
+        CK(cudaMemcpyAsync(x->d_aux32[q], f32.data(), S * sizeof(float), cudaMemcpyHostToDevice, x->stream));
+        CK(cudaStreamSynchronize(x->stream));
+        if (!all_zero(aux[q], S)) extra = 1;
+      } else if (!cont) {
+        CK(cudaMemsetAsync(x->d_aux64[q], 0, bytes, x->stream));
+        CK(cudaMemsetAsync(x->d_aux32[q], 0, S * sizeof(float), x->stream));
+      }
+    }
+    if (!cont) x->c32.extra = extra;
+    else x->c32.extra = x->c32.extra || extra;
+  }
+  CK(cudaStreamSynchronize(x->stream));
   return SW2G_OK;
 }
 
@@ -161,7 +328,9 @@ const char* sw2g_status_string(sw2g_status s) {
 sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx** out) {
   if (!out) return SW2G_ERR_BAD_ARG;
   *out = nullptr;
-  if (!case_ok(c) || (precision != SW2G_FP64)) return SW2G_ERR_BAD_ARG;
+  if (!case_ok(c) || (precision != SW2G_FP64 && precision != SW2G_FP32)) return SW2G_ERR_BAD_ARG;
+  // the FP32 form covers nabla^2 and nabla^4 hyperviscosity (the configurations' operators)
+  if (precision == SW2G_FP32 && c->hypernu[2] != 0) return SW2G_ERR_BAD_ARG;
   sw2g_ctx* x = new (std::nothrow) sw2g_ctx();
   if (!x) return SW2G_ERR_NOMEM;
   x->c = *c;
@@ -198,15 +367,31 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
                                       cudaMemcpyHostToDevice, x->stream), "rows")) != SW2G_OK)
     return fail(st);
   s.rows = x->d_rows;
-  Fp64Buffers& b = x->b;
-  double** all[] = {&b.f[0], &b.f[1], &b.f[2], &b.f[3], &b.f[4], &b.f[5], &b.f[6],
-                    &b.deta[0], &b.deta[1], &b.deta[2], &b.du[0], &b.du[1], &b.du[2],
-                    &b.dv[0], &b.dv[1], &b.dv[2], &b.dtr[0], &b.dtr[1], &b.dtr[2],
-                    &b.detaAB, &b.duAB, &b.dvAB, &b.dtrAB, &b.duadv, &b.dvadv,
-                    &b.Le[0], &b.Le[1], &b.Le[2], &b.L[0], &b.L[1], &b.L[2], &b.L[3], &b.L[4], &b.L[5],
-                    &b.psi, &b.xi, &b.ze, &b.di};
-  for (double** p : all)
-    if ((st = dalloc(x, p, S)) != SW2G_OK) return fail(st);
+  if (precision == SW2G_FP64) {
+    Fp64Buffers& b = x->b;
+    double** all[] = {&b.f[0], &b.f[1], &b.f[2], &b.f[3], &b.f[4], &b.f[5], &b.f[6],
+                      &b.deta[0], &b.deta[1], &b.deta[2], &b.du[0], &b.du[1], &b.du[2],
+                      &b.dv[0], &b.dv[1], &b.dv[2], &b.dtr[0], &b.dtr[1], &b.dtr[2],
+                      &b.detaAB, &b.duAB, &b.dvAB, &b.dtrAB, &b.duadv, &b.dvadv,
+                      &b.Le[0], &b.Le[1], &b.Le[2], &b.L[0], &b.L[1], &b.L[2], &b.L[3], &b.L[4], &b.L[5],
+                      &b.psi, &b.xi, &b.ze, &b.di};
+    for (double** p : all)
+      if ((st = dalloc(x, p, S)) != SW2G_OK) return fail(st);
+  } else {
+    if ((st = alloc_fp32(x)) != SW2G_OK) return fail(st);
+    Fp32Ctx& c32 = x->c32;
+    c32.nx = c->nx;
+    c32.ny = c->ny;
+    c32.sch = (c->sch == 3) ? kVanLeerSafe : c->sch;  // the FP32 form always uses the safe Van Leer
+    c32.q = x->d_q32;
+    c32.sig2dt = (float)(2.0 * c->Dt * s.sigma);
+    c32.sigdt = (float)(s.sigma * c->Dt);
+    c32.nu2dt = (float)(s.nu2 * c->Dt);
+    c32.nu4dt = (float)(s.nu4 * c->Dt);
+    c32.wx = x->d_aux32[0];
+    c32.wy = x->d_aux32[1];
+    c32.hb = x->d_aux32[2];
+  }
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
     return fail(st);
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_bad, sizeof(int) * kChunk), "bad")) != SW2G_OK) return fail(st);
@@ -223,6 +408,17 @@ sw2g_status sw2g_upload(sw2g_ctx* x, const double* eta, const double* u, const d
   const bool cont = (mode == SW2G_UPLOAD_CONTINUE);
   if (cont && !x->uploaded) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
+  if (x->precision == SW2G_FP32) {
+    sw2g_status st = upload_fp32(x, eta, u, v, tracer, windx, windy, hB, mode);
+    if (st != SW2G_OK) return st;
+    if (!cont) {
+      x->k = 0;
+      x->steps = 0;
+      x->err_step = -1;
+    }
+    x->uploaded = true;
+    return SW2G_OK;
+  }
   const DevState& s = x->s;
   const size_t S = (size_t)s.W * s.H, bytes = S * sizeof(double);
   const double* src[7] = {eta, u, v, tracer, windx, windy, hB};
@@ -269,20 +465,39 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
   std::vector<int> bad(kChunk);
   int done = 0;
   x->last_step_ms = 0;
+  const bool f32 = (x->precision == SW2G_FP32);
+  std::vector<unsigned> cfl32(f32 ? 2 * kChunk : 0);
   while (done < nsteps) {
     const int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
-    CK(cudaMemsetAsync(x->d_cfl, 0, sizeof(unsigned long long) * 2 * n, x->stream));
-    CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int) * n, x->stream));
+    if (f32) {
+      CK(cudaMemsetAsync(x->e32.cfl, 0, sizeof(unsigned) * 2 * n, x->stream));
+      CK(cudaMemsetAsync(x->e32.bad, 0, sizeof(int) * n, x->stream));
+    } else {
+      CK(cudaMemsetAsync(x->d_cfl, 0, sizeof(unsigned long long) * 2 * n, x->stream));
+      CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int) * n, x->stream));
+    }
     StepChecks chk{x->d_cfl, x->d_bad};
     CK(cudaEventRecord(x->ev[0], x->stream));
     for (int t = 0; t < n; t++) {
-      x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers);
+      if (f32) {
+        int nl = 0;
+        x->e32.step(x->c32, x->k, t, x->stream, &x->timers, nl);
+        x->last_launches += nl;
+      } else {
+        x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers);
+      }
       x->k++;
     }
     CK(cudaEventRecord(x->ev[1], x->stream));
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(cfl.data(), x->d_cfl, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost, x->stream));
-    CK(cudaMemcpyAsync(bad.data(), x->d_bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+    if (f32) {
+      CK(cudaMemcpyAsync(cfl32.data(), x->e32.cfl, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaMemcpyAsync(bad.data(), x->e32.bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+    } else {
+      CK(cudaMemcpyAsync(cfl.data(), x->d_cfl, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost,
+                         x->stream));
+      CK(cudaMemcpyAsync(bad.data(), x->d_bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+    }
     CK(cudaStreamSynchronize(x->stream));
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
@@ -291,8 +506,16 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
     for (int t = 0; t < n; t++) {
       // compute_Dt (calc.c:701-738) and its check (core.c:158)
       double mx, my;
-      std::memcpy(&mx, &cfl[2 * t], sizeof(double));
-      std::memcpy(&my, &cfl[2 * t + 1], sizeof(double));
+      if (f32) {
+        float a, b2;
+        std::memcpy(&a, &cfl32[2 * t], sizeof(float));
+        std::memcpy(&b2, &cfl32[2 * t + 1], sizeof(float));
+        mx = a;
+        my = b2;
+      } else {
+        std::memcpy(&mx, &cfl[2 * t], sizeof(double));
+        std::memcpy(&my, &cfl[2 * t + 1], sizeof(double));
+      }
       if (mx + my == 0) { mx = x->rest_mx; my = x->rest_my; }
       const double dt_cfl = (x->c.courant / (mx + my));
       if (x->c.Dt > dt_cfl) {
@@ -322,6 +545,18 @@ sw2g_status sw2g_download(sw2g_ctx* x, double* eta, double* u, double* v, double
   CK(cudaSetDevice(x->device));
   const size_t bytes = sizeof(double) * (size_t)x->s.W * x->s.H;
   double* dst[4] = {eta, u, v, tracer};
+  if (x->precision == SW2G_FP32) {
+    const Fp32Engine& e = x->e32;
+    if (eta) {
+      add_row_ref(x->d_tmp, e.eta[e.cur], x->d_ref, x->s.nx, x->s.ny, x->stream);
+      CK(cudaMemcpyAsync(eta, x->d_tmp, bytes, cudaMemcpyDeviceToHost, x->stream));
+    }
+    if (u) CK(cudaMemcpyAsync(u, e.u[e.cur], bytes, cudaMemcpyDeviceToHost, x->stream));
+    if (v) CK(cudaMemcpyAsync(v, e.v[e.cur], bytes, cudaMemcpyDeviceToHost, x->stream));
+    CK(cudaStreamSynchronize(x->stream));
+    if (tracer) std::memset(tracer, 0, bytes);
+    return SW2G_OK;
+  }
   for (int q = 0; q < 4; q++)
     if (dst[q]) CK(cudaMemcpyAsync(dst[q], x->b.f[q], bytes, cudaMemcpyDeviceToHost, x->stream));
   CK(cudaStreamSynchronize(x->stream));
@@ -333,7 +568,19 @@ sw2g_status sw2g_diag(sw2g_ctx* x, double* ke, double* ape, double* mass) {
   if (!x->uploaded) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
   const double* f[7];
-  for (int q = 0; q < 7; q++) f[q] = x->b.f[q];
+  if (x->precision == SW2G_FP32) {
+    const Fp32Engine& e = x->e32;
+    add_row_ref(x->d_tmp, e.eta[e.cur], x->d_ref, x->s.nx, x->s.ny, x->stream);
+    f[0] = x->d_tmp;
+    f[1] = e.u[e.cur];
+    f[2] = e.v[e.cur];
+    f[3] = x->d_aux64[0];  // not read by the energy sum
+    f[4] = x->d_aux64[0];
+    f[5] = x->d_aux64[1];
+    f[6] = x->d_aux64[2];
+  } else {
+    for (int q = 0; q < 7; q++) f[q] = x->b.f[q];
+  }
   energy_rows(x->s, f, x->d_energy, x->stream);
   energy_sum(x->d_energy, x->s.ny, x->d_energy + 3 * (size_t)x->s.ny, x->stream);
   double h[3];
@@ -353,6 +600,11 @@ sw2g_status sw2g_reset_ab(sw2g_ctx* x) {
 
 void* sw2g_device_field(sw2g_ctx* x, int which) {
   if (!x || which < 0 || which > 3) return nullptr;
+  if (x->precision == SW2G_FP32) {
+    const Fp32Engine& e = x->e32;
+    // eta is held as eta - eta_ref(j) in this form; the tracer is not held
+    return which == 0 ? (void*)e.eta[e.cur] : which == 1 ? (void*)e.u[e.cur] : which == 2 ? (void*)e.v[e.cur] : nullptr;
+  }
   return x->b.f[which];
 }
 
@@ -363,6 +615,7 @@ void sw2g_destroy(sw2g_ctx* x) {
   cudaSetDevice(x->device);
   if (x->stream) cudaStreamSynchronize(x->stream);
   for (double* p : x->allocs) cudaFree(p);
+  for (void* p : x->allocs32) cudaFree(p);
   if (x->d_cfl) cudaFree(x->d_cfl);
   if (x->d_bad) cudaFree(x->d_bad);
   x->timers.release();

@@ -1,0 +1,510 @@
+// FP32 precision form of the SW2 step.
+//
+// Same algorithm and step order as the reference (core.c:134-338), including
+// its halo and wall semantics, but the stencils, limiters and Laplacians run
+// in FP32 while the state is accumulated in FP64:
+//   * eta is kept in FP64 as a perturbation about a per-row reference profile
+//     (the zonal mean of the uploaded eta), so the FP32 stencil sees small
+//     numbers and row-to-row differences of the reference are exact FP64
+//     differences rounded once;
+//   * u, v are FP64; each step adds an FP32 increment to them in FP64;
+//   * the Adams-Bashforth histories and the intermediate fields are FP32.
+// Three kernels per step:
+//   k_lap1   : first Laplacian of (u, v) (laplacian.c:51-111) -> L, with the
+//              reference's halo images and wall fixes written by each producer;
+//   k_main1  : mass sweep + AB + geofactor -> eta (calc.c:70-113, 403-422),
+//              second Laplacian of (u, v) from L, momentum advection and
+//              dissipation -> partial tendencies, CFL maxima;
+//   k_main2  : pressure, AB, semi-implicit Coriolis u then v (calc.c:500-598),
+//              halo images and do_channel (calc.c:600-649) of u and v.
+// Halos of intermediate fields at the periodic seam are computed at their
+// source column ("ghosts"), because the reference's wrapped halo of a field
+// is not the value its stencil would give at the halo column near the walls.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "sw2g_internal.h"
+
+namespace sw2g {
+namespace f32 {
+
+constexpr int TW = 32, TH = 8, NT = TW * TH;
+constexpr int NONE = INT_MIN;
+
+__device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
+
+struct KP {
+  int nx, ny, W, H;
+  const float* q;  // Q_NUM x H per-row FP32 table
+  float sig2dt, sigdt, nu2dt, nu4dt;
+  int k;           // Adams-Bashforth index
+  int extra;       // winds / bottom present
+  const float* wx; const float* wy; const float* hb;  // FP32 copies (pitch W) when extra
+};
+
+__device__ __forceinline__ float Q(const KP& p, int t, int j) { return p.q[t * p.H + j + 1]; }
+
+// ------------------------------------------------------------------ limiters
+template <int SCH>
+__device__ __forceinline__ float psi(float r) {
+  if constexpr (SCH == 0) return fmaxf(0.f, fminf(fminf((1.f + r) * 0.5f, 2.f * r), 2.f));
+  else if constexpr (SCH == 1) return fmaxf(fmaxf(0.f, fminf(2.f * r, 1.f)), fmaxf(0.f, fminf(r, 2.f)));
+  else if constexpr (SCH == 2) return (r < 1.f) ? r : 1.f;
+  else if constexpr (SCH == 3) return (r + fabsf(r)) / (1.f + r);
+  else if constexpr (SCH == 4) return fmaxf(0.f, fminf(2.f * r, fminf((1.f + 2.f * r) * (1.f / 3.f), 2.f)));
+  else if constexpr (SCH == 5) return __fdividef(1.5f * (r * r + r), r * r + r + 1.f);
+  else if constexpr (SCH == 6) return __fdividef(r * r + r, r * r + 1.f);
+  else if constexpr (SCH == 7) return fmaxf(0.f, fminf(fminf(2.f, 2.f * r), fminf(0.25f + 0.75f * r, 0.75f + 0.25f * r)));
+  else if constexpr (SCH == 8) return 0.f;
+  else if constexpr (SCH == 9) return 1.f;
+  else return (r > 0.f) ? __fdividef(2.f * r, 1.f + r) : 0.f;  // Van Leer, 0 for r <= 0 (its limit at -1)
+}
+
+// One upwind face with a single Courant number c (mass): c*B of calc.c:41-49,100
+// with B_P (c > 0) or B_M (c < 0) reconstructed from q0|q1, outer neighbours qm, q2.
+template <int SCH>
+__device__ __forceinline__ float face1(float qm, float q0, float q1, float q2, float c) {
+  const float d = q1 - q0;
+  const bool pos = c > 0.f;
+  const float n = pos ? (q0 - qm) : (q2 - q1);
+  const float base = pos ? q0 : q1;
+  const float r = (d != 0.f) ? __fdividef(n, d) : 0.f;
+  const float s = pos ? 0.5f : -0.5f;
+  return c * (base + s * psi<SCH>(r) * (1.f - fabsf(c)) * d);
+}
+
+// A face with both split Courant numbers (momentum bodies, calc.c:170-177).
+template <int SCH>
+__device__ __forceinline__ float face2(float qm, float q0, float q1, float q2, float cP, float cM) {
+  const float d = q1 - q0;
+  const float inv = (d != 0.f) ? __frcp_rn(d) : 0.f;
+  const float rP = (q0 - qm) * inv, rM = (q2 - q1) * inv;
+  const float bP = q0 + 0.5f * psi<SCH>(rP) * (1.f - cP) * d;
+  const float bM = q1 - 0.5f * psi<SCH>(rM) * (1.f + cM) * d;
+  return cP * bP + cM * bM;
+}
+
+__device__ __forceinline__ float cpos2(float a, float b, float k) { return 0.5f * (fmaxf(a, 0.f) + fmaxf(b, 0.f)) * k; }
+__device__ __forceinline__ float cneg2(float a, float b, float k) { return 0.5f * (fminf(a, 0.f) + fminf(b, 0.f)) * k; }
+
+// ---------------------------------------------------------- halo images
+enum Img { IMG_ETA, IMG_U, IMG_V, IMG_LU, IMG_LV };
+
+// Writes the value of interior cell (i,j) and every halo cell whose final
+// value in the reference comes from it: the single-rank halo update
+// (sppde_hupdate.c:274-342, y pass then x pass) followed by do_channel for
+// u and v (calc.c:600-649) or the wall fixes of laplacian_vels (laplacian.c:94-107).
+template <Img M, typename T>
+__device__ __forceinline__ void put(T* f, int W, int nx, int ny, int i, int j, T val) {
+  const T zero = T(0);
+  f[IX(W, i, j)] = (M == IMG_V && j == ny) ? zero : val;
+  const int xa = (i <= 2) ? i + nx : NONE, xb = (i >= nx - 1) ? i - nx : NONE;
+  const int ya = (j <= 2) ? j + ny : NONE, yb = (j >= ny - 1) ? j - ny : NONE;
+  if (xa != NONE) f[IX(W, xa, j)] = val;
+  if (xb != NONE) f[IX(W, xb, j)] = val;
+  if (ya != NONE) {
+    if (xa != NONE) f[IX(W, xa, ya)] = val;
+    if (xb != NONE) f[IX(W, xb, ya)] = val;
+  }
+  if (yb != NONE) {
+    if (xa != NONE) f[IX(W, xa, yb)] = val;
+    if (xb != NONE) f[IX(W, xb, yb)] = val;
+  }
+  if constexpr (M == IMG_ETA) {
+    if (ya != NONE) f[IX(W, i, ya)] = val;
+    if (yb != NONE) f[IX(W, i, yb)] = val;
+  } else if constexpr (M == IMG_U) {
+    if (j == 1) { f[IX(W, i, 0)] = val; f[IX(W, i, -1)] = val; }
+    if (j == ny) { f[IX(W, i, ny + 1)] = val; f[IX(W, i, ny + 2)] = val; }
+  } else if constexpr (M == IMG_V) {
+    if (j == 1) { f[IX(W, i, 0)] = zero; f[IX(W, i, -1)] = zero; }
+    if (j == ny) { f[IX(W, i, ny + 1)] = zero; f[IX(W, i, ny + 2)] = zero; }
+  } else {
+    if (j == 2) f[IX(W, i, ny + 2)] = val;
+    if (j == ny - 1) f[IX(W, i, -1)] = val;
+    if (j == 1) f[IX(W, i, 0)] = (M == IMG_LU) ? val : zero;
+    if (j == ny) f[IX(W, i, ny + 1)] = (M == IMG_LU) ? val : zero;
+  }
+}
+
+// ------------------------------------------------ Laplacian of (u,v), one level
+// Tile inputs U, V (ring 1) in shared memory: local (a,b) <-> global (i0-1+a, j0-1+b).
+// Produces ZE at (i0-1+a, j0-1+b) and DI at (i0+a, j0+b), a in [0,TW], b in [0,TH],
+// following laplacian.c:59-81: ZE(i,0) = 0 and DI(i,ny+1) fixed at the walls;
+// ZE(0,j) and DI(nx+1,j) are the wrapped values ZE(nx,j) and DI(1,j),
+// evaluated at their source column from the global arrays gU, gV.
+template <typename TG>
+__device__ __forceinline__ void zeta_div(const KP& p, int i0, int j0, const float (*su)[TW + 2],
+                                         const float (*sv)[TW + 2], const TG* gU, const TG* gV,
+                                         float (*ze)[TW + 1], float (*di)[TW + 1]) {
+  const int W = p.W, nx = p.nx, ny = p.ny;
+  for (int t = threadIdx.x; t < (TW + 1) * (TH + 1); t += NT) {
+    const int a = t % (TW + 1), b = t / (TW + 1);
+    // ZE at (i, j) = (i0 - 1 + a, j0 - 1 + b)
+    {
+      const int i = i0 - 1 + a, j = j0 - 1 + b;
+      float z = 0.f;
+      if (j >= 1 && j <= ny && i <= nx) {
+        const float idxv = Q(p, Q_IDXV, j), idyc1 = Q(p, Q_IDYC, j + 1), dxc1 = Q(p, Q_DXC, j + 1),
+                    dxc = Q(p, Q_DXC, j);
+        float v1, v0, u1, u0;
+        if (i >= 1) {
+          v1 = sv[b][a + 1]; v0 = sv[b][a]; u1 = su[b + 1][a]; u0 = su[b][a];
+        } else {  // i == 0: ZE(nx, j) from the source column
+          v1 = (float)gV[IX(W, nx + 1, j)]; v0 = (float)gV[IX(W, nx, j)];
+          u1 = (float)gU[IX(W, nx, j + 1)]; u0 = (float)gU[IX(W, nx, j)];
+        }
+        z = idxv * ((v1 - v0) - idyc1 * (dxc1 * u1 - dxc * u0));
+      }
+      ze[b][a] = z;
+    }
+    // DI at (i, j) = (i0 + a, j0 + b)
+    {
+      const int i = i0 + a, j = j0 + b;
+      float d = 0.f;
+      if (j >= 1 && j <= ny && i >= 1 && i <= nx + 1) {
+        const float idxe = Q(p, Q_IDXE, j), idyn = Q(p, Q_IDYN, j), dxv = Q(p, Q_DXV, j),
+                    dxvs = Q(p, Q_DXV, j - 1);
+        float uc, uw, vc, vs;
+        if (i <= nx) {
+          uc = su[b + 1][a + 1]; uw = su[b + 1][a]; vc = sv[b + 1][a + 1]; vs = sv[b][a + 1];
+        } else {  // i == nx + 1: DI(1, j) from the source column
+          uc = (float)gU[IX(W, 1, j)]; uw = (float)gU[IX(W, 0, j)];
+          vc = (float)gV[IX(W, 1, j)]; vs = (float)gV[IX(W, 1, j - 1)];
+        }
+        d = idxe * ((uc - uw) + idyn * (dxv * vc - dxvs * vs));
+      } else if (j == ny + 1 && i >= 1 && i <= nx) {
+        d = (su[b][a + 1] - su[b][a]) * Q(p, Q_IDXE, ny);  // laplacian.c:73
+      }
+      di[b][a] = d;
+    }
+  }
+}
+
+// Second pass at tile cell (a,b) (laplacian.c:83-89).
+__device__ __forceinline__ void lap_out(const KP& p, int j, int a, int b, const float (*ze)[TW + 1],
+                                        const float (*di)[TW + 1], float& lu, float& lv) {
+  lu = -Q(p, Q_IDYN, j) * (ze[b + 1][a + 1] - ze[b][a + 1]) + Q(p, Q_IDXC, j) * (di[b][a + 1] - di[b][a]);
+  lv = Q(p, Q_IDXV, j) * (ze[b + 1][a + 1] - ze[b + 1][a]) + Q(p, Q_IDYC, j + 1) * (di[b + 1][a] - di[b][a]);
+}
+
+template <typename TG>
+__device__ __forceinline__ void load_ring1(const KP& p, int i0, int j0, const TG* U, const TG* V,
+                                           float (*su)[TW + 2], float (*sv)[TW + 2]) {
+  const int W = p.W;
+  for (int t = threadIdx.x; t < (TW + 2) * (TH + 2); t += NT) {
+    const int a = t % (TW + 2), b = t / (TW + 2);
+    const int i = min(i0 - 1 + a, p.nx + 2), j = min(j0 - 1 + b, p.ny + 2);
+    su[b][a] = (float)U[IX(W, i, j)];
+    sv[b][a] = (float)V[IX(W, i, j)];
+  }
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(NT) k_lap1(KP p, const double* __restrict__ u, const double* __restrict__ v,
+                                             float* Lu, float* Lv) {
+  __shared__ float su[TH + 2][TW + 2], sv[TH + 2][TW + 2];
+  __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
+  const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
+  load_ring1(p, i0, j0, u, v, su, sv);
+  __syncthreads();
+  zeta_div(p, i0, j0, su, sv, u, v, ze, di);
+  __syncthreads();
+  const int a = threadIdx.x % TW, b = threadIdx.x / TW;
+  const int i = i0 + a, j = j0 + b;
+  if (i > p.nx || j > p.ny) return;
+  float lu, lv;
+  lap_out(p, j, a, b, ze, di, lu, lv);
+  put<IMG_LU>(Lu, p.W, p.nx, p.ny, i, j, lu);
+  put<IMG_LV>(Lv, p.W, p.nx, p.ny, i, j, lv);
+}
+
+struct Main1Out {
+  double* eta_next;
+  float* hist_eta;  // slot for Deta_n
+  float* dup; float* dvp;
+  unsigned* cfl;    // 2 floats as bits (max |u|/dx, max |v|/dy)
+  int* bad;
+};
+
+template <int SCH>
+__global__ void __launch_bounds__(NT) k_main1(KP p, const double* __restrict__ eta, const double* __restrict__ u,
+                                              const double* __restrict__ v, const float* __restrict__ Lu,
+                                              const float* __restrict__ Lv, const float* __restrict__ h1,
+                                              const float* __restrict__ h2, Main1Out o) {
+  __shared__ float se[TH + 4][TW + 4], su[TH + 4][TW + 4], sv[TH + 4][TW + 4];
+  __shared__ float sl[TH + 2][TW + 2], sm[TH + 2][TW + 2];
+  __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
+  __shared__ float red[2][NT / 32];
+  const int W = p.W, nx = p.nx, ny = p.ny;
+  const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
+  // ring-2 tile of eta (perturbation), u, v (+ winds)
+  for (int t = threadIdx.x; t < (TW + 4) * (TH + 4); t += NT) {
+    const int a = t % (TW + 4), b = t / (TW + 4);
+    const int i = min(i0 - 2 + a, nx + 2), j = min(j0 - 2 + b, ny + 2);
+    const int q = IX(W, i, j);
+    se[b][a] = (float)eta[q];
+    float uu = (float)u[q], vv = (float)v[q];
+    if (p.extra) { uu += p.wx[q]; vv += p.wy[q]; }
+    su[b][a] = uu;
+    sv[b][a] = vv;
+  }
+  load_ring1(p, i0, j0, Lu, Lv, sl, sm);
+  __syncthreads();
+  zeta_div(p, i0, j0, sl, sm, Lu, Lv, ze, di);
+  __syncthreads();
+
+  const int a = threadIdx.x % TW + 2, b = threadIdx.x / TW + 2;  // ring-2 local coordinates
+  const int i = i0 + a - 2, j = j0 + b - 2;
+  const bool live = (i <= nx && j <= ny);
+  float mxu = 0.f, mxv = 0.f;
+  if (live) {
+    const int q = IX(W, i, j);
+    // ---- mass (BODYH, calc.c:70-113), H relative to the row reference Hb(j)
+    float qx[5], qy[5];
+#pragma unroll
+    for (int s = -2; s <= 2; s++) qx[s + 2] = se[b][a + s];
+    qy[0] = se[b - 2][a] + Q(p, Q_DHBM2, j);
+    qy[1] = se[b - 1][a] + Q(p, Q_DHBM1, j);
+    qy[2] = qx[2];
+    qy[3] = se[b + 1][a] + Q(p, Q_DHBP1, j);
+    qy[4] = se[b + 2][a] + Q(p, Q_DHBP2, j);
+    if (p.extra) {
+#pragma unroll
+      for (int s = -2; s <= 2; s++) {
+        qx[s + 2] -= p.hb[IX(W, i + s, j)];
+        qy[s + 2] -= p.hb[IX(W, i, j + s)];
+      }
+    }
+    const float kx = Q(p, Q_KXE, j), ky = Q(p, Q_KYN, j);
+    const float cw = su[b][a - 1] * kx, ce = su[b][a] * kx, cs = sv[b - 1][a] * ky, cn = sv[b][a] * ky;
+    float deta = face1<SCH>(qx[0], qx[1], qx[2], qx[3], cw) - face1<SCH>(qx[1], qx[2], qx[3], qx[4], ce) +
+                 face1<SCH>(qy[0], qy[1], qy[2], qy[3], cs) - face1<SCH>(qy[1], qy[2], qy[3], qy[4], cn);
+    deta += Q(p, Q_HB, j) * ((cw - ce) + (cs - cn));
+    deta -= p.sig2dt * (Q(p, Q_EREF, j) + se[b][a]);
+    // Adams-Bashforth (calc.c:651-699) then the geofactor (calc.c:403-422)
+    float ab;
+    if (p.k == 0) ab = deta;
+    else if (p.k == 1) ab = 1.5f * deta - 0.5f * h1[q];
+    else ab = (23.f / 12.f) * deta - (4.f / 3.f) * h1[q] + (5.f / 12.f) * h2[q];
+    const float hcell = Q(p, Q_HB, j) + qx[2];
+    ab -= Q(p, Q_GEO, j) * hcell * 0.5f * (sv[b][a] + sv[b - 1][a]);
+    o.hist_eta[q] = deta;
+    const double en = eta[q] + (double)ab;
+    put<IMG_ETA>(o.eta_next, W, nx, ny, i, j, en);
+    if (!(en >= -1e10 && en <= 1e10)) atomicOr(o.bad, 1);
+
+    // ---- second Laplacian of (u, v) from L (laplacian.c:83-89)
+    float llu, llv;
+    lap_out(p, j, a - 2, b - 2, ze, di, llu, llv);
+
+    // ---- BODYU (calc.c:168-200)
+    {
+      float ux[5], uy[5];
+#pragma unroll
+      for (int s = -2; s <= 2; s++) { ux[s + 2] = su[b][a + s]; uy[s + 2] = su[b + s][a]; }
+      const float uwm = ux[1], u0 = ux[2], uep = ux[3];
+      const float vs0 = sv[b - 1][a], vs1 = sv[b - 1][a + 1], vn0 = sv[b][a], vn1 = sv[b][a + 1];
+      const float kc = Q(p, Q_KXC, j), kv = Q(p, Q_KYV, j);
+      float p1 = face2<SCH>(ux[0], ux[1], ux[2], ux[3], cpos2(uwm, u0, kc), cneg2(uwm, u0, kc)) -
+                 face2<SCH>(ux[1], ux[2], ux[3], ux[4], cpos2(u0, uep, kc), cneg2(u0, uep, kc)) +
+                 face2<SCH>(uy[0], uy[1], uy[2], uy[3], cpos2(vs0, vs1, kv), cneg2(vs0, vs1, kv)) -
+                 face2<SCH>(uy[1], uy[2], uy[3], uy[4], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv));
+      const float p2 = u0 * (uep - uwm) * Q(p, Q_K2XE, j) + u0 * (0.5f * (vn0 + vn1) - 0.5f * (vs0 + vs1)) * kv;
+      const float ul = (float)u[q];
+      float du = p1 + p2 - ul * p.sigdt;
+      du += p.nu2dt * Lu[q] + p.nu4dt * llu;
+      o.dup[q] = du;
+      mxu = fabsf(u0) * Q(p, Q_IDXE, j);
+    }
+    // ---- BODYV (calc.c:205-237)
+    {
+      float vx[5], vy[5];
+#pragma unroll
+      for (int s = -2; s <= 2; s++) { vx[s + 2] = sv[b][a + s]; vy[s + 2] = sv[b + s][a]; }
+      const float vsm = vy[1], v0 = vy[2], vnp = vy[3];
+      const float uw1 = su[b + 1][a - 1], uw0 = su[b][a - 1], ue1 = su[b + 1][a], ue0 = su[b][a];
+      const float kxv = Q(p, Q_KXV, j), kyc = Q(p, Q_KYC, j);
+      float p1 = face2<SCH>(vx[0], vx[1], vx[2], vx[3], cpos2(uw1, uw0, kxv), cneg2(uw1, uw0, kxv)) -
+                 face2<SCH>(vx[1], vx[2], vx[3], vx[4], cpos2(ue1, ue0, kxv), cneg2(ue1, ue0, kxv)) +
+                 face2<SCH>(vy[0], vy[1], vy[2], vy[3], cpos2(vsm, v0, kyc), cneg2(vsm, v0, kyc)) -
+                 face2<SCH>(vy[1], vy[2], vy[3], vy[4], cpos2(v0, vnp, kyc), cneg2(v0, vnp, kyc));
+      const float p2 = v0 * (0.5f * (ue0 + ue1) - 0.5f * (uw0 + uw1)) * kxv + v0 * (vnp - vsm) * Q(p, Q_KDYNS, j);
+      const float vl = (float)v[q];
+      float dv = p1 + p2 - vl * p.sigdt;
+      dv += p.nu2dt * Lv[q] + p.nu4dt * llv;
+      o.dvp[q] = dv;
+      mxv = fabsf(v0) * Q(p, Q_IDYN, j);
+    }
+  }
+  // CFL maxima of this block (calc.c:705-712)
+  for (int s = 16; s > 0; s >>= 1) {
+    mxu = fmaxf(mxu, __shfl_xor_sync(0xffffffffu, mxu, s));
+    mxv = fmaxf(mxv, __shfl_xor_sync(0xffffffffu, mxv, s));
+  }
+  if ((threadIdx.x & 31) == 0) { red[0][threadIdx.x >> 5] = mxu; red[1][threadIdx.x >> 5] = mxv; }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    float m = 0.f;
+    for (int w = 0; w < NT / 32; w++) m = fmaxf(m, red[threadIdx.x][w]);
+    if (m > 0.f) atomicMax(o.cfl + threadIdx.x, __float_as_uint(m));
+  }
+}
+
+struct Main2Io {
+  const double* u; const double* v;      // state at step start
+  double* u_next; double* v_next;
+  const float* dup; const float* dvp;
+  const float* hu1; const float* hu2; const float* hv1; const float* hv2;
+  float* hu0; float* hv0;                // slots for Du_n, Dv_n
+  int* bad;
+};
+
+// Pressure (calc.c:500-540), AB, Coriolis u then v (calc.c:542-598).
+__global__ void __launch_bounds__(NT) k_main2(KP p, const double* __restrict__ eta_new, Main2Io io) {
+  __shared__ float se[TH + 2][TW + 2], su[TH + 2][TW + 2], sv[TH + 2][TW + 2];
+  __shared__ float un[TH + 1][TW + 1];  // new u at (i0-1+a, j0+b)
+  const int W = p.W, nx = p.nx, ny = p.ny;
+  const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
+  for (int t = threadIdx.x; t < (TW + 2) * (TH + 2); t += NT) {
+    const int a = t % (TW + 2), b = t / (TW + 2);
+    const int i = min(i0 - 1 + a, nx + 2), j = min(j0 - 1 + b, ny + 2);
+    const int q = IX(W, i, j);
+    se[b][a] = (float)eta_new[q];
+    su[b][a] = (float)io.u[q];  // Coriolis uses U and V without the winds
+    sv[b][a] = (float)io.v[q];
+  }
+  __syncthreads();
+  // new u on [i0-1, i0+TW-1] x [j0, j0+TH]: interior cells recomputed, the
+  // halo column 0 and the halo row ny+1 keep the old u (the v update reads
+  // them before the halo refresh, core.c:283-289)
+  for (int t = threadIdx.x; t < (TW + 1) * (TH + 1); t += NT) {
+    const int a = t % (TW + 1), b = t / (TW + 1);
+    const int i = i0 - 1 + a, j = j0 + b;
+    const int la = a, lb = b + 1;  // ring-1 local of (i, j)
+    float val = 0.f;
+    if (i <= nx && j <= ny + 1) {
+      if (i >= 1 && j <= ny) {
+        const int q = IX(W, i, j);
+        const float dun = io.dup[q] + Q(p, Q_GEX, j) * (se[lb][la + 1] - se[lb][la]);
+        float ab;
+        if (p.k == 0) ab = dun;
+        else if (p.k == 1) ab = 1.5f * dun - 0.5f * io.hu1[q];
+        else ab = (23.f / 12.f) * dun - (4.f / 3.f) * io.hu1[q] + (5.f / 12.f) * io.hu2[q];
+        const float uu = su[lb][la];
+        const float semi = 0.25f * (sv[lb][la] + sv[lb][la + 1] + sv[lb - 1][la] + sv[lb - 1][la + 1]);
+        const float al = Q(p, Q_DTFE, j) + uu * Q(p, Q_GEO, j);
+        const float be = 0.25f * al * al;
+        const float du = __fdividef(ab - 2.f * be * uu + al * semi, 1.f + be);
+        val = uu + du;
+        if (a >= 1 && b < TH) {  // a cell of this tile: accumulate in FP64 and write
+          io.hu0[q] = dun;
+          const double unew = io.u[q] + (double)du;
+          put<IMG_U>(io.u_next, W, nx, ny, i, j, unew);
+          if (!(unew >= -1e10 && unew <= 1e10)) atomicOr(io.bad, 1);
+        }
+      } else {
+        val = su[lb][la];
+      }
+    }
+    un[b][a] = val;
+  }
+  __syncthreads();
+  const int a = threadIdx.x % TW, b = threadIdx.x / TW;
+  const int i = i0 + a, j = j0 + b;
+  if (i > nx || j > ny) return;
+  const int q = IX(W, i, j);
+  const int la = a + 1, lb = b + 1;
+  const float dvn = io.dvp[q] + Q(p, Q_GNY, j) * (se[lb + 1][la] - se[lb][la] + Q(p, Q_DHBP1, j));
+  float ab;
+  if (p.k == 0) ab = dvn;
+  else if (p.k == 1) ab = 1.5f * dvn - 0.5f * io.hv1[q];
+  else ab = (23.f / 12.f) * dvn - (4.f / 3.f) * io.hv1[q] + (5.f / 12.f) * io.hv2[q];
+  const float vv = sv[lb][la];
+  // un local: (i-1, j+1) -> (a, b+1), (i, j+1) -> (a+1, b+1), (i, j) -> (a+1, b), (i-1, j) -> (a, b)
+  const float semi = 0.25f * (un[b + 1][a] + un[b + 1][a + 1] + un[b][a + 1] + un[b][a]);
+  const float al = Q(p, Q_DTFN, j) + semi * Q(p, Q_CV, j);
+  const float be = 0.25f * al * al;
+  const float dv = __fdividef(ab - 2.f * be * vv - al * semi, 1.f + be);
+  io.hv0[q] = dvn;
+  const double vnew = io.v[q] + (double)dv;
+  put<IMG_V>(io.v_next, W, nx, ny, i, j, vnew);
+  if (!(vnew >= -1e10 && vnew <= 1e10)) atomicOr(io.bad, 1);
+}
+
+template <int SCH>
+void launch_main1(dim3 g, cudaStream_t st, const KP& p, const double* eta, const double* u, const double* v,
+                  const float* Lu, const float* Lv, const float* h1, const float* h2, const Main1Out& o) {
+  k_main1<SCH><<<g, NT, 0, st>>>(p, eta, u, v, Lu, Lv, h1, h2, o);
+}
+
+}  // namespace f32
+
+using namespace f32;
+
+// ------------------------------------------------------------------ host
+void Fp32Engine::step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers* tm, int& nl) {
+  KP p{};
+  p.nx = c.nx; p.ny = c.ny; p.W = c.nx + 4; p.H = c.ny + 4;
+  p.q = c.q;
+  p.sig2dt = c.sig2dt; p.sigdt = c.sigdt; p.nu2dt = c.nu2dt; p.nu4dt = c.nu4dt;
+  p.k = k;
+  p.extra = c.extra;
+  p.wx = c.wx; p.wy = c.wy; p.hb = c.hb;
+  const dim3 g((c.nx + TW - 1) / TW, (c.ny + TH - 1) / TH);
+#define LAUNCH(tag, ...)                        \
+  do {                                          \
+    if (tm && tm->on) tm->begin(tag, st);       \
+    __VA_ARGS__;                                \
+    if (tm && tm->on) tm->end(st);              \
+    nl++;                                       \
+  } while (0)
+  LAUNCH("f32_lap1", k_lap1<<<g, NT, 0, st>>>(p, u[cur], v[cur], Lu, Lv));
+  Main1Out o1{eta[1 - cur], heta[0], dup, dvp, cfl + 2 * slot, bad + slot};
+  switch (c.sch) {
+    case 0: LAUNCH("f32_main1", launch_main1<0>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 1: LAUNCH("f32_main1", launch_main1<1>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 2: LAUNCH("f32_main1", launch_main1<2>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 3: LAUNCH("f32_main1", launch_main1<3>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 4: LAUNCH("f32_main1", launch_main1<4>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 5: LAUNCH("f32_main1", launch_main1<5>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 6: LAUNCH("f32_main1", launch_main1<6>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 7: LAUNCH("f32_main1", launch_main1<7>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 8: LAUNCH("f32_main1", launch_main1<8>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 9: LAUNCH("f32_main1", launch_main1<9>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    default: LAUNCH("f32_main1", launch_main1<kVanLeerSafe>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+  }
+  Main2Io io{u[cur], v[cur], u[1 - cur], v[1 - cur], dup, dvp, hu[1], hu[2], hv[1], hv[2], hu[0], hv[0], bad + slot};
+  LAUNCH("f32_main2", k_main2<<<g, NT, 0, st>>>(p, eta[1 - cur], io));
+#undef LAUNCH
+  // the slot just written becomes n-1, n-1 becomes n-2, n-2 is reused
+  float* t;
+  t = heta[2]; heta[2] = heta[1]; heta[1] = heta[0]; heta[0] = t;
+  t = hu[2]; hu[2] = hu[1]; hu[1] = hu[0]; hu[0] = t;
+  t = hv[2]; hv[2] = hv[1]; hv[1] = hv[0]; hv[0] = t;
+  cur = 1 - cur;
+}
+
+}  // namespace sw2g
+
+namespace sw2g {
+namespace {
+__global__ void k_add_row_ref(double* dst, const double* src, const double* ref, int W, int H) {
+  const size_t n = (size_t)W * H;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+    const int row = (int)(t / W);
+    dst[t] = src[t] + ref[row];
+  }
+}
+}  // namespace
+
+void add_row_ref(double* dst, const double* src, const double* ref_rows, int nx, int ny, cudaStream_t st) {
+  const int W = nx + 4, H = ny + 4;
+  const size_t n = (size_t)W * H;
+  const int blocks = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+  k_add_row_ref<<<blocks, 256, 0, st>>>(dst, src, ref_rows, W, H);
+}
+}  // namespace sw2g

@@ -98,6 +98,48 @@ class Timers {
 
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int step_slot,
               cudaStream_t st, Timers* tm);
+// FP32 precision form (step_fp32.cu). Per-row FP32 constants, index j+1.
+enum Q32 {
+  Q_KXE, Q_KYN, Q_KXC, Q_KYV, Q_KXV, Q_KYC,  // Dt/DXE, Dt/DYN, Dt/DXC, Dt/DYV, Dt/DXV, Dt/DYC
+  Q_K2XE,   // Dt/(DXE+DXE)
+  Q_KDYNS,  // Dt/(DYN(j)+DYN(j+1))
+  Q_GEX,    // -GE*Dt/DXC
+  Q_GNY,    // -GN*Dt/DYC(j+1)
+  Q_GEO,    // Dt*sin(latc)/rZ(latc)
+  Q_CV,     // Dt*sin(latn)/rZ(latn)
+  Q_DTFE, Q_DTFN,
+  Q_HB,     // reference height of the row: eta_ref(j) + depth
+  Q_EREF,   // eta_ref(j)
+  Q_DHBM2, Q_DHBM1, Q_DHBP1, Q_DHBP2,  // eta_ref(j+k) - eta_ref(j), k = -2,-1,1,2
+  Q_IDXV, Q_IDYC, Q_DXC, Q_IDXE, Q_IDYN, Q_DXV, Q_IDXC,
+  Q_NUM
+};
+
+struct Fp32Ctx {
+  int nx, ny, sch, extra;
+  const float* q;
+  float sig2dt, sigdt, nu2dt, nu4dt;
+  const float* wx; const float* wy; const float* hb;
+};
+
+struct Fp32Engine {
+  double* eta[2] = {nullptr, nullptr};  // eta - eta_ref(j), double-buffered
+  double* u[2] = {nullptr, nullptr};
+  double* v[2] = {nullptr, nullptr};
+  int cur = 0;
+  float* heta[3] = {nullptr, nullptr, nullptr};  // [0] slot for step n, [1] n-1, [2] n-2
+  float* hu[3] = {nullptr, nullptr, nullptr};
+  float* hv[3] = {nullptr, nullptr, nullptr};
+  float* Lu = nullptr; float* Lv = nullptr;
+  float* dup = nullptr; float* dvp = nullptr;
+  unsigned* cfl = nullptr;  // 2 per step (float bits)
+  int* bad = nullptr;       // 1 per step
+  void step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers* tm, int& nl);
+};
+
+// dst = src + ref(j) row by row over a padded field (eta perturbation -> eta)
+void add_row_ref(double* dst, const double* src, const double* ref_rows, int nx, int ny, cudaStream_t st);
+
 void halo_wrap(double* x, int nx, int ny, cudaStream_t st);
 void energy_rows(const DevState& s, const double* const* f, double* row_out, cudaStream_t st);
 void energy_sum(const double* row_in, int ny, double* out3, cudaStream_t st);

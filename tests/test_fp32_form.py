@@ -1,0 +1,101 @@
+"""FP32 precision form against the FP64 reference-exact step.
+
+The FP32 form runs the same algorithm (including the reference's halo and wall
+semantics) with FP32 stencils and FP64 state accumulation. Checks:
+  * after a few steps every padded cell (halos included) is within FP32
+    round-off of the FP64 result, so any error in the halo images, the seam
+    ghosts or the wall fixes would show up as an O(1) difference;
+  * after many steps the relative L2 error of h = eta + depth is below 1e-5
+    (the stated bar), and u, v stay close.
+"""
+import numpy as np
+import pytest
+
+from sw2_gb300 import cases, lib
+
+pytestmark = pytest.mark.gpu
+
+
+def run(case, precision, n, flags=0):
+    s = lib.Solver(case.params, precision=precision, flags=flags)
+    s.upload(*case.fields())
+    rc = s.step(n)
+    assert rc == lib.OK, (rc, s.error_step())
+    return s, s.download()
+
+
+def rel_l2(a, b):
+    a, b = a[2:-2, 2:-2], b[2:-2, 2:-2]
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("sch", [2, 1, 0, 3, 4, 7])
+def test_fp32_all_cells_close_after_few_steps(sch):
+    case = cases.make_case(nx=97, ny=45, sch=sch, seed=40 + sch, bumps=3, sigma_km=(3000.0, 6000.0))
+    flags = lib.FLAG_VANLEER_SAFE if sch == 3 else 0
+    _, a = run(case, lib.FP32, 4, flags)
+    _, b = run(case, lib.FP64, 4, flags)
+    depth = case.params.depth
+    assert np.max(np.abs(a["eta"] - b["eta"])) <= 2e-6 * depth
+    for k in ("u", "v"):
+        scale = np.max(np.abs(b["u"]))
+        assert np.max(np.abs(a[k] - b[k])) <= 2e-5 * scale, (k, np.max(np.abs(a[k] - b[k])))
+
+
+def test_fp32_halos_follow_the_reference_quirks():
+    """Row ny of v: interior zeroed by the wall, x-halo columns keep the
+    pre-wall Coriolis value (calc.c:600-649 after the halo update)."""
+    case = cases.make_case(nx=64, ny=32, sch=2, seed=5, bumps=2)
+    _, a = run(case, lib.FP32, 3)
+    _, b = run(case, lib.FP64, 3)
+    ny = case.params.ny
+    row = ny + 1
+    assert np.all(a["v"][row, 2:-2] == 0) and np.all(b["v"][row, 2:-2] == 0)
+    stale = b["v"][row, [0, 1, -2, -1]]
+    assert np.any(stale != 0)
+    assert np.allclose(a["v"][row, [0, 1, -2, -1]], stale, rtol=1e-4, atol=1e-6 * np.max(np.abs(b["v"])))
+
+
+@pytest.mark.parametrize("nx,ny", [(3, 3), (33, 9), (130, 66)])
+def test_fp32_odd_sizes(nx, ny):
+    case = cases.make_case(nx=nx, ny=ny, sch=1, seed=8, bumps=1, sigma_km=(8000.0, 8000.0))
+    _, a = run(case, lib.FP32, 5)
+    _, b = run(case, lib.FP64, 5)
+    assert np.max(np.abs(a["eta"] - b["eta"])) <= 2e-6 * case.params.depth
+    assert np.max(np.abs(a["u"] - b["u"])) <= 2e-5 * max(1.0, np.max(np.abs(b["u"])))
+
+
+def test_fp32_winds_and_nu2():
+    wind = np.stack([np.arange(-180.0, 181.0), 20 * np.cos(np.deg2rad(np.arange(-180.0, 181.0)) * 4)], axis=1)
+    case = cases.make_case(nx=80, ny=40, sch=2, seed=9, wind=wind)
+    nu4 = case.params.hypernu[1]
+    case.params.hypernu = (1e-3 * nu4 ** 0.5, nu4, 0.0)
+    _, a = run(case, lib.FP32, 4)
+    _, b = run(case, lib.FP64, 4)
+    assert np.max(np.abs(a["eta"] - b["eta"])) <= 2e-6 * case.params.depth
+    assert np.max(np.abs(a["u"] - b["u"])) <= 2e-5 * np.max(np.abs(b["u"]))
+
+
+def test_fp32_rejects_what_it_does_not_cover():
+    case = cases.make_case(nx=16, ny=8, sch=2, seed=1)
+    case.params.hypernu = (0.0, 1.0, 1.0)
+    with pytest.raises(lib.SW2GError):
+        lib.Solver(case.params, precision=lib.FP32)
+    case = cases.make_case(nx=16, ny=8, sch=2, seed=1, tracer=True)
+    s = lib.Solver(case.params, precision=lib.FP32)
+    with pytest.raises(lib.SW2GError):
+        s.upload(*case.fields())
+
+
+@pytest.mark.slow
+def test_fp32_band256_500_steps_error_bar():
+    case = cases.config_case("band256")
+    sa, a = run(case, lib.FP32, 500)
+    sb, b = run(case, lib.FP64, 500)
+    d = case.params.depth
+    e_h = rel_l2(a["eta"] + d, b["eta"] + d)
+    assert e_h <= 1e-5, e_h
+    assert rel_l2(a["u"], b["u"]) <= 1e-3
+    ka, pa, ma = sa.diag()
+    kb, pb, mb = sb.diag()
+    assert abs(ma - mb) <= 1e-9 * abs(mb)
