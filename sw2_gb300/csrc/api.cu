@@ -99,24 +99,32 @@ sw2g_status dalloc32(sw2g_ctx* x, T** p, size_t n) {
 // FP32 histories and intermediates.
 sw2g_status alloc_fp32(sw2g_ctx* x) {
   const size_t S = (size_t)x->s.W * x->s.H;
+  int P = 0, R = 0;
+  fp32_geometry(x->s.nx, x->s.ny, &P, &R);
+  x->c32.P = P;
+  x->c32.R = R;
+  const size_t S32 = (size_t)P * R;
   Fp32Engine& e = x->e32;
   sw2g_status st;
   for (int q = 0; q < 2; q++) {
     if ((st = dalloc(x, &e.eta[q], S)) != SW2G_OK) return st;
     if ((st = dalloc(x, &e.u[q], S)) != SW2G_OK) return st;
     if ((st = dalloc(x, &e.v[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.es[q], S32)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.us[q], S32)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.vs[q], S32)) != SW2G_OK) return st;
   }
   for (int q = 0; q < 3; q++) {
-    if ((st = dalloc32(x, &e.heta[q], S)) != SW2G_OK) return st;
-    if ((st = dalloc32(x, &e.hu[q], S)) != SW2G_OK) return st;
-    if ((st = dalloc32(x, &e.hv[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.heta[q], S32)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.hu[q], S32)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.hv[q], S32)) != SW2G_OK) return st;
     if ((st = dalloc(x, &x->d_aux64[q], S)) != SW2G_OK) return st;
-    if ((st = dalloc32(x, &x->d_aux32[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &x->d_aux32[q], S32)) != SW2G_OK) return st;
   }
-  if ((st = dalloc32(x, &e.Lu, S)) != SW2G_OK) return st;
-  if ((st = dalloc32(x, &e.Lv, S)) != SW2G_OK) return st;
-  if ((st = dalloc32(x, &e.dup, S)) != SW2G_OK) return st;
-  if ((st = dalloc32(x, &e.dvp, S)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.Lu, S32)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.Lv, S32)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.dup, S32)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &e.dvp, S32)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.cfl, 2 * (size_t)kChunk)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.bad, (size_t)kChunk)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &x->d_q32, (size_t)Q_NUM * x->s.H)) != SW2G_OK) return st;
@@ -134,7 +142,7 @@ void build_q32(const sw2g_ctx* x, std::vector<float>& q) {
   auto R = [&](int t, int j) { return x->rows[(size_t)t * H + (j + 1)]; };
   auto ref = [&](int j) { return x->ref[j + 1]; };
   for (int j = -1; j <= ny + 2; j++) {
-    auto set = [&](int t, double v) { q[(size_t)t * H + (j + 1)] = (float)v; };
+    auto set = [&](int t, double v) { q[(size_t)(j + 1) * Q_NUM + t] = (float)v; };
     const bool up = (j + 1 <= ny + 2), up2 = (j + 2 <= ny + 2), dn2 = (j - 2 >= -1);
     set(Q_KXE, Dt / R(R_DXE, j));
     set(Q_KYN, Dt / R(R_DYN, j));
@@ -221,20 +229,21 @@ sw2g_status upload_fp32(sw2g_ctx* x, const double* eta, const double* u, const d
     halo_wrap(e.u[e.cur], nx, ny, x->stream);
     halo_wrap(e.v[e.cur], nx, ny, x->stream);
   }
+  const int P = x->c32.P;
+  fp32_shadow(e.es[e.cur], e.eta[e.cur], nx, ny, P, x->stream);
+  fp32_shadow(e.us[e.cur], e.u[e.cur], nx, ny, P, x->stream);
+  fp32_shadow(e.vs[e.cur], e.v[e.cur], nx, ny, P, x->stream);
   const double* aux[3] = {windx, windy, hB};
   if (!cont || windx || windy || hB) {
     int extra = 0;
-    std::vector<float> f32(S);
     for (int q = 0; q < 3; q++) {
       if (aux[q]) {
         CK(cudaMemcpyAsync(x->d_aux64[q], aux[q], bytes, cudaMemcpyHostToDevice, x->stream));
-        for (size_t t = 0; t < S; t++) f32[t] = (float)aux[q][t];
-        CK(cudaMemcpyAsync(x->d_aux32[q], f32.data(), S * sizeof(float), cudaMemcpyHostToDevice, x->stream));
-        CK(cudaStreamSynchronize(x->stream));
+        fp32_shadow(x->d_aux32[q], x->d_aux64[q], nx, ny, P, x->stream);
         if (!all_zero(aux[q], S)) extra = 1;
       } else if (!cont) {
         CK(cudaMemsetAsync(x->d_aux64[q], 0, bytes, x->stream));
-        CK(cudaMemsetAsync(x->d_aux32[q], 0, S * sizeof(float), x->stream));
+        CK(cudaMemsetAsync(x->d_aux32[q], 0, (size_t)P * x->c32.R * sizeof(float), x->stream));
       }
     }
     if (!cont) x->c32.extra = extra;

@@ -37,15 +37,65 @@ constexpr int NONE = INT_MIN;
 __device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
 
 struct KP {
-  int nx, ny, W, H;
+  int nx, ny, W, H, P;
   const float* q;  // Q_NUM x H per-row FP32 table
   float sig2dt, sigdt, nu2dt, nu4dt;
   int k;           // Adams-Bashforth index
   int extra;       // winds / bottom present
-  const float* wx; const float* wy; const float* hb;  // FP32 copies (pitch W) when extra
+  const float* wx; const float* wy; const float* hb;  // FP32 copies (pitch P) when extra
 };
 
-__device__ __forceinline__ float Q(const KP& p, int t, int j) { return p.q[t * p.H + j + 1]; }
+// Per-row constants of the rows a block touches (j0-2 .. j0+TH+2), staged in
+// shared memory once per block from the row-major table p.q[(j+1)*Q_NUM + t].
+typedef float RowCache[TH + 5][Q_NUM];
+struct Rows {
+  const float (*r)[Q_NUM];
+  int j0;
+};
+__device__ __forceinline__ float Q(const Rows& c, int t, int j) { return c.r[j - c.j0 + 2][t]; }
+__device__ __forceinline__ void fill_rows(const KP& p, int j0, RowCache& sq) {
+  for (int t = threadIdx.x; t < (TH + 5) * Q_NUM; t += TW * TH) {
+    const int r = t / Q_NUM, c = t - r * Q_NUM;
+    const int row = min(j0 - 2 + r, p.ny + 2);
+    sq[r][c] = p.q[(size_t)(row + 1) * Q_NUM + c];
+  }
+}
+
+// FP64 <-> FP32 conversions on the integer pipe. On GB300 the hardware
+// conversions issue on the FP64 unit, whose throughput (~1/64 of FP32) would
+// otherwise bound these kernels; here only the state additions use it.
+// d2f: round to nearest (ties away), magnitudes below 2^-126 flush to zero,
+// overflow gives inf, NaN stays NaN.
+__device__ __forceinline__ float d2f(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long mag = b & 0x7fffffffffffffffULL;
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  unsigned r;
+  if (mag < (897ULL << 52)) r = 0u;
+  else if (mag >= (1151ULL << 52)) r = (mag > (2047ULL << 52)) ? 0x7fc00000u : 0x7f800000u;
+  else r = (unsigned)(((mag + (1ULL << 28)) >> 29) - (896ULL << 23));
+  return __uint_as_float(r | sign);
+}
+__device__ __forceinline__ float d2f(float x) { return x; }
+
+// f2d: exact widening; FP32 subnormals flush to zero.
+__device__ __forceinline__ double f2d(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  unsigned long long r;
+  if (e == 0u) r = 0ULL;
+  else if (e == 255u) r = 0x7ff0000000000000ULL | ((unsigned long long)(b & 0x7fffffu) << 29);
+  else r = ((unsigned long long)(b & 0x7fffffffu) << 29) + (896ULL << 52);
+  r |= (unsigned long long)(b & 0x80000000u) << 32;
+  return __longlong_as_double((long long)r);
+}
+
+// |x| <= 1e10 and not NaN, tested on the bits (the reference's range check,
+// sppde_core.c:386-395, without an FP64 compare).
+__device__ __forceinline__ bool in_range(double x) {
+  const unsigned long long mag = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  return mag <= 0x4202a05f20000000ULL;  // bits of 1e10
+}
 
 // ------------------------------------------------------------------ limiters
 template <int SCH>
@@ -130,54 +180,66 @@ __device__ __forceinline__ void put(T* f, int W, int nx, int ny, int i, int j, T
   }
 }
 
+// ------------------------------------------------------------- tile loads
+// FP32 fields of this form use a row pitch P (a multiple of 4) and enough
+// padding rows and columns that the ring-2 window of any tile is in bounds.
+// The window [i0-2, i0+TW+1] x [j0-2, j0+TH+1] starts on a 16-byte boundary
+// (padded column i0-1 = TW*blockIdx.x), so it is read with 16-byte loads.
+typedef float Tile[TH + 4][TW + 4];
+
+__device__ __forceinline__ int IX32(int P, int i, int j) { return (i + 1) + (j + 1) * P; }
+
+__device__ __forceinline__ void load_tile(const float* __restrict__ f, int P, int i0, int j0, Tile& t) {
+  constexpr int C4 = (TW + 4) / 4;
+  const float* base = f + (size_t)(j0 - 1) * P + (i0 - 1);
+  for (int q = threadIdx.x; q < (TH + 4) * C4; q += NT) {
+    const int r = q / C4, c = q - r * C4;
+    const float4 v = __ldg(reinterpret_cast<const float4*>(base + (size_t)r * P) + c);
+    *reinterpret_cast<float4*>(&t[r][4 * c]) = v;
+  }
+}
+
 // ------------------------------------------------ Laplacian of (u,v), one level
-// Tile inputs U, V (ring 1) in shared memory: local (a,b) <-> global (i0-1+a, j0-1+b).
+// Tiles U, V in ring-2 layout: local (a,b) <-> global (i0-2+a, j0-2+b).
 // Produces ZE at (i0-1+a, j0-1+b) and DI at (i0+a, j0+b), a in [0,TW], b in [0,TH],
 // following laplacian.c:59-81: ZE(i,0) = 0 and DI(i,ny+1) fixed at the walls;
 // ZE(0,j) and DI(nx+1,j) are the wrapped values ZE(nx,j) and DI(1,j),
 // evaluated at their source column from the global arrays gU, gV.
-template <typename TG>
-__device__ __forceinline__ void zeta_div(const KP& p, int i0, int j0, const float (*su)[TW + 2],
-                                         const float (*sv)[TW + 2], const TG* gU, const TG* gV,
-                                         float (*ze)[TW + 1], float (*di)[TW + 1]) {
-  const int W = p.W, nx = p.nx, ny = p.ny;
+__device__ __forceinline__ void zeta_div(const KP& p, const Rows& rc, int i0, int j0, const Tile& su, const Tile& sv,
+                                         const float* gU, const float* gV, float (*ze)[TW + 1],
+                                         float (*di)[TW + 1]) {
+  const int P = p.P, nx = p.nx, ny = p.ny;
   for (int t = threadIdx.x; t < (TW + 1) * (TH + 1); t += NT) {
     const int a = t % (TW + 1), b = t / (TW + 1);
-    // ZE at (i, j) = (i0 - 1 + a, j0 - 1 + b)
-    {
+    {  // ZE at (i, j) = (i0 - 1 + a, j0 - 1 + b)
       const int i = i0 - 1 + a, j = j0 - 1 + b;
       float z = 0.f;
       if (j >= 1 && j <= ny && i <= nx) {
-        const float idxv = Q(p, Q_IDXV, j), idyc1 = Q(p, Q_IDYC, j + 1), dxc1 = Q(p, Q_DXC, j + 1),
-                    dxc = Q(p, Q_DXC, j);
         float v1, v0, u1, u0;
         if (i >= 1) {
-          v1 = sv[b][a + 1]; v0 = sv[b][a]; u1 = su[b + 1][a]; u0 = su[b][a];
+          v1 = sv[b + 1][a + 2]; v0 = sv[b + 1][a + 1]; u1 = su[b + 2][a + 1]; u0 = su[b + 1][a + 1];
         } else {  // i == 0: ZE(nx, j) from the source column
-          v1 = (float)gV[IX(W, nx + 1, j)]; v0 = (float)gV[IX(W, nx, j)];
-          u1 = (float)gU[IX(W, nx, j + 1)]; u0 = (float)gU[IX(W, nx, j)];
+          v1 = gV[IX32(P, nx + 1, j)]; v0 = gV[IX32(P, nx, j)];
+          u1 = gU[IX32(P, nx, j + 1)]; u0 = gU[IX32(P, nx, j)];
         }
-        z = idxv * ((v1 - v0) - idyc1 * (dxc1 * u1 - dxc * u0));
+        z = Q(rc, Q_IDXV, j) * ((v1 - v0) - Q(rc, Q_IDYC, j + 1) * (Q(rc, Q_DXC, j + 1) * u1 - Q(rc, Q_DXC, j) * u0));
       }
       ze[b][a] = z;
     }
-    // DI at (i, j) = (i0 + a, j0 + b)
-    {
+    {  // DI at (i, j) = (i0 + a, j0 + b)
       const int i = i0 + a, j = j0 + b;
       float d = 0.f;
       if (j >= 1 && j <= ny && i >= 1 && i <= nx + 1) {
-        const float idxe = Q(p, Q_IDXE, j), idyn = Q(p, Q_IDYN, j), dxv = Q(p, Q_DXV, j),
-                    dxvs = Q(p, Q_DXV, j - 1);
         float uc, uw, vc, vs;
         if (i <= nx) {
-          uc = su[b + 1][a + 1]; uw = su[b + 1][a]; vc = sv[b + 1][a + 1]; vs = sv[b][a + 1];
+          uc = su[b + 2][a + 2]; uw = su[b + 2][a + 1]; vc = sv[b + 2][a + 2]; vs = sv[b + 1][a + 2];
         } else {  // i == nx + 1: DI(1, j) from the source column
-          uc = (float)gU[IX(W, 1, j)]; uw = (float)gU[IX(W, 0, j)];
-          vc = (float)gV[IX(W, 1, j)]; vs = (float)gV[IX(W, 1, j - 1)];
+          uc = gU[IX32(P, 1, j)]; uw = gU[IX32(P, 0, j)];
+          vc = gV[IX32(P, 1, j)]; vs = gV[IX32(P, 1, j - 1)];
         }
-        d = idxe * ((uc - uw) + idyn * (dxv * vc - dxvs * vs));
+        d = Q(rc, Q_IDXE, j) * ((uc - uw) + Q(rc, Q_IDYN, j) * (Q(rc, Q_DXV, j) * vc - Q(rc, Q_DXV, j - 1) * vs));
       } else if (j == ny + 1 && i >= 1 && i <= nx) {
-        d = (su[b][a + 1] - su[b][a]) * Q(p, Q_IDXE, ny);  // laplacian.c:73
+        d = (su[b + 1][a + 2] - su[b + 1][a + 1]) * Q(rc, Q_IDXE, ny);  // laplacian.c:73
       }
       di[b][a] = d;
     }
@@ -185,121 +247,122 @@ __device__ __forceinline__ void zeta_div(const KP& p, int i0, int j0, const floa
 }
 
 // Second pass at tile cell (a,b) (laplacian.c:83-89).
-__device__ __forceinline__ void lap_out(const KP& p, int j, int a, int b, const float (*ze)[TW + 1],
+__device__ __forceinline__ void lap_out(const Rows& rc, int j, int a, int b, const float (*ze)[TW + 1],
                                         const float (*di)[TW + 1], float& lu, float& lv) {
-  lu = -Q(p, Q_IDYN, j) * (ze[b + 1][a + 1] - ze[b][a + 1]) + Q(p, Q_IDXC, j) * (di[b][a + 1] - di[b][a]);
-  lv = Q(p, Q_IDXV, j) * (ze[b + 1][a + 1] - ze[b + 1][a]) + Q(p, Q_IDYC, j + 1) * (di[b + 1][a] - di[b][a]);
-}
-
-template <typename TG>
-__device__ __forceinline__ void load_ring1(const KP& p, int i0, int j0, const TG* U, const TG* V,
-                                           float (*su)[TW + 2], float (*sv)[TW + 2]) {
-  const int W = p.W;
-  for (int t = threadIdx.x; t < (TW + 2) * (TH + 2); t += NT) {
-    const int a = t % (TW + 2), b = t / (TW + 2);
-    const int i = min(i0 - 1 + a, p.nx + 2), j = min(j0 - 1 + b, p.ny + 2);
-    su[b][a] = (float)U[IX(W, i, j)];
-    sv[b][a] = (float)V[IX(W, i, j)];
-  }
+  lu = -Q(rc, Q_IDYN, j) * (ze[b + 1][a + 1] - ze[b][a + 1]) + Q(rc, Q_IDXC, j) * (di[b][a + 1] - di[b][a]);
+  lv = Q(rc, Q_IDXV, j) * (ze[b + 1][a + 1] - ze[b + 1][a]) + Q(rc, Q_IDYC, j + 1) * (di[b + 1][a] - di[b][a]);
 }
 
 // ------------------------------------------------------------------ kernels
-__global__ void __launch_bounds__(NT) k_lap1(KP p, const double* __restrict__ u, const double* __restrict__ v,
+__global__ void __launch_bounds__(NT) k_lap1(KP p, const float* __restrict__ u, const float* __restrict__ v,
                                              float* Lu, float* Lv) {
-  __shared__ float su[TH + 2][TW + 2], sv[TH + 2][TW + 2];
+  __shared__ __align__(16) Tile su, sv;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
+  __shared__ RowCache sq;
   const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
-  load_ring1(p, i0, j0, u, v, su, sv);
+  fill_rows(p, j0, sq);
+  const Rows rc{sq, j0};
+  load_tile(u, p.P, i0, j0, su);
+  load_tile(v, p.P, i0, j0, sv);
   __syncthreads();
-  zeta_div(p, i0, j0, su, sv, u, v, ze, di);
+  zeta_div(p, rc, i0, j0, su, sv, u, v, ze, di);
   __syncthreads();
   const int a = threadIdx.x % TW, b = threadIdx.x / TW;
   const int i = i0 + a, j = j0 + b;
   if (i > p.nx || j > p.ny) return;
   float lu, lv;
-  lap_out(p, j, a, b, ze, di, lu, lv);
-  put<IMG_LU>(Lu, p.W, p.nx, p.ny, i, j, lu);
-  put<IMG_LV>(Lv, p.W, p.nx, p.ny, i, j, lv);
+  lap_out(rc, j, a, b, ze, di, lu, lv);
+  put<IMG_LU>(Lu, p.P, p.nx, p.ny, i, j, lu);
+  put<IMG_LV>(Lv, p.P, p.nx, p.ny, i, j, lv);
 }
 
-struct Main1Out {
-  double* eta_next;
-  float* hist_eta;  // slot for Deta_n
+struct Main1Io {
+  const double* eta;        // FP64 perturbation (pitch W)
+  const float* es; const float* us; const float* vs;  // FP32 shadows (pitch P)
+  const float* Lu; const float* Lv;
+  const float* h1; const float* h2;
+  double* eta_next; float* es_next;
+  float* hist_eta;          // slot for Deta_n
   float* dup; float* dvp;
-  unsigned* cfl;    // 2 floats as bits (max |u|/dx, max |v|/dy)
+  unsigned* cfl;            // 2 floats as bits (max |u|/dx, max |v|/dy)
   int* bad;
 };
 
 template <int SCH>
-__global__ void __launch_bounds__(NT) k_main1(KP p, const double* __restrict__ eta, const double* __restrict__ u,
-                                              const double* __restrict__ v, const float* __restrict__ Lu,
-                                              const float* __restrict__ Lv, const float* __restrict__ h1,
-                                              const float* __restrict__ h2, Main1Out o) {
-  __shared__ float se[TH + 4][TW + 4], su[TH + 4][TW + 4], sv[TH + 4][TW + 4];
-  __shared__ float sl[TH + 2][TW + 2], sm[TH + 2][TW + 2];
+__global__ void __launch_bounds__(NT) k_main1(KP p, Main1Io o) {
+  __shared__ __align__(16) Tile se, su, sv, sl, sm;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
   __shared__ float red[2][NT / 32];
-  const int W = p.W, nx = p.nx, ny = p.ny;
+  __shared__ RowCache sq;
+  const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
   const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
-  // ring-2 tile of eta (perturbation), u, v (+ winds)
-  for (int t = threadIdx.x; t < (TW + 4) * (TH + 4); t += NT) {
-    const int a = t % (TW + 4), b = t / (TW + 4);
-    const int i = min(i0 - 2 + a, nx + 2), j = min(j0 - 2 + b, ny + 2);
-    const int q = IX(W, i, j);
-    se[b][a] = (float)eta[q];
-    float uu = (float)u[q], vv = (float)v[q];
-    if (p.extra) { uu += p.wx[q]; vv += p.wy[q]; }
-    su[b][a] = uu;
-    sv[b][a] = vv;
-  }
-  load_ring1(p, i0, j0, Lu, Lv, sl, sm);
-  __syncthreads();
-  zeta_div(p, i0, j0, sl, sm, Lu, Lv, ze, di);
-  __syncthreads();
-
+  // this thread's own cell: issue its global loads before the tile traffic
   const int a = threadIdx.x % TW + 2, b = threadIdx.x / TW + 2;  // ring-2 local coordinates
   const int i = i0 + a - 2, j = j0 + b - 2;
   const bool live = (i <= nx && j <= ny);
+  const int q = IX(W, live ? i : 1, live ? j : 1), q32 = IX32(P, i, j);
+  const double eta_old = o.eta[q];
+  const float h1v = (p.k >= 1) ? o.h1[q32] : 0.f, h2v = (p.k >= 2) ? o.h2[q32] : 0.f;
+  fill_rows(p, j0, sq);
+  const Rows rc{sq, j0};
+  load_tile(o.es, P, i0, j0, se);
+  load_tile(o.us, P, i0, j0, su);
+  load_tile(o.vs, P, i0, j0, sv);
+  load_tile(o.Lu, P, i0, j0, sl);
+  load_tile(o.Lv, P, i0, j0, sm);
+  __syncthreads();
+  if (p.extra) {  // UWINDX, VWINDY (sw.h:216-217); the bottom enters H below
+    for (int t = threadIdx.x; t < (TH + 4) * (TW + 4); t += NT) {
+      const int a = t % (TW + 4), b = t / (TW + 4);
+      const int q = IX32(P, i0 - 2 + a, j0 - 2 + b);
+      su[b][a] += p.wx[q];
+      sv[b][a] += p.wy[q];
+    }
+    __syncthreads();
+  }
+  zeta_div(p, rc, i0, j0, sl, sm, o.Lu, o.Lv, ze, di);
+  __syncthreads();
+
   float mxu = 0.f, mxv = 0.f;
   if (live) {
-    const int q = IX(W, i, j);
     // ---- mass (BODYH, calc.c:70-113), H relative to the row reference Hb(j)
     float qx[5], qy[5];
 #pragma unroll
     for (int s = -2; s <= 2; s++) qx[s + 2] = se[b][a + s];
-    qy[0] = se[b - 2][a] + Q(p, Q_DHBM2, j);
-    qy[1] = se[b - 1][a] + Q(p, Q_DHBM1, j);
+    qy[0] = se[b - 2][a] + Q(rc, Q_DHBM2, j);
+    qy[1] = se[b - 1][a] + Q(rc, Q_DHBM1, j);
     qy[2] = qx[2];
-    qy[3] = se[b + 1][a] + Q(p, Q_DHBP1, j);
-    qy[4] = se[b + 2][a] + Q(p, Q_DHBP2, j);
+    qy[3] = se[b + 1][a] + Q(rc, Q_DHBP1, j);
+    qy[4] = se[b + 2][a] + Q(rc, Q_DHBP2, j);
     if (p.extra) {
 #pragma unroll
       for (int s = -2; s <= 2; s++) {
-        qx[s + 2] -= p.hb[IX(W, i + s, j)];
-        qy[s + 2] -= p.hb[IX(W, i, j + s)];
+        qx[s + 2] -= p.hb[IX32(P, i + s, j)];
+        qy[s + 2] -= p.hb[IX32(P, i, j + s)];
       }
     }
-    const float kx = Q(p, Q_KXE, j), ky = Q(p, Q_KYN, j);
+    const float kx = Q(rc, Q_KXE, j), ky = Q(rc, Q_KYN, j);
     const float cw = su[b][a - 1] * kx, ce = su[b][a] * kx, cs = sv[b - 1][a] * ky, cn = sv[b][a] * ky;
     float deta = face1<SCH>(qx[0], qx[1], qx[2], qx[3], cw) - face1<SCH>(qx[1], qx[2], qx[3], qx[4], ce) +
                  face1<SCH>(qy[0], qy[1], qy[2], qy[3], cs) - face1<SCH>(qy[1], qy[2], qy[3], qy[4], cn);
-    deta += Q(p, Q_HB, j) * ((cw - ce) + (cs - cn));
-    deta -= p.sig2dt * (Q(p, Q_EREF, j) + se[b][a]);
+    deta += Q(rc, Q_HB, j) * ((cw - ce) + (cs - cn));
+    deta -= p.sig2dt * (Q(rc, Q_EREF, j) + se[b][a]);
     // Adams-Bashforth (calc.c:651-699) then the geofactor (calc.c:403-422)
     float ab;
     if (p.k == 0) ab = deta;
-    else if (p.k == 1) ab = 1.5f * deta - 0.5f * h1[q];
-    else ab = (23.f / 12.f) * deta - (4.f / 3.f) * h1[q] + (5.f / 12.f) * h2[q];
-    const float hcell = Q(p, Q_HB, j) + qx[2];
-    ab -= Q(p, Q_GEO, j) * hcell * 0.5f * (sv[b][a] + sv[b - 1][a]);
-    o.hist_eta[q] = deta;
-    const double en = eta[q] + (double)ab;
+    else if (p.k == 1) ab = 1.5f * deta - 0.5f * h1v;
+    else ab = (23.f / 12.f) * deta - (4.f / 3.f) * h1v + (5.f / 12.f) * h2v;
+    const float hcell = Q(rc, Q_HB, j) + qx[2];
+    ab -= Q(rc, Q_GEO, j) * hcell * 0.5f * (sv[b][a] + sv[b - 1][a]);
+    o.hist_eta[q32] = deta;
+    const double en = eta_old + f2d(ab);
     put<IMG_ETA>(o.eta_next, W, nx, ny, i, j, en);
-    if (!(en >= -1e10 && en <= 1e10)) atomicOr(o.bad, 1);
+    put<IMG_ETA>(o.es_next, P, nx, ny, i, j, d2f(en));
+    if (!in_range(en)) atomicOr(o.bad, 1);
 
     // ---- second Laplacian of (u, v) from L (laplacian.c:83-89)
     float llu, llv;
-    lap_out(p, j, a - 2, b - 2, ze, di, llu, llv);
+    lap_out(rc, j, a - 2, b - 2, ze, di, llu, llv);
 
     // ---- BODYU (calc.c:168-200)
     {
@@ -308,17 +371,17 @@ __global__ void __launch_bounds__(NT) k_main1(KP p, const double* __restrict__ e
       for (int s = -2; s <= 2; s++) { ux[s + 2] = su[b][a + s]; uy[s + 2] = su[b + s][a]; }
       const float uwm = ux[1], u0 = ux[2], uep = ux[3];
       const float vs0 = sv[b - 1][a], vs1 = sv[b - 1][a + 1], vn0 = sv[b][a], vn1 = sv[b][a + 1];
-      const float kc = Q(p, Q_KXC, j), kv = Q(p, Q_KYV, j);
+      const float kc = Q(rc, Q_KXC, j), kv = Q(rc, Q_KYV, j);
       float p1 = face2<SCH>(ux[0], ux[1], ux[2], ux[3], cpos2(uwm, u0, kc), cneg2(uwm, u0, kc)) -
                  face2<SCH>(ux[1], ux[2], ux[3], ux[4], cpos2(u0, uep, kc), cneg2(u0, uep, kc)) +
                  face2<SCH>(uy[0], uy[1], uy[2], uy[3], cpos2(vs0, vs1, kv), cneg2(vs0, vs1, kv)) -
                  face2<SCH>(uy[1], uy[2], uy[3], uy[4], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv));
-      const float p2 = u0 * (uep - uwm) * Q(p, Q_K2XE, j) + u0 * (0.5f * (vn0 + vn1) - 0.5f * (vs0 + vs1)) * kv;
-      const float ul = (float)u[q];
+      const float p2 = u0 * (uep - uwm) * Q(rc, Q_K2XE, j) + u0 * (0.5f * (vn0 + vn1) - 0.5f * (vs0 + vs1)) * kv;
+      const float ul = p.extra ? o.us[q32] : u0;  // dissipation acts on U without the wind
       float du = p1 + p2 - ul * p.sigdt;
-      du += p.nu2dt * Lu[q] + p.nu4dt * llu;
-      o.dup[q] = du;
-      mxu = fabsf(u0) * Q(p, Q_IDXE, j);
+      du += p.nu2dt * sl[b][a] + p.nu4dt * llu;
+      o.dup[q32] = du;
+      mxu = fabsf(u0) * Q(rc, Q_IDXE, j);
     }
     // ---- BODYV (calc.c:205-237)
     {
@@ -327,17 +390,17 @@ __global__ void __launch_bounds__(NT) k_main1(KP p, const double* __restrict__ e
       for (int s = -2; s <= 2; s++) { vx[s + 2] = sv[b][a + s]; vy[s + 2] = sv[b + s][a]; }
       const float vsm = vy[1], v0 = vy[2], vnp = vy[3];
       const float uw1 = su[b + 1][a - 1], uw0 = su[b][a - 1], ue1 = su[b + 1][a], ue0 = su[b][a];
-      const float kxv = Q(p, Q_KXV, j), kyc = Q(p, Q_KYC, j);
+      const float kxv = Q(rc, Q_KXV, j), kyc = Q(rc, Q_KYC, j);
       float p1 = face2<SCH>(vx[0], vx[1], vx[2], vx[3], cpos2(uw1, uw0, kxv), cneg2(uw1, uw0, kxv)) -
                  face2<SCH>(vx[1], vx[2], vx[3], vx[4], cpos2(ue1, ue0, kxv), cneg2(ue1, ue0, kxv)) +
                  face2<SCH>(vy[0], vy[1], vy[2], vy[3], cpos2(vsm, v0, kyc), cneg2(vsm, v0, kyc)) -
                  face2<SCH>(vy[1], vy[2], vy[3], vy[4], cpos2(v0, vnp, kyc), cneg2(v0, vnp, kyc));
-      const float p2 = v0 * (0.5f * (ue0 + ue1) - 0.5f * (uw0 + uw1)) * kxv + v0 * (vnp - vsm) * Q(p, Q_KDYNS, j);
-      const float vl = (float)v[q];
+      const float p2 = v0 * (0.5f * (ue0 + ue1) - 0.5f * (uw0 + uw1)) * kxv + v0 * (vnp - vsm) * Q(rc, Q_KDYNS, j);
+      const float vl = p.extra ? o.vs[q32] : v0;
       float dv = p1 + p2 - vl * p.sigdt;
-      dv += p.nu2dt * Lv[q] + p.nu4dt * llv;
-      o.dvp[q] = dv;
-      mxv = fabsf(v0) * Q(p, Q_IDYN, j);
+      dv += p.nu2dt * sm[b][a] + p.nu4dt * llv;
+      o.dvp[q32] = dv;
+      mxv = fabsf(v0) * Q(rc, Q_IDYN, j);
     }
   }
   // CFL maxima of this block (calc.c:705-712)
@@ -355,56 +418,87 @@ __global__ void __launch_bounds__(NT) k_main1(KP p, const double* __restrict__ e
 }
 
 struct Main2Io {
-  const double* u; const double* v;      // state at step start
+  const float* es;                        // new eta shadow
+  const double* u; const double* v;       // FP64 state at step start (pitch W)
+  const float* us; const float* vs;       // and its shadows (pitch P)
   double* u_next; double* v_next;
+  float* us_next; float* vs_next;
   const float* dup; const float* dvp;
   const float* hu1; const float* hu2; const float* hv1; const float* hv2;
-  float* hu0; float* hv0;                // slots for Du_n, Dv_n
+  float* hu0; float* hv0;                 // slots for Du_n, Dv_n
   int* bad;
 };
 
 // Pressure (calc.c:500-540), AB, Coriolis u then v (calc.c:542-598).
-__global__ void __launch_bounds__(NT) k_main2(KP p, const double* __restrict__ eta_new, Main2Io io) {
-  __shared__ float se[TH + 2][TW + 2], su[TH + 2][TW + 2], sv[TH + 2][TW + 2];
-  __shared__ float un[TH + 1][TW + 1];  // new u at (i0-1+a, j0+b)
-  const int W = p.W, nx = p.nx, ny = p.ny;
+__global__ void __launch_bounds__(NT) k_main2(KP p, Main2Io io) {
+  __shared__ __align__(16) Tile se, su, sv;  // ring-2 windows, ring 1 used
+  __shared__ float un[TH + 1][TW + 1];       // new u at (i0-1+a, j0+b)
+  __shared__ RowCache sq;
+  const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
   const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
-  for (int t = threadIdx.x; t < (TW + 2) * (TH + 2); t += NT) {
-    const int a = t % (TW + 2), b = t / (TW + 2);
-    const int i = min(i0 - 1 + a, nx + 2), j = min(j0 - 1 + b, ny + 2);
-    const int q = IX(W, i, j);
-    se[b][a] = (float)eta_new[q];
-    su[b][a] = (float)io.u[q];  // Coriolis uses U and V without the winds
-    sv[b][a] = (float)io.v[q];
+  // own cell of the v update: issue its global loads first
+  const int ac = threadIdx.x % TW, bc = threadIdx.x / TW;
+  const int ic = i0 + ac, jc = j0 + bc;
+  const bool livec = (ic <= nx && jc <= ny);
+  const int qc = IX(W, livec ? ic : 1, livec ? jc : 1), qc32 = IX32(P, ic, jc);
+  const double v_old = io.v[qc];
+  const float dvp_c = io.dvp[qc32];
+  const float hv1_c = (p.k >= 1) ? io.hv1[qc32] : 0.f, hv2_c = (p.k >= 2) ? io.hv2[qc32] : 0.f;
+  // the (at most two) positions of the new-u region this thread updates:
+  // their global operands are loaded now as well
+  constexpr int NU = (TW + 1) * (TH + 1);
+  float pre_dup[2], pre_h1[2], pre_h2[2];
+  double pre_u[2];
+#pragma unroll
+  for (int s2 = 0; s2 < 2; s2++) {
+    const int t = threadIdx.x + s2 * NT;
+    const int a = t % (TW + 1), b = t / (TW + 1);
+    const int i = i0 - 1 + a, j = j0 + b;
+    const bool comp = (t < NU) && (i >= 1 && i <= nx && j <= ny);
+    const bool own = comp && a >= 1 && b < TH;
+    const int q32 = IX32(P, comp ? i : 1, comp ? j : 1);
+    pre_dup[s2] = comp ? io.dup[q32] : 0.f;
+    pre_h1[s2] = (comp && p.k >= 1) ? io.hu1[q32] : 0.f;
+    pre_h2[s2] = (comp && p.k >= 2) ? io.hu2[q32] : 0.f;
+    pre_u[s2] = own ? io.u[IX(W, i, j)] : 0.0;
   }
+  fill_rows(p, j0, sq);
+  const Rows rc{sq, j0};
+  load_tile(io.es, P, i0, j0, se);
+  load_tile(io.us, P, i0, j0, su);  // Coriolis uses U and V without the winds
+  load_tile(io.vs, P, i0, j0, sv);
   __syncthreads();
   // new u on [i0-1, i0+TW-1] x [j0, j0+TH]: interior cells recomputed, the
   // halo column 0 and the halo row ny+1 keep the old u (the v update reads
   // them before the halo refresh, core.c:283-289)
-  for (int t = threadIdx.x; t < (TW + 1) * (TH + 1); t += NT) {
+#pragma unroll
+  for (int s2 = 0; s2 < 2; s2++) {
+    const int t = threadIdx.x + s2 * NT;
+    if (t >= NU) break;
     const int a = t % (TW + 1), b = t / (TW + 1);
     const int i = i0 - 1 + a, j = j0 + b;
-    const int la = a, lb = b + 1;  // ring-1 local of (i, j)
+    const int la = a + 1, lb = b + 2;  // ring-2 local of (i, j)
     float val = 0.f;
     if (i <= nx && j <= ny + 1) {
       if (i >= 1 && j <= ny) {
-        const int q = IX(W, i, j);
-        const float dun = io.dup[q] + Q(p, Q_GEX, j) * (se[lb][la + 1] - se[lb][la]);
+        const int q32 = IX32(P, i, j);
+        const float dun = pre_dup[s2] + Q(rc, Q_GEX, j) * (se[lb][la + 1] - se[lb][la]);
         float ab;
         if (p.k == 0) ab = dun;
-        else if (p.k == 1) ab = 1.5f * dun - 0.5f * io.hu1[q];
-        else ab = (23.f / 12.f) * dun - (4.f / 3.f) * io.hu1[q] + (5.f / 12.f) * io.hu2[q];
+        else if (p.k == 1) ab = 1.5f * dun - 0.5f * pre_h1[s2];
+        else ab = (23.f / 12.f) * dun - (4.f / 3.f) * pre_h1[s2] + (5.f / 12.f) * pre_h2[s2];
         const float uu = su[lb][la];
         const float semi = 0.25f * (sv[lb][la] + sv[lb][la + 1] + sv[lb - 1][la] + sv[lb - 1][la + 1]);
-        const float al = Q(p, Q_DTFE, j) + uu * Q(p, Q_GEO, j);
+        const float al = Q(rc, Q_DTFE, j) + uu * Q(rc, Q_GEO, j);
         const float be = 0.25f * al * al;
         const float du = __fdividef(ab - 2.f * be * uu + al * semi, 1.f + be);
         val = uu + du;
         if (a >= 1 && b < TH) {  // a cell of this tile: accumulate in FP64 and write
-          io.hu0[q] = dun;
-          const double unew = io.u[q] + (double)du;
+          io.hu0[q32] = dun;
+          const double unew = pre_u[s2] + f2d(du);
           put<IMG_U>(io.u_next, W, nx, ny, i, j, unew);
-          if (!(unew >= -1e10 && unew <= 1e10)) atomicOr(io.bad, 1);
+          put<IMG_U>(io.us_next, P, nx, ny, i, j, d2f(unew));
+          if (!in_range(unew)) atomicOr(io.bad, 1);
         }
       } else {
         val = su[lb][la];
@@ -413,42 +507,60 @@ __global__ void __launch_bounds__(NT) k_main2(KP p, const double* __restrict__ e
     un[b][a] = val;
   }
   __syncthreads();
-  const int a = threadIdx.x % TW, b = threadIdx.x / TW;
-  const int i = i0 + a, j = j0 + b;
-  if (i > nx || j > ny) return;
-  const int q = IX(W, i, j);
-  const int la = a + 1, lb = b + 1;
-  const float dvn = io.dvp[q] + Q(p, Q_GNY, j) * (se[lb + 1][la] - se[lb][la] + Q(p, Q_DHBP1, j));
+  if (!livec) return;
+  const int a = ac, b = bc, i = ic, j = jc, q32 = qc32;
+  const int la = a + 2, lb = b + 2;
+  const float dvn = dvp_c + Q(rc, Q_GNY, j) * (se[lb + 1][la] - se[lb][la] + Q(rc, Q_DHBP1, j));
   float ab;
   if (p.k == 0) ab = dvn;
-  else if (p.k == 1) ab = 1.5f * dvn - 0.5f * io.hv1[q];
-  else ab = (23.f / 12.f) * dvn - (4.f / 3.f) * io.hv1[q] + (5.f / 12.f) * io.hv2[q];
+  else if (p.k == 1) ab = 1.5f * dvn - 0.5f * hv1_c;
+  else ab = (23.f / 12.f) * dvn - (4.f / 3.f) * hv1_c + (5.f / 12.f) * hv2_c;
   const float vv = sv[lb][la];
   // un local: (i-1, j+1) -> (a, b+1), (i, j+1) -> (a+1, b+1), (i, j) -> (a+1, b), (i-1, j) -> (a, b)
   const float semi = 0.25f * (un[b + 1][a] + un[b + 1][a + 1] + un[b][a + 1] + un[b][a]);
-  const float al = Q(p, Q_DTFN, j) + semi * Q(p, Q_CV, j);
+  const float al = Q(rc, Q_DTFN, j) + semi * Q(rc, Q_CV, j);
   const float be = 0.25f * al * al;
   const float dv = __fdividef(ab - 2.f * be * vv - al * semi, 1.f + be);
-  io.hv0[q] = dvn;
-  const double vnew = io.v[q] + (double)dv;
+  io.hv0[q32] = dvn;
+  const double vnew = v_old + f2d(dv);
   put<IMG_V>(io.v_next, W, nx, ny, i, j, vnew);
-  if (!(vnew >= -1e10 && vnew <= 1e10)) atomicOr(io.bad, 1);
+  put<IMG_V>(io.vs_next, P, nx, ny, i, j, d2f(vnew));
+  if (!in_range(vnew)) atomicOr(io.bad, 1);
+}
+
+// FP32 shadow of an FP64 field over all padded cells (pitch W -> pitch P).
+__global__ void k_shadow(float* dst, const double* src, int nx, int ny, int W, int P) {
+  const int n = W * (ny + 4);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int r = t / W, c = t - r * W;
+    dst[(size_t)r * P + c] = d2f(src[t]);
+  }
 }
 
 template <int SCH>
-void launch_main1(dim3 g, cudaStream_t st, const KP& p, const double* eta, const double* u, const double* v,
-                  const float* Lu, const float* Lv, const float* h1, const float* h2, const Main1Out& o) {
-  k_main1<SCH><<<g, NT, 0, st>>>(p, eta, u, v, Lu, Lv, h1, h2, o);
+void launch_main1(dim3 g, cudaStream_t st, const KP& p, const Main1Io& o) {
+  k_main1<SCH><<<g, NT, 0, st>>>(p, o);
 }
 
 }  // namespace f32
 
 using namespace f32;
 
+void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStream_t st) {
+  const int W = nx + 4, n = W * (ny + 4);
+  const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_shadow<<<blocks, 256, 0, st>>>(dst, src, nx, ny, W, P);
+}
+
+void fp32_geometry(int nx, int ny, int* P, int* R) {
+  *P = TW * ((nx + TW - 1) / TW) + 4;
+  *R = TH * ((ny + TH - 1) / TH) + 4;
+}
+
 // ------------------------------------------------------------------ host
 void Fp32Engine::step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers* tm, int& nl) {
   KP p{};
-  p.nx = c.nx; p.ny = c.ny; p.W = c.nx + 4; p.H = c.ny + 4;
+  p.nx = c.nx; p.ny = c.ny; p.W = c.nx + 4; p.H = c.ny + 4; p.P = c.P;
   p.q = c.q;
   p.sig2dt = c.sig2dt; p.sigdt = c.sigdt; p.nu2dt = c.nu2dt; p.nu4dt = c.nu4dt;
   p.k = k;
@@ -462,23 +574,25 @@ void Fp32Engine::step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers
     if (tm && tm->on) tm->end(st);              \
     nl++;                                       \
   } while (0)
-  LAUNCH("f32_lap1", k_lap1<<<g, NT, 0, st>>>(p, u[cur], v[cur], Lu, Lv));
-  Main1Out o1{eta[1 - cur], heta[0], dup, dvp, cfl + 2 * slot, bad + slot};
+  LAUNCH("f32_lap1", k_lap1<<<g, NT, 0, st>>>(p, us[cur], vs[cur], Lu, Lv));
+  Main1Io o1{eta[cur], es[cur], us[cur], vs[cur], Lu, Lv, heta[1], heta[2], eta[1 - cur], es[1 - cur],
+             heta[0], dup, dvp, cfl + 2 * slot, bad + slot};
   switch (c.sch) {
-    case 0: LAUNCH("f32_main1", launch_main1<0>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 1: LAUNCH("f32_main1", launch_main1<1>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 2: LAUNCH("f32_main1", launch_main1<2>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 3: LAUNCH("f32_main1", launch_main1<3>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 4: LAUNCH("f32_main1", launch_main1<4>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 5: LAUNCH("f32_main1", launch_main1<5>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 6: LAUNCH("f32_main1", launch_main1<6>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 7: LAUNCH("f32_main1", launch_main1<7>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 8: LAUNCH("f32_main1", launch_main1<8>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    case 9: LAUNCH("f32_main1", launch_main1<9>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
-    default: LAUNCH("f32_main1", launch_main1<kVanLeerSafe>(g, st, p, eta[cur], u[cur], v[cur], Lu, Lv, heta[1], heta[2], o1)); break;
+    case 0: LAUNCH("f32_main1", launch_main1<0>(g, st, p, o1)); break;
+    case 1: LAUNCH("f32_main1", launch_main1<1>(g, st, p, o1)); break;
+    case 2: LAUNCH("f32_main1", launch_main1<2>(g, st, p, o1)); break;
+    case 3: LAUNCH("f32_main1", launch_main1<3>(g, st, p, o1)); break;
+    case 4: LAUNCH("f32_main1", launch_main1<4>(g, st, p, o1)); break;
+    case 5: LAUNCH("f32_main1", launch_main1<5>(g, st, p, o1)); break;
+    case 6: LAUNCH("f32_main1", launch_main1<6>(g, st, p, o1)); break;
+    case 7: LAUNCH("f32_main1", launch_main1<7>(g, st, p, o1)); break;
+    case 8: LAUNCH("f32_main1", launch_main1<8>(g, st, p, o1)); break;
+    case 9: LAUNCH("f32_main1", launch_main1<9>(g, st, p, o1)); break;
+    default: LAUNCH("f32_main1", launch_main1<kVanLeerSafe>(g, st, p, o1)); break;
   }
-  Main2Io io{u[cur], v[cur], u[1 - cur], v[1 - cur], dup, dvp, hu[1], hu[2], hv[1], hv[2], hu[0], hv[0], bad + slot};
-  LAUNCH("f32_main2", k_main2<<<g, NT, 0, st>>>(p, eta[1 - cur], io));
+  Main2Io io{es[1 - cur], u[cur], v[cur], us[cur], vs[cur], u[1 - cur], v[1 - cur], us[1 - cur], vs[1 - cur],
+             dup, dvp, hu[1], hu[2], hv[1], hv[2], hu[0], hv[0], bad + slot};
+  LAUNCH("f32_main2", k_main2<<<g, NT, 0, st>>>(p, io));
 #undef LAUNCH
   // the slot just written becomes n-1, n-1 becomes n-2, n-2 is reused
   float* t;

@@ -117,6 +117,7 @@ enum Q32 {
 
 struct Fp32Ctx {
   int nx, ny, sch, extra;
+  int P, R;  // FP32 arrays: row pitch and rows (padded so tile windows stay in bounds)
   const float* q;
   float sig2dt, sigdt, nu2dt, nu4dt;
   const float* wx; const float* wy; const float* hb;
@@ -126,6 +127,9 @@ struct Fp32Engine {
   double* eta[2] = {nullptr, nullptr};  // eta - eta_ref(j), double-buffered
   double* u[2] = {nullptr, nullptr};
   double* v[2] = {nullptr, nullptr};
+  float* es[2] = {nullptr, nullptr};  // FP32 shadows of the state (pitch P)
+  float* us[2] = {nullptr, nullptr};
+  float* vs[2] = {nullptr, nullptr};
   int cur = 0;
   float* heta[3] = {nullptr, nullptr, nullptr};  // [0] slot for step n, [1] n-1, [2] n-2
   float* hu[3] = {nullptr, nullptr, nullptr};
@@ -136,6 +140,11 @@ struct Fp32Engine {
   int* bad = nullptr;       // 1 per step
   void step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers* tm, int& nl);
 };
+
+// FP32 shadow (pitch P) of an FP64 padded field (pitch nx+4), all padded cells.
+void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStream_t st);
+// Pitch and row count of the FP32 arrays for a grid.
+void fp32_geometry(int nx, int ny, int* P, int* R);
 
 // dst = src + ref(j) row by row over a padded field (eta perturbation -> eta)
 void add_row_ref(double* dst, const double* src, const double* ref_rows, int nx, int ny, cudaStream_t st);
