@@ -137,6 +137,35 @@ sw2g_status sw2g_timer_read(const sw2g_ctx *ctx, int idx, const char **name, lon
 
 void sw2g_destroy(sw2g_ctx *ctx);
 
+/* ------------------------------------------------------------------ batches
+ * Ensembles of independent runs (the reference runs one case per MPI job).
+ * A batch steps several SW2G_FP32 contexts together: one launch per phase of
+ * the step covers every tile of every member, grids may differ in size, and
+ * the time loop replays a captured CUDA graph of one step. Members must be
+ * uploaded FP32 contexts on one device with the same limiter; each member's
+ * state stays readable through its own context (sw2g_download, sw2g_diag). */
+typedef struct sw2g_batch sw2g_batch;
+
+sw2g_status sw2g_batch_create(sw2g_ctx *const *members, int n, sw2g_batch **out);
+/* Advances every member nsteps steps. On SW2G_ERR_CFL / SW2G_ERR_NONFINITE
+ * the first failing (step, member) is reported by the two calls below and
+ * through that member's sw2g_error_step. */
+sw2g_status sw2g_batch_step(sw2g_batch *b, int nsteps);
+int sw2g_batch_error_member(const sw2g_batch *b);
+int sw2g_batch_error_step(const sw2g_batch *b);
+double sw2g_batch_last_step_ms(const sw2g_batch *b);
+long long sw2g_batch_last_launches(const sw2g_batch *b);
+
+/* Sweep-schedule autotuner. The order in which the tiles of all members are
+ * assigned to blocks changes no result, so candidates are timed on the live
+ * run: each of the SW2G_SCHEDULES orders advances the batch
+ * steps_per_candidate steps (ms_per_step[s] receives its time per step, may
+ * be NULL), and the fastest is kept. */
+#define SW2G_SCHEDULES 4
+sw2g_status sw2g_batch_tune(sw2g_batch *b, int steps_per_candidate, double *ms_per_step);
+int sw2g_batch_schedule(const sw2g_batch *b);
+void sw2g_batch_destroy(sw2g_batch *b);
+
 /* Largest ny accepted by sw2g_energy_noalloc. */
 #define SW2G_NOALLOC_MAX_ROWS 8192
 

@@ -13,7 +13,100 @@ using namespace sw2g;
 
 namespace {
 
-constexpr int kChunk = 1024;  // steps per check read-back
+constexpr int kChunk = kCheckSlots;  // steps per check read-back
+
+// Launch state of an FP32-form batch: member descriptors, the tile table (the
+// sweep schedule), the device step counter and the captured one-step graph.
+struct BatchExec {
+  MemberDesc* d_desc = nullptr;
+  int4* d_tiles = nullptr;
+  int ntiles = 0;
+  long long* d_counter = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int sch = 0;
+
+  cudaError_t alloc(int nmem, int ntile) {
+    ntiles = ntile;
+    cudaError_t e = cudaMalloc((void**)&d_desc, sizeof(MemberDesc) * nmem);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_tiles, sizeof(int4) * ntile);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_counter, sizeof(long long));
+    return e;
+  }
+  void release() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (d_desc) cudaFree(d_desc);
+    if (d_tiles) cudaFree(d_tiles);
+    if (d_counter) cudaFree(d_counter);
+    exec = nullptr;
+    d_desc = nullptr;
+    d_tiles = nullptr;
+    d_counter = nullptr;
+  }
+  // Enqueues n steps: replays of a captured one-step graph, or direct
+  // launches while per-kernel timers are on.
+  cudaError_t enqueue(int n, cudaStream_t st, Timers* tm, long long& launches) {
+    if (tm && tm->on) {
+      for (int s = 0; s < n; s++) launches += fp32_batch_step(sch, d_desc, d_tiles, ntiles, d_counter, st, tm);
+      return cudaGetLastError();
+    }
+    if (!exec) {
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return e;
+      fp32_batch_step(sch, d_desc, d_tiles, ntiles, d_counter, st, nullptr);
+      e = cudaStreamEndCapture(st, &g);
+      if (e != cudaSuccess) return e;
+      e = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return e;
+    }
+    for (int s = 0; s < n; s++) {
+      cudaError_t e = cudaGraphLaunch(exec, st);
+      if (e != cudaSuccess) return e;
+    }
+    launches += 4LL * n;
+    return cudaSuccess;
+  }
+};
+
+// Tile tables (sweep schedules) over members given as (nbx, nby) pairs.
+enum Schedule { SCHED_ROWS = 0, SCHED_COLS = 1, SCHED_INTERLEAVE = 2, SCHED_BANDS = 3, SCHED_COUNT = 4 };
+
+std::vector<int4> tile_table(const std::vector<int2>& nb, int sched) {
+  std::vector<int4> t;
+  const int M = (int)nb.size();
+  if (sched == SCHED_INTERLEAVE) {
+    std::vector<int> next(M, 0);
+    bool more = true;
+    while (more) {
+      more = false;
+      for (int m = 0; m < M; m++) {
+        const int total = nb[m].x * nb[m].y;
+        if (next[m] < total) {
+          const int k = next[m]++;
+          t.push_back(make_int4(m, k % nb[m].x, k / nb[m].x, 0));
+          more = true;
+        }
+      }
+    }
+    return t;
+  }
+  for (int m = 0; m < M; m++) {
+    const int nbx = nb[m].x, nby = nb[m].y;
+    if (sched == SCHED_COLS) {
+      for (int bx = 0; bx < nbx; bx++)
+        for (int by = 0; by < nby; by++) t.push_back(make_int4(m, bx, by, 0));
+    } else if (sched == SCHED_BANDS) {  // vertical bands of 8 tile columns, rows inside a band
+      for (int b0 = 0; b0 < nbx; b0 += 8)
+        for (int by = 0; by < nby; by++)
+          for (int bx = b0; bx < nbx && bx < b0 + 8; bx++) t.push_back(make_int4(m, bx, by, 0));
+    } else {
+      for (int by = 0; by < nby; by++)
+        for (int bx = 0; bx < nbx; bx++) t.push_back(make_int4(m, bx, by, 0));
+    }
+  }
+  return t;
+}
 
 }  // namespace
 
@@ -51,6 +144,7 @@ struct sw2g_ctx {
   double* d_aux64[3] = {nullptr, nullptr, nullptr};  // windx, windy, hB (FP64) for the diagnostic
   float* d_aux32[3] = {nullptr, nullptr, nullptr};   // the same in FP32 for the stencils
   double* d_tmp = nullptr;         // full eta for download and diagnostics
+  BatchExec run32;                 // this context as a batch of one
 };
 
 namespace {
@@ -400,6 +494,14 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     c32.wx = x->d_aux32[0];
     c32.wy = x->d_aux32[1];
     c32.hb = x->d_aux32[2];
+    int nbx = 0, nby = 0;
+    fp32_tiles(c->nx, c->ny, &nbx, &nby);
+    const std::vector<int4> tiles = tile_table({make_int2(nbx, nby)}, SCHED_ROWS);
+    if ((st = cuda_fail(x->run32.alloc(1, (int)tiles.size()), "batch")) != SW2G_OK) return fail(st);
+    x->run32.sch = c32.sch;
+    if ((st = cuda_fail(cudaMemcpy(x->run32.d_tiles, tiles.data(), tiles.size() * sizeof(int4),
+                                   cudaMemcpyHostToDevice), "tiles")) != SW2G_OK)
+      return fail(st);
   }
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
     return fail(st);
@@ -486,16 +588,21 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
       CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int) * n, x->stream));
     }
     StepChecks chk{x->d_cfl, x->d_bad};
+    if (f32) {
+      const MemberDesc d = fp32_desc(x->c32, x->e32, x->k);
+      CK(cudaMemcpyAsync(x->run32.d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, x->stream));
+      CK(cudaMemsetAsync(x->run32.d_counter, 0, sizeof(long long), x->stream));
+    }
     CK(cudaEventRecord(x->ev[0], x->stream));
-    for (int t = 0; t < n; t++) {
-      if (f32) {
-        int nl = 0;
-        x->e32.step(x->c32, x->k, t, x->stream, &x->timers, nl);
-        x->last_launches += nl;
-      } else {
+    if (f32) {
+      CK(x->run32.enqueue(n, x->stream, &x->timers, x->last_launches));
+      x->e32.advance_host(n);
+      x->k += n;
+    } else {
+      for (int t = 0; t < n; t++) {
         x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers);
+        x->k++;
       }
-      x->k++;
     }
     CK(cudaEventRecord(x->ev[1], x->stream));
     CK(cudaGetLastError());
@@ -628,6 +735,7 @@ void sw2g_destroy(sw2g_ctx* x) {
   if (x->d_cfl) cudaFree(x->d_cfl);
   if (x->d_bad) cudaFree(x->d_bad);
   x->timers.release();
+  x->run32.release();
   for (int e = 0; e < 2; e++)
     if (x->ev[e]) cudaEventDestroy(x->ev[e]);
   if (x->stream) cudaStreamDestroy(x->stream);
@@ -655,6 +763,175 @@ sw2g_status sw2g_timer_read(const sw2g_ctx* x, int idx, const char** name, long 
   if (launches) *launches = e.launches;
   if (total_ms) *total_ms = e.ms;
   return SW2G_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batches
+struct sw2g_batch {
+  std::vector<sw2g_ctx*> mem;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  BatchExec run;
+  std::vector<int2> nb;
+  std::vector<MemberDesc> desc;
+  int sched = SCHED_ROWS;
+  double last_ms = 0;
+  long long last_launches = 0;
+  int err_member = -1, err_step = -1;
+};
+
+namespace {
+
+sw2g_status batch_set_schedule(sw2g_batch* b, int sched) {
+  const std::vector<int4> t = tile_table(b->nb, sched);
+  CK(cudaMemcpy(b->run.d_tiles, t.data(), t.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  b->sched = sched;
+  return SW2G_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+sw2g_status sw2g_batch_create(sw2g_ctx* const* members, int n, sw2g_batch** out) {
+  if (!out || !members || n < 1) return SW2G_ERR_BAD_ARG;
+  *out = nullptr;
+  for (int m = 0; m < n; m++) {
+    const sw2g_ctx* x = members[m];
+    if (!x || x->precision != SW2G_FP32 || x->device != members[0]->device) return SW2G_ERR_BAD_ARG;
+    if (x->c32.sch != members[0]->c32.sch) return SW2G_ERR_BAD_ARG;
+    if (!x->uploaded) return SW2G_ERR_STATE;
+    for (int q = 0; q < m; q++)
+      if (members[q] == x) return SW2G_ERR_BAD_ARG;
+  }
+  sw2g_batch* b = new (std::nothrow) sw2g_batch();
+  if (!b) return SW2G_ERR_NOMEM;
+  b->mem.assign(members, members + n);
+  b->device = members[0]->device;
+  auto fail = [&](sw2g_status e) {
+    sw2g_batch_destroy(b);
+    return e;
+  };
+  sw2g_status st;
+  if ((st = cuda_fail(cudaSetDevice(b->device), "cudaSetDevice")) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream")) != SW2G_OK)
+    return fail(st);
+  for (int e = 0; e < 2; e++)
+    if ((st = cuda_fail(cudaEventCreate(&b->ev[e]), "event")) != SW2G_OK) return fail(st);
+  int ntiles = 0;
+  for (sw2g_ctx* x : b->mem) {
+    int nbx = 0, nby = 0;
+    fp32_tiles(x->c32.nx, x->c32.ny, &nbx, &nby);
+    b->nb.push_back(make_int2(nbx, nby));
+    ntiles += nbx * nby;
+  }
+  if ((st = cuda_fail(b->run.alloc(n, ntiles), "batch")) != SW2G_OK) return fail(st);
+  b->run.sch = members[0]->c32.sch;
+  b->desc.resize(n);
+  if ((st = batch_set_schedule(b, SCHED_ROWS)) != SW2G_OK) return fail(st);
+  *out = b;
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_batch_step(sw2g_batch* b, int nsteps) {
+  if (!b || nsteps < 0) return SW2G_ERR_BAD_ARG;
+  CK(cudaSetDevice(b->device));
+  const int M = (int)b->mem.size();
+  b->last_ms = 0;
+  b->last_launches = 0;
+  b->err_member = -1;
+  b->err_step = -1;
+  std::vector<unsigned> cfl((size_t)M * 2 * kChunk);
+  std::vector<int> bad((size_t)M * kChunk);
+  int done = 0;
+  while (done < nsteps) {
+    const int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
+    for (int m = 0; m < M; m++) {
+      sw2g_ctx* x = b->mem[m];
+      b->desc[m] = fp32_desc(x->c32, x->e32, x->k);
+      CK(cudaMemsetAsync(x->e32.cfl, 0, sizeof(unsigned) * 2 * n, b->stream));
+      CK(cudaMemsetAsync(x->e32.bad, 0, sizeof(int) * n, b->stream));
+    }
+    CK(cudaMemcpyAsync(b->run.d_desc, b->desc.data(), sizeof(MemberDesc) * M, cudaMemcpyHostToDevice, b->stream));
+    CK(cudaMemsetAsync(b->run.d_counter, 0, sizeof(long long), b->stream));
+    CK(cudaEventRecord(b->ev[0], b->stream));
+    CK(b->run.enqueue(n, b->stream, nullptr, b->last_launches));
+    CK(cudaEventRecord(b->ev[1], b->stream));
+    for (int m = 0; m < M; m++) {
+      sw2g_ctx* x = b->mem[m];
+      CK(cudaMemcpyAsync(&cfl[(size_t)m * 2 * kChunk], x->e32.cfl, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost,
+                         b->stream));
+      CK(cudaMemcpyAsync(&bad[(size_t)m * kChunk], x->e32.bad, sizeof(int) * n, cudaMemcpyDeviceToHost, b->stream));
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+    b->last_ms += ms;
+    for (sw2g_ctx* x : b->mem) {
+      x->e32.advance_host(n);
+      x->k += n;
+    }
+    // first failing step over all members, in step order (compute_Dt then the range check)
+    for (int t = 0; t < n && b->err_member < 0; t++) {
+      for (int m = 0; m < M; m++) {
+        sw2g_ctx* x = b->mem[m];
+        float a, c;
+        std::memcpy(&a, &cfl[(size_t)m * 2 * kChunk + 2 * t], sizeof(float));
+        std::memcpy(&c, &cfl[(size_t)m * 2 * kChunk + 2 * t + 1], sizeof(float));
+        double mx = a, my = c;
+        if (mx + my == 0) { mx = x->rest_mx; my = x->rest_my; }
+        const bool cfl_bad = x->c.Dt > (x->c.courant / (mx + my));
+        if (cfl_bad || bad[(size_t)m * kChunk + t]) {
+          b->err_member = m;
+          b->err_step = done + t;
+          x->err_step = (int)(x->steps + t);
+          for (sw2g_ctx* y : b->mem) y->steps += (y == x) ? t : n;
+          return cfl_bad ? SW2G_ERR_CFL : SW2G_ERR_NONFINITE;
+        }
+      }
+    }
+    for (sw2g_ctx* x : b->mem) x->steps += n;
+    done += n;
+  }
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_batch_tune(sw2g_batch* b, int steps_per_candidate, double* ms_per_step) {
+  if (!b || steps_per_candidate < 1) return SW2G_ERR_BAD_ARG;
+  double best = 0;
+  int best_s = SCHED_ROWS;
+  for (int s = 0; s < SCHED_COUNT; s++) {
+    sw2g_status st = batch_set_schedule(b, s);
+    if (st != SW2G_OK) return st;
+    st = sw2g_batch_step(b, steps_per_candidate);
+    if (st != SW2G_OK) return st;
+    const double ms = b->last_ms / steps_per_candidate;
+    if (ms_per_step) ms_per_step[s] = ms;
+    if (s == 0 || ms < best) {
+      best = ms;
+      best_s = s;
+    }
+  }
+  return batch_set_schedule(b, best_s);
+}
+
+int sw2g_batch_schedule(const sw2g_batch* b) { return b ? b->sched : -1; }
+int sw2g_batch_error_member(const sw2g_batch* b) { return b ? b->err_member : -1; }
+int sw2g_batch_error_step(const sw2g_batch* b) { return b ? b->err_step : -1; }
+double sw2g_batch_last_step_ms(const sw2g_batch* b) { return b ? b->last_ms : 0.0; }
+long long sw2g_batch_last_launches(const sw2g_batch* b) { return b ? b->last_launches : 0; }
+
+void sw2g_batch_destroy(sw2g_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  b->run.release();
+  for (int e = 0; e < 2; e++)
+    if (b->ev[e]) cudaEventDestroy(b->ev[e]);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
 }
 
 }  // extern "C"

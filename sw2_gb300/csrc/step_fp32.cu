@@ -184,7 +184,7 @@ __device__ __forceinline__ void put(T* f, int W, int nx, int ny, int i, int j, T
 // FP32 fields of this form use a row pitch P (a multiple of 4) and enough
 // padding rows and columns that the ring-2 window of any tile is in bounds.
 // The window [i0-2, i0+TW+1] x [j0-2, j0+TH+1] starts on a 16-byte boundary
-// (padded column i0-1 = TW*blockIdx.x), so it is read with 16-byte loads.
+// (padded column i0-1 = TW*bx), so it is read with 16-byte loads.
 typedef float Tile[TH + 4][TW + 4];
 
 __device__ __forceinline__ int IX32(int P, int i, int j) { return (i + 1) + (j + 1) * P; }
@@ -254,12 +254,12 @@ __device__ __forceinline__ void lap_out(const Rows& rc, int j, int a, int b, con
 }
 
 // ------------------------------------------------------------------ kernels
-__global__ void __launch_bounds__(NT) k_lap1(KP p, const float* __restrict__ u, const float* __restrict__ v,
-                                             float* Lu, float* Lv) {
+__device__ __forceinline__ void d_lap1(const KP& p, int bx, int by, const float* __restrict__ u,
+                                       const float* __restrict__ v, float* Lu, float* Lv) {
   __shared__ __align__(16) Tile su, sv;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
   __shared__ RowCache sq;
-  const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
+  const int i0 = bx * TW + 1, j0 = by * TH + 1;
   fill_rows(p, j0, sq);
   const Rows rc{sq, j0};
   load_tile(u, p.P, i0, j0, su);
@@ -289,13 +289,13 @@ struct Main1Io {
 };
 
 template <int SCH>
-__global__ void __launch_bounds__(NT) k_main1(KP p, Main1Io o) {
+__device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1Io& o) {
   __shared__ __align__(16) Tile se, su, sv, sl, sm;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
   __shared__ float red[2][NT / 32];
   __shared__ RowCache sq;
   const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
-  const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
+  const int i0 = bx * TW + 1, j0 = by * TH + 1;
   // this thread's own cell: issue its global loads before the tile traffic
   const int a = threadIdx.x % TW + 2, b = threadIdx.x / TW + 2;  // ring-2 local coordinates
   const int i = i0 + a - 2, j = j0 + b - 2;
@@ -430,12 +430,12 @@ struct Main2Io {
 };
 
 // Pressure (calc.c:500-540), AB, Coriolis u then v (calc.c:542-598).
-__global__ void __launch_bounds__(NT) k_main2(KP p, Main2Io io) {
+__device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2Io& io) {
   __shared__ __align__(16) Tile se, su, sv;  // ring-2 windows, ring 1 used
   __shared__ float un[TH + 1][TW + 1];       // new u at (i0-1+a, j0+b)
   __shared__ RowCache sq;
   const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
-  const int i0 = blockIdx.x * TW + 1, j0 = blockIdx.y * TH + 1;
+  const int i0 = bx * TW + 1, j0 = by * TH + 1;
   // own cell of the v update: issue its global loads first
   const int ac = threadIdx.x % TW, bc = threadIdx.x / TW;
   const int ic = i0 + ac, jc = j0 + bc;
@@ -528,6 +528,71 @@ __global__ void __launch_bounds__(NT) k_main2(KP p, Main2Io io) {
   if (!in_range(vnew)) atomicOr(io.bad, 1);
 }
 
+// ------------------------------------------------------------ batched launch
+// One launch per phase covers every tile of every member of a batch (a single
+// context is a batch of one). Block b works on tiles[b] = (member, bx, by).
+// Buffer rotation is derived from a device step counter n, which a one-thread
+// kernel advances after each step: state buffers alternate with n, the three
+// Adams-Bashforth slots form a ring written at n mod 3, the AB index is
+// min(k0 + n, 2) and step checks go to slot n. A captured graph of one step
+// can therefore be replayed for any number of steps.
+struct View {
+  KP p;
+  int cur, w, h1, h2, slot;
+};
+
+__device__ __forceinline__ View view_of(const MemberDesc& d, long long n) {
+  View v;
+  KP& p = v.p;
+  p.nx = d.nx; p.ny = d.ny; p.W = d.nx + 4; p.H = d.ny + 4; p.P = d.P;
+  p.q = d.q;
+  p.sig2dt = d.sig2dt; p.sigdt = d.sigdt; p.nu2dt = d.nu2dt; p.nu4dt = d.nu4dt;
+  const long long kk = (long long)d.k0 + n;
+  p.k = kk > 2 ? 2 : (int)kk;
+  p.extra = d.extra;
+  p.wx = d.wx; p.wy = d.wy; p.hb = d.hb;
+  v.cur = d.cur0 ^ (int)(n & 1);
+  const int r = (int)(n % 3);
+  v.w = r;
+  v.h1 = (r + 2) % 3;
+  v.h2 = (r + 1) % 3;
+  v.slot = (int)(n % kCheckSlots);
+  return v;
+}
+
+__global__ void __launch_bounds__(NT) kb_lap1(const MemberDesc* __restrict__ mem, const int4* __restrict__ tiles,
+                                              const long long* __restrict__ counter) {
+  const int4 t = tiles[blockIdx.x];
+  const MemberDesc& d = mem[t.x];
+  const View v = view_of(d, *counter);
+  d_lap1(v.p, t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
+}
+
+template <int SCH>
+__global__ void __launch_bounds__(NT) kb_main1(const MemberDesc* __restrict__ mem, const int4* __restrict__ tiles,
+                                               const long long* __restrict__ counter) {
+  const int4 t = tiles[blockIdx.x];
+  const MemberDesc& d = mem[t.x];
+  const View v = view_of(d, *counter);
+  const Main1Io o{d.eta[v.cur], d.es[v.cur], d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv, d.heta[v.h1], d.heta[v.h2],
+                  d.eta[1 - v.cur], d.es[1 - v.cur], d.heta[v.w], d.dup, d.dvp, d.cfl + 2 * v.slot,
+                  d.bad + v.slot};
+  d_main1<SCH>(v.p, t.y, t.z, o);
+}
+
+__global__ void __launch_bounds__(NT) kb_main2(const MemberDesc* __restrict__ mem, const int4* __restrict__ tiles,
+                                               const long long* __restrict__ counter) {
+  const int4 t = tiles[blockIdx.x];
+  const MemberDesc& d = mem[t.x];
+  const View v = view_of(d, *counter);
+  const Main2Io io{d.es[1 - v.cur], d.u[v.cur], d.v[v.cur], d.us[v.cur], d.vs[v.cur], d.u[1 - v.cur],
+                   d.v[1 - v.cur], d.us[1 - v.cur], d.vs[1 - v.cur], d.dup, d.dvp, d.hu[v.h1], d.hu[v.h2],
+                   d.hv[v.h1], d.hv[v.h2], d.hu[v.w], d.hv[v.w], d.bad + v.slot};
+  d_main2(v.p, t.y, t.z, io);
+}
+
+__global__ void kb_advance(long long* counter) { *counter += 1; }
+
 // FP32 shadow of an FP64 field over all padded cells (pitch W -> pitch P).
 __global__ void k_shadow(float* dst, const double* src, int nx, int ny, int W, int P) {
   const int n = W * (ny + 4);
@@ -535,11 +600,6 @@ __global__ void k_shadow(float* dst, const double* src, int nx, int ny, int W, i
     const int r = t / W, c = t - r * W;
     dst[(size_t)r * P + c] = d2f(src[t]);
   }
-}
-
-template <int SCH>
-void launch_main1(dim3 g, cudaStream_t st, const KP& p, const Main1Io& o) {
-  k_main1<SCH><<<g, NT, 0, st>>>(p, o);
 }
 
 }  // namespace f32
@@ -557,16 +617,47 @@ void fp32_geometry(int nx, int ny, int* P, int* R) {
   *R = TH * ((ny + TH - 1) / TH) + 4;
 }
 
-// ------------------------------------------------------------------ host
-void Fp32Engine::step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers* tm, int& nl) {
-  KP p{};
-  p.nx = c.nx; p.ny = c.ny; p.W = c.nx + 4; p.H = c.ny + 4; p.P = c.P;
-  p.q = c.q;
-  p.sig2dt = c.sig2dt; p.sigdt = c.sigdt; p.nu2dt = c.nu2dt; p.nu4dt = c.nu4dt;
-  p.k = k;
-  p.extra = c.extra;
-  p.wx = c.wx; p.wy = c.wy; p.hb = c.hb;
-  const dim3 g((c.nx + TW - 1) / TW, (c.ny + TH - 1) / TH);
+void fp32_tiles(int nx, int ny, int* nbx, int* nby) {
+  *nbx = (nx + TW - 1) / TW;
+  *nby = (ny + TH - 1) / TH;
+}
+
+MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k0) {
+  MemberDesc d{};
+  d.nx = c.nx; d.ny = c.ny; d.P = c.P;
+  d.extra = c.extra;
+  d.sig2dt = c.sig2dt; d.sigdt = c.sigdt; d.nu2dt = c.nu2dt; d.nu4dt = c.nu4dt;
+  d.q = c.q;
+  d.wx = c.wx; d.wy = c.wy; d.hb = c.hb;
+  for (int q = 0; q < 2; q++) {
+    d.eta[q] = e.eta[q]; d.u[q] = e.u[q]; d.v[q] = e.v[q];
+    d.es[q] = e.es[q]; d.us[q] = e.us[q]; d.vs[q] = e.vs[q];
+  }
+  // ring: slot 0 is written at n = 0, slot 2 holds step n-1, slot 1 step n-2
+  d.heta[0] = e.heta[0]; d.heta[2] = e.heta[1]; d.heta[1] = e.heta[2];
+  d.hu[0] = e.hu[0]; d.hu[2] = e.hu[1]; d.hu[1] = e.hu[2];
+  d.hv[0] = e.hv[0]; d.hv[2] = e.hv[1]; d.hv[1] = e.hv[2];
+  d.Lu = e.Lu; d.Lv = e.Lv; d.dup = e.dup; d.dvp = e.dvp;
+  d.cfl = e.cfl; d.bad = e.bad;
+  d.cur0 = e.cur;
+  d.k0 = k0 > 2 ? 2 : k0;
+  return d;
+}
+
+void Fp32Engine::advance_host(long long nsteps) {
+  if (nsteps & 1) cur = 1 - cur;
+  for (long long s = 0; s < nsteps % 3; s++) {
+    float* t;
+    t = heta[2]; heta[2] = heta[1]; heta[1] = heta[0]; heta[0] = t;
+    t = hu[2]; hu[2] = hu[1]; hu[1] = hu[0]; hu[0] = t;
+    t = hv[2]; hv[2] = hv[1]; hv[1] = hv[0]; hv[0] = t;
+  }
+}
+
+// Enqueues the four launches of one step of a batch; returns kernel launches.
+int fp32_batch_step(int sch, const MemberDesc* mem, const int4* tiles, int ntiles, long long* counter,
+                    cudaStream_t st, Timers* tm) {
+  int nl = 0;
 #define LAUNCH(tag, ...)                        \
   do {                                          \
     if (tm && tm->on) tm->begin(tag, st);       \
@@ -574,32 +665,26 @@ void Fp32Engine::step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers
     if (tm && tm->on) tm->end(st);              \
     nl++;                                       \
   } while (0)
-  LAUNCH("f32_lap1", k_lap1<<<g, NT, 0, st>>>(p, us[cur], vs[cur], Lu, Lv));
-  Main1Io o1{eta[cur], es[cur], us[cur], vs[cur], Lu, Lv, heta[1], heta[2], eta[1 - cur], es[1 - cur],
-             heta[0], dup, dvp, cfl + 2 * slot, bad + slot};
-  switch (c.sch) {
-    case 0: LAUNCH("f32_main1", launch_main1<0>(g, st, p, o1)); break;
-    case 1: LAUNCH("f32_main1", launch_main1<1>(g, st, p, o1)); break;
-    case 2: LAUNCH("f32_main1", launch_main1<2>(g, st, p, o1)); break;
-    case 3: LAUNCH("f32_main1", launch_main1<3>(g, st, p, o1)); break;
-    case 4: LAUNCH("f32_main1", launch_main1<4>(g, st, p, o1)); break;
-    case 5: LAUNCH("f32_main1", launch_main1<5>(g, st, p, o1)); break;
-    case 6: LAUNCH("f32_main1", launch_main1<6>(g, st, p, o1)); break;
-    case 7: LAUNCH("f32_main1", launch_main1<7>(g, st, p, o1)); break;
-    case 8: LAUNCH("f32_main1", launch_main1<8>(g, st, p, o1)); break;
-    case 9: LAUNCH("f32_main1", launch_main1<9>(g, st, p, o1)); break;
-    default: LAUNCH("f32_main1", launch_main1<kVanLeerSafe>(g, st, p, o1)); break;
+  const dim3 g(ntiles);
+  LAUNCH("f32_lap1", kb_lap1<<<g, NT, 0, st>>>(mem, tiles, counter));
+  switch (sch) {
+    case 0: LAUNCH("f32_main1", kb_main1<0><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 1: LAUNCH("f32_main1", kb_main1<1><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 2: LAUNCH("f32_main1", kb_main1<2><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 3: LAUNCH("f32_main1", kb_main1<3><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 4: LAUNCH("f32_main1", kb_main1<4><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 5: LAUNCH("f32_main1", kb_main1<5><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 6: LAUNCH("f32_main1", kb_main1<6><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 7: LAUNCH("f32_main1", kb_main1<7><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 8: LAUNCH("f32_main1", kb_main1<8><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 9: LAUNCH("f32_main1", kb_main1<9><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    default: LAUNCH("f32_main1", kb_main1<kVanLeerSafe><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
   }
-  Main2Io io{es[1 - cur], u[cur], v[cur], us[cur], vs[cur], u[1 - cur], v[1 - cur], us[1 - cur], vs[1 - cur],
-             dup, dvp, hu[1], hu[2], hv[1], hv[2], hu[0], hv[0], bad + slot};
-  LAUNCH("f32_main2", k_main2<<<g, NT, 0, st>>>(p, io));
+  LAUNCH("f32_main2", kb_main2<<<g, NT, 0, st>>>(mem, tiles, counter));
+  kb_advance<<<1, 1, 0, st>>>(counter);
+  nl++;
 #undef LAUNCH
-  // the slot just written becomes n-1, n-1 becomes n-2, n-2 is reused
-  float* t;
-  t = heta[2]; heta[2] = heta[1]; heta[1] = heta[0]; heta[0] = t;
-  t = hu[2]; hu[2] = hu[1]; hu[1] = hu[0]; hu[0] = t;
-  t = hv[2]; hv[2] = hv[1]; hv[1] = hv[0]; hv[0] = t;
-  cur = 1 - cur;
+  return nl;
 }
 
 }  // namespace sw2g

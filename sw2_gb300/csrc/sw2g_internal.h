@@ -138,8 +138,34 @@ struct Fp32Engine {
   float* dup = nullptr; float* dvp = nullptr;
   unsigned* cfl = nullptr;  // 2 per step (float bits)
   int* bad = nullptr;       // 1 per step
-  void step(const Fp32Ctx& c, int k, int slot, cudaStream_t st, Timers* tm, int& nl);
+  // host view after nsteps more steps: state buffer and AB history rotation
+  void advance_host(long long nsteps);
 };
+
+// Steps whose checks are kept on the device before the host reads them back.
+constexpr int kCheckSlots = 1024;
+
+// Device descriptor of one member of an FP32-form batch (a context is a batch
+// of one). Pointers are fixed; the per-step rotation is derived in-kernel from
+// the step counter (state buffers alternate, AB slots form a ring).
+struct MemberDesc {
+  int nx, ny, P;
+  int extra;
+  float sig2dt, sigdt, nu2dt, nu4dt;
+  const float* q;
+  const float* wx; const float* wy; const float* hb;
+  double* eta[2]; double* u[2]; double* v[2];
+  float* es[2]; float* us[2]; float* vs[2];
+  float* heta[3]; float* hu[3]; float* hv[3];  // ring: slot n%3 written at step n
+  float* Lu; float* Lv; float* dup; float* dvp;
+  unsigned* cfl; int* bad;
+  int cur0, k0;
+};
+
+MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k0);
+void fp32_tiles(int nx, int ny, int* nbx, int* nby);
+int fp32_batch_step(int sch, const MemberDesc* mem, const int4* tiles, int ntiles, long long* counter,
+                    cudaStream_t st, Timers* tm);
 
 // FP32 shadow (pitch P) of an FP64 padded field (pitch nx+4), all padded cells.
 void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStream_t st);

@@ -202,3 +202,65 @@ class Solver:
 
     def stream(self) -> int:
         return load().sw2g_stream(self.h)
+
+
+class Batch:
+    """Several SW2G_FP32 solvers stepped together (sw2g_batch_*): one launch
+    per phase over all members' tiles, time loop replayed as a CUDA graph."""
+
+    SCHEDULES = ("rows", "columns", "interleaved", "bands")
+
+    def __init__(self, solvers):
+        L = load()
+        vp = ctypes.c_void_p
+        L.sw2g_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, ctypes.POINTER(vp)]
+        L.sw2g_batch_step.argtypes = [vp, ctypes.c_int]
+        L.sw2g_batch_error_member.argtypes = [vp]
+        L.sw2g_batch_error_step.argtypes = [vp]
+        L.sw2g_batch_last_step_ms.restype = ctypes.c_double
+        L.sw2g_batch_last_step_ms.argtypes = [vp]
+        L.sw2g_batch_last_launches.restype = ctypes.c_longlong
+        L.sw2g_batch_last_launches.argtypes = [vp]
+        L.sw2g_batch_tune.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        L.sw2g_batch_schedule.argtypes = [vp]
+        L.sw2g_batch_destroy.argtypes = [vp]
+        self.solvers = list(solvers)
+        arr = (vp * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = vp()
+        rc = L.sw2g_batch_create(arr, len(self.solvers), ctypes.byref(h))
+        if rc != OK:
+            raise SW2GError(rc, "sw2g_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().sw2g_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def step(self, n: int) -> int:
+        rc = load().sw2g_batch_step(self.h, int(n))
+        if rc in (OK, ERR_CFL, ERR_NONFINITE):
+            return rc
+        raise SW2GError(rc, "sw2g_batch_step")
+
+    def error(self):
+        return load().sw2g_batch_error_member(self.h), load().sw2g_batch_error_step(self.h)
+
+    def last_step_ms(self) -> float:
+        return load().sw2g_batch_last_step_ms(self.h)
+
+    def last_launches(self) -> int:
+        return load().sw2g_batch_last_launches(self.h)
+
+    def tune(self, steps_per_candidate: int):
+        ms = (ctypes.c_double * 4)()
+        rc = load().sw2g_batch_tune(self.h, int(steps_per_candidate), ms)
+        if rc != OK:
+            raise SW2GError(rc, "sw2g_batch_tune")
+        return {self.SCHEDULES[i]: ms[i] for i in range(4)}
+
+    def schedule(self) -> str:
+        return self.SCHEDULES[load().sw2g_batch_schedule(self.h)]

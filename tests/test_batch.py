@@ -1,0 +1,105 @@
+"""Batched ensembles of FP32-form members (sw2g_batch_*).
+
+A batch runs the same kernels over all members' tiles in one launch per phase
+and replays a captured one-step CUDA graph, so each member must end bit for
+bit where it ends when stepped alone; the sweep-schedule tuner only reorders
+independent blocks, so tuning must not change any result either.
+"""
+import numpy as np
+import pytest
+
+from sw2_gb300 import cases, lib
+
+pytestmark = pytest.mark.gpu
+
+
+def members(seed=3):
+    specs = [(64, 32, 1), (97, 40, 2), (128, 64, 3)]
+    out = []
+    for nx, ny, k in specs:
+        c = cases.make_case(nx=nx, ny=ny, sch=3, seed=seed * 10 + k, bumps=1, amp=(0.01, 0.08),
+                            sigma_km=(1000.0, 3000.0))
+        out.append(c)
+    return out
+
+
+def solo(case, n):
+    s = lib.Solver(case.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+    s.upload(*case.fields())
+    assert s.step(n) == lib.OK
+    return s.download()
+
+
+def test_batch_matches_members_stepped_alone():
+    cs = members()
+    ss = []
+    for c in cs:
+        s = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+        s.upload(*c.fields())
+        ss.append(s)
+    b = lib.Batch(ss)
+    assert b.step(7) == lib.OK
+    assert b.step(9) == lib.OK
+    assert b.last_launches() == 4 * 9
+    for c, s in zip(cs, ss):
+        got, ref = s.download(), solo(c, 16)
+        for k in ("eta", "u", "v"):
+            assert np.array_equal(got[k], ref[k]), k
+        assert s.steps_done() == 16
+
+
+def test_tuning_changes_no_result():
+    cs = members(seed=5)
+    ss = []
+    for c in cs:
+        s = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+        s.upload(*c.fields())
+        ss.append(s)
+    b = lib.Batch(ss)
+    times = b.tune(3)
+    assert set(times) == set(lib.Batch.SCHEDULES) and all(t > 0 for t in times.values())
+    assert b.schedule() in lib.Batch.SCHEDULES
+    assert b.step(4) == lib.OK
+    for c, s in zip(cs, ss):
+        got, ref = s.download(), solo(c, 4 * 3 + 4)
+        for k in ("eta", "u", "v"):
+            assert np.array_equal(got[k], ref[k]), k
+
+
+def test_batch_reports_the_failing_member():
+    cs = members(seed=7)
+    cs[1].params.Dt *= 100  # violates the CFL bound at the first step
+    ss = []
+    for c in cs:
+        s = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+        s.upload(*c.fields())
+        ss.append(s)
+    b = lib.Batch(ss)
+    assert b.step(5) == lib.ERR_CFL
+    assert b.error() == (1, 0)
+    assert ss[1].error_step() == 0
+
+
+def test_graph_replay_equals_direct_launches():
+    c = members(seed=9)[2]
+    a = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+    a.upload(*c.fields())
+    a.timers(True)  # per-kernel timers force direct launches
+    assert a.step(11) == lib.OK
+    assert set(a.timer_table()) == {"f32_lap1", "f32_main1", "f32_main2"}
+    ref = solo(c, 11)
+    got = a.download()
+    for k in ("eta", "u", "v"):
+        assert np.array_equal(got[k], ref[k]), k
+
+
+def test_batch_rejects_mixed_members():
+    c = members()[0]
+    s64 = lib.Solver(c.params, precision=lib.FP64)
+    s64.upload(*c.fields())
+    s32 = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+    s32.upload(*c.fields())
+    with pytest.raises(lib.SW2GError):
+        lib.Batch([s32, s64])
+    with pytest.raises(lib.SW2GError):
+        lib.Batch([s32, s32])
