@@ -261,6 +261,59 @@ def accuracy(lib, case, nsteps, local):
     return out
 
 
+def ensemble(lib, nsteps, tune_steps, acc_steps, local, seed=7):
+    """The 64-member ensemble on uneven grids (16 x 512x256, 24 x 1024x512,
+    24 x 2048x1024; Van Leer, FP32 form) stepped as one batch: one launch per
+    phase over all members, one-step CUDA graph replays, sweep schedule chosen
+    by the tuner. Worst-member h error against the FP64 step is measured on one
+    member of each grid size."""
+    from sw2_gb300 import cases
+
+    specs = cases.ensemble_members(seed)
+    solvers, cs = [], []
+    for nx, ny, kw in specs:
+        c = cases.make_case(nx, ny, **kw)
+        s = lib.Solver(c.params, precision=lib.FP32, device=local, flags=lib.FLAG_VANLEER_SAFE)
+        s.upload(*c.fields())
+        solvers.append(s)
+        cs.append(c)
+    cells = sum(c.params.nx * c.params.ny for c in cs)
+    b = lib.Batch(solvers)
+    assert b.step(3) == lib.OK
+    tune = b.tune(tune_steps)
+    rc = b.step(nsteps)
+    if rc != lib.OK:
+        raise RuntimeError(f"ensemble step failed: {lib.status_string(rc)} {b.error()}")
+    ms = b.last_step_ms()
+    out = {"members": len(cs), "grids": "16 x 512x256, 24 x 1024x512, 24 x 2048x1024",
+           "cells_per_step": cells, "steps": nsteps, "value": cells * nsteps / (ms * 1e-3), "unit": UNIT,
+           "ms_per_step": ms / nsteps, "launches_per_step": b.last_launches() / nsteps,
+           "schedule": b.schedule(), "tune_ms_per_step": tune, "limiter": "Van Leer (r <= 0 -> 0)"}
+    b.close()
+    if acc_steps > 0:
+        worst = 0.0
+        picks = [0, 16, 40]
+        for m in picks:
+            c = cs[m]
+            d = c.params.depth
+            res = {}
+            for nm, prec in (("fp64", lib.FP64), ("fp32", lib.FP32)):
+                s = lib.Solver(c.params, precision=prec, device=local, flags=lib.FLAG_VANLEER_SAFE)
+                s.upload(*c.fields())
+                if s.step(acc_steps) != lib.OK:
+                    raise RuntimeError("ensemble accuracy run failed")
+                res[nm] = s.download()["eta"][2:-2, 2:-2]
+                s.close()
+            e = float(np.linalg.norm(res["fp32"] - res["fp64"]) / np.linalg.norm(res["fp64"] + d))
+            worst = max(worst, e)
+        out["worst_member_h_rel_l2"] = worst
+        out["accuracy_members"] = [f"{cs[m].params.nx}x{cs[m].params.ny}" for m in picks]
+        out["accuracy_steps"] = acc_steps
+    for s in solvers:
+        s.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -270,6 +323,7 @@ def main():
     ap.add_argument("--config", default="band2048")
     ap.add_argument("--fp32-config", default="saturn4096", help="workload of the FP32-form throughput line")
     ap.add_argument("--accuracy-steps", type=int, default=2000)
+    ap.add_argument("--ensemble-steps", type=int, default=1000, help="0 skips the 64-member ensemble leg")
     ap.add_argument("--cpu-steps", type=int, default=None, help="oracle steps for the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -342,6 +396,7 @@ def main():
     m32b["solver"].close()
     clk.__exit__(None, None, None)
     acc = accuracy(lib, case, args.accuracy_steps, local) if args.accuracy_steps > 0 else None
+    ens = ensemble(lib, args.ensemble_steps, 5, min(args.ensemble_steps, 1000), local) if args.ensemble_steps > 0 else None
 
     if rank != 0:
         pg.destroy_process_group()
@@ -390,6 +445,8 @@ def main():
         },
         "fp32_over_fp64": m32["value"] / m64["value"],
         "accuracy_fp32_vs_fp64": acc,
+        "ensemble_fp32_batched": ens,
+        "fp32_batched_over_fp64": (ens["value"] / m64["value"]) if ens else None,
     }
     print(json.dumps(line), flush=True)
     if pg:

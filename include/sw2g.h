@@ -146,6 +146,9 @@ void sw2g_destroy(sw2g_ctx *ctx);
  * state stays readable through its own context (sw2g_download, sw2g_diag). */
 typedef struct sw2g_batch sw2g_batch;
 
+/* Most members of one batch. */
+#define SW2G_BATCH_MAX 96
+
 sw2g_status sw2g_batch_create(sw2g_ctx *const *members, int n, sw2g_batch **out);
 /* Advances every member nsteps steps. On SW2G_ERR_CFL / SW2G_ERR_NONFINITE
  * the first failing (step, member) is reported by the two calls below and

@@ -15,45 +15,68 @@ namespace {
 
 constexpr int kChunk = kCheckSlots;  // steps per check read-back
 
-// Launch state of an FP32-form batch: member descriptors, the tile table (the
-// sweep schedule), the device step counter and the captured one-step graph.
+// Launch state of an FP32-form batch: the tile table (the sweep schedule),
+// the device step counter, the member descriptors a one-step CUDA graph was
+// captured with, and that graph.
 struct BatchExec {
-  MemberDesc* d_desc = nullptr;
   int4* d_tiles = nullptr;
-  int ntiles = 0;
-  long long* d_counter = nullptr;
+  int ntiles = 0, nbx = 0, nby = 0;  // nbx x nby: the grid of a single member
+  int* d_counter = nullptr;
+  int n_dev = 0;                     // device counter: steps since cap was taken
+  std::vector<MemberDesc> cap;
   cudaGraphExec_t exec = nullptr;
   int sch = 0;
 
-  cudaError_t alloc(int nmem, int ntile) {
+  cudaError_t alloc(int ntile) {
     ntiles = ntile;
-    cudaError_t e = cudaMalloc((void**)&d_desc, sizeof(MemberDesc) * nmem);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&d_tiles, sizeof(int4) * ntile);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&d_counter, sizeof(long long));
+    cudaError_t e = cudaMalloc((void**)&d_counter, sizeof(int));
+    if (e == cudaSuccess && ntile > 0) e = cudaMalloc((void**)&d_tiles, sizeof(int4) * ntile);
     return e;
   }
   void release() {
     if (exec) cudaGraphExecDestroy(exec);
-    if (d_desc) cudaFree(d_desc);
     if (d_tiles) cudaFree(d_tiles);
     if (d_counter) cudaFree(d_counter);
     exec = nullptr;
-    d_desc = nullptr;
     d_tiles = nullptr;
     d_counter = nullptr;
+    cap.clear();
   }
+  // Brings the launch state in line with the members' descriptors at their
+  // current step. The captured graph and the counter are kept when every
+  // member is where the counter says (only this launch state has stepped
+  // it); otherwise the new descriptors are taken and the counter restarts.
+  cudaError_t sync_to(const std::vector<MemberDesc>& now, cudaStream_t st) {
+    bool same = cap.size() == now.size() && n_dev < (1 << 30);
+    for (size_t m = 0; same && m < now.size(); m++) {
+      const MemberDesc a = fp32_desc_after(cap[m], n_dev);
+      same = std::memcmp(&a, &now[m], sizeof a) == 0;
+    }
+    if (same) return cudaSuccess;
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+    cap = now;
+    n_dev = 0;
+    return cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+  }
+  // Check slot of the next step, and the steps left before the slots wrap.
+  int slot() const { return n_dev & (kCheckSlots - 1); }
+  int room() const { return kCheckSlots - slot(); }
   // Enqueues n steps: replays of a captured one-step graph, or direct
   // launches while per-kernel timers are on.
   cudaError_t enqueue(int n, cudaStream_t st, Timers* tm, long long& launches) {
+    const int M = (int)cap.size();
     if (tm && tm->on) {
-      for (int s = 0; s < n; s++) launches += fp32_batch_step(sch, d_desc, d_tiles, ntiles, d_counter, st, tm);
+      for (int s = 0; s < n; s++)
+        launches += fp32_batch_step(sch, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, tm);
+      n_dev += n;
       return cudaGetLastError();
     }
     if (!exec) {
       cudaGraph_t g = nullptr;
       cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
-      fp32_batch_step(sch, d_desc, d_tiles, ntiles, d_counter, st, nullptr);
+      fp32_batch_step(sch, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, nullptr);
       e = cudaStreamEndCapture(st, &g);
       if (e != cudaSuccess) return e;
       e = cudaGraphInstantiate(&exec, g, 0);
@@ -64,6 +87,7 @@ struct BatchExec {
       cudaError_t e = cudaGraphLaunch(exec, st);
       if (e != cudaSuccess) return e;
     }
+    n_dev += n;
     launches += 4LL * n;
     return cudaSuccess;
   }
@@ -494,14 +518,9 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     c32.wx = x->d_aux32[0];
     c32.wy = x->d_aux32[1];
     c32.hb = x->d_aux32[2];
-    int nbx = 0, nby = 0;
-    fp32_tiles(c->nx, c->ny, &nbx, &nby);
-    const std::vector<int4> tiles = tile_table({make_int2(nbx, nby)}, SCHED_ROWS);
-    if ((st = cuda_fail(x->run32.alloc(1, (int)tiles.size()), "batch")) != SW2G_OK) return fail(st);
+    fp32_tiles(c->nx, c->ny, &x->run32.nbx, &x->run32.nby);
+    if ((st = cuda_fail(x->run32.alloc(0), "batch")) != SW2G_OK) return fail(st);
     x->run32.sch = c32.sch;
-    if ((st = cuda_fail(cudaMemcpy(x->run32.d_tiles, tiles.data(), tiles.size() * sizeof(int4),
-                                   cudaMemcpyHostToDevice), "tiles")) != SW2G_OK)
-      return fail(st);
   }
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
     return fail(st);
@@ -579,20 +598,19 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
   const bool f32 = (x->precision == SW2G_FP32);
   std::vector<unsigned> cfl32(f32 ? 2 * kChunk : 0);
   while (done < nsteps) {
-    const int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
+    int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
+    int slot0 = 0;  // check slot of the chunk's first step
     if (f32) {
-      CK(cudaMemsetAsync(x->e32.cfl, 0, sizeof(unsigned) * 2 * n, x->stream));
-      CK(cudaMemsetAsync(x->e32.bad, 0, sizeof(int) * n, x->stream));
+      CK(x->run32.sync_to({fp32_desc(x->c32, x->e32, x->k)}, x->stream));
+      if (n > x->run32.room()) n = x->run32.room();
+      slot0 = x->run32.slot();
+      CK(cudaMemsetAsync(x->e32.cfl + 2 * slot0, 0, sizeof(unsigned) * 2 * n, x->stream));
+      CK(cudaMemsetAsync(x->e32.bad + slot0, 0, sizeof(int) * n, x->stream));
     } else {
       CK(cudaMemsetAsync(x->d_cfl, 0, sizeof(unsigned long long) * 2 * n, x->stream));
       CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int) * n, x->stream));
     }
     StepChecks chk{x->d_cfl, x->d_bad};
-    if (f32) {
-      const MemberDesc d = fp32_desc(x->c32, x->e32, x->k);
-      CK(cudaMemcpyAsync(x->run32.d_desc, &d, sizeof(d), cudaMemcpyHostToDevice, x->stream));
-      CK(cudaMemsetAsync(x->run32.d_counter, 0, sizeof(long long), x->stream));
-    }
     CK(cudaEventRecord(x->ev[0], x->stream));
     if (f32) {
       CK(x->run32.enqueue(n, x->stream, &x->timers, x->last_launches));
@@ -607,8 +625,9 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
     CK(cudaEventRecord(x->ev[1], x->stream));
     CK(cudaGetLastError());
     if (f32) {
-      CK(cudaMemcpyAsync(cfl32.data(), x->e32.cfl, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost, x->stream));
-      CK(cudaMemcpyAsync(bad.data(), x->e32.bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaMemcpyAsync(cfl32.data(), x->e32.cfl + 2 * slot0, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost,
+                         x->stream));
+      CK(cudaMemcpyAsync(bad.data(), x->e32.bad + slot0, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
     } else {
       CK(cudaMemcpyAsync(cfl.data(), x->d_cfl, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost,
                          x->stream));
@@ -775,7 +794,6 @@ struct sw2g_batch {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   BatchExec run;
   std::vector<int2> nb;
-  std::vector<MemberDesc> desc;
   int sched = SCHED_ROWS;
   double last_ms = 0;
   long long last_launches = 0;
@@ -796,7 +814,7 @@ sw2g_status batch_set_schedule(sw2g_batch* b, int sched) {
 extern "C" {
 
 sw2g_status sw2g_batch_create(sw2g_ctx* const* members, int n, sw2g_batch** out) {
-  if (!out || !members || n < 1) return SW2G_ERR_BAD_ARG;
+  if (!out || !members || n < 1 || n > SW2G_BATCH_MAX) return SW2G_ERR_BAD_ARG;
   *out = nullptr;
   for (int m = 0; m < n; m++) {
     const sw2g_ctx* x = members[m];
@@ -827,9 +845,10 @@ sw2g_status sw2g_batch_create(sw2g_ctx* const* members, int n, sw2g_batch** out)
     b->nb.push_back(make_int2(nbx, nby));
     ntiles += nbx * nby;
   }
-  if ((st = cuda_fail(b->run.alloc(n, ntiles), "batch")) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(b->run.alloc(ntiles), "batch")) != SW2G_OK) return fail(st);
   b->run.sch = members[0]->c32.sch;
-  b->desc.resize(n);
+  b->run.nbx = b->nb[0].x;
+  b->run.nby = b->nb[0].y;
   if ((st = batch_set_schedule(b, SCHED_ROWS)) != SW2G_OK) return fail(st);
   *out = b;
   return SW2G_OK;
@@ -846,24 +865,27 @@ sw2g_status sw2g_batch_step(sw2g_batch* b, int nsteps) {
   std::vector<unsigned> cfl((size_t)M * 2 * kChunk);
   std::vector<int> bad((size_t)M * kChunk);
   int done = 0;
+  std::vector<MemberDesc> now(M);
   while (done < nsteps) {
-    const int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
+    int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
+    for (int m = 0; m < M; m++) now[m] = fp32_desc(b->mem[m]->c32, b->mem[m]->e32, b->mem[m]->k);
+    CK(b->run.sync_to(now, b->stream));
+    if (n > b->run.room()) n = b->run.room();
+    const int slot0 = b->run.slot();
     for (int m = 0; m < M; m++) {
       sw2g_ctx* x = b->mem[m];
-      b->desc[m] = fp32_desc(x->c32, x->e32, x->k);
-      CK(cudaMemsetAsync(x->e32.cfl, 0, sizeof(unsigned) * 2 * n, b->stream));
-      CK(cudaMemsetAsync(x->e32.bad, 0, sizeof(int) * n, b->stream));
+      CK(cudaMemsetAsync(x->e32.cfl + 2 * slot0, 0, sizeof(unsigned) * 2 * n, b->stream));
+      CK(cudaMemsetAsync(x->e32.bad + slot0, 0, sizeof(int) * n, b->stream));
     }
-    CK(cudaMemcpyAsync(b->run.d_desc, b->desc.data(), sizeof(MemberDesc) * M, cudaMemcpyHostToDevice, b->stream));
-    CK(cudaMemsetAsync(b->run.d_counter, 0, sizeof(long long), b->stream));
     CK(cudaEventRecord(b->ev[0], b->stream));
     CK(b->run.enqueue(n, b->stream, nullptr, b->last_launches));
     CK(cudaEventRecord(b->ev[1], b->stream));
     for (int m = 0; m < M; m++) {
       sw2g_ctx* x = b->mem[m];
-      CK(cudaMemcpyAsync(&cfl[(size_t)m * 2 * kChunk], x->e32.cfl, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost,
+      CK(cudaMemcpyAsync(&cfl[(size_t)m * 2 * kChunk], x->e32.cfl + 2 * slot0, sizeof(unsigned) * 2 * n,
+                         cudaMemcpyDeviceToHost, b->stream));
+      CK(cudaMemcpyAsync(&bad[(size_t)m * kChunk], x->e32.bad + slot0, sizeof(int) * n, cudaMemcpyDeviceToHost,
                          b->stream));
-      CK(cudaMemcpyAsync(&bad[(size_t)m * kChunk], x->e32.bad, sizeof(int) * n, cudaMemcpyDeviceToHost, b->stream));
     }
     CK(cudaStreamSynchronize(b->stream));
     float ms = 0;

@@ -530,68 +530,92 @@ __device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2
 
 // ------------------------------------------------------------ batched launch
 // One launch per phase covers every tile of every member of a batch (a single
-// context is a batch of one). Block b works on tiles[b] = (member, bx, by).
+// context is a batch of one). The member descriptors travel by value in the
+// launch parameters (the constant bank), so their fields are read like kernel
+// arguments: uniform over the block and loaded where they are used rather than
+// held in registers. With one member the grid is the member's nbx x nby tiles;
+// otherwise block b works on tiles[b] = (member, bx, by).
 // Buffer rotation is derived from a device step counter n, which a one-thread
-// kernel advances after each step: state buffers alternate with n, the three
-// Adams-Bashforth slots form a ring written at n mod 3, the AB index is
-// min(k0 + n, 2) and step checks go to slot n. A captured graph of one step
-// can therefore be replayed for any number of steps.
-struct View {
-  KP p;
-  int cur, w, h1, h2, slot;
+// kernel advances after each step (see MemberDesc), so a captured graph of one
+// step can be replayed for any number of steps.
+template <int N>
+struct DescSet {
+  MemberDesc m[N];
 };
 
-__device__ __forceinline__ View view_of(const MemberDesc& d, long long n) {
+struct View {
+  int cur, w, h1, h2, slot, k;
+};
+
+static_assert((kCheckSlots & (kCheckSlots - 1)) == 0, "check slots are indexed with a mask");
+static_assert(kMaxBatch == SW2G_BATCH_MAX, "batch limit of the header");
+
+__device__ __forceinline__ View view_of(const MemberDesc& d, int n) {
   View v;
-  KP& p = v.p;
-  p.nx = d.nx; p.ny = d.ny; p.W = d.nx + 4; p.H = d.ny + 4; p.P = d.P;
-  p.q = d.q;
-  p.sig2dt = d.sig2dt; p.sigdt = d.sigdt; p.nu2dt = d.nu2dt; p.nu4dt = d.nu4dt;
-  const long long kk = (long long)d.k0 + n;
-  p.k = kk > 2 ? 2 : (int)kk;
-  p.extra = d.extra;
-  p.wx = d.wx; p.wy = d.wy; p.hb = d.hb;
-  v.cur = d.cur0 ^ (int)(n & 1);
-  const int r = (int)(n % 3);
+  v.k = (n >= 2 - d.k0) ? 2 : d.k0 + n;
+  v.cur = d.cur0 ^ (n & 1);
+  const int r = (int)(((unsigned)d.w0 + (unsigned)n % 3u) % 3u);
   v.w = r;
-  v.h1 = (r + 2) % 3;
-  v.h2 = (r + 1) % 3;
-  v.slot = (int)(n % kCheckSlots);
+  v.h1 = (r == 0) ? 2 : r - 1;
+  v.h2 = (r == 2) ? 0 : r + 1;
+  v.slot = n & (kCheckSlots - 1);
   return v;
 }
 
-__global__ void __launch_bounds__(NT) kb_lap1(const MemberDesc* __restrict__ mem, const int4* __restrict__ tiles,
-                                              const long long* __restrict__ counter) {
-  const int4 t = tiles[blockIdx.x];
-  const MemberDesc& d = mem[t.x];
-  const View v = view_of(d, *counter);
-  d_lap1(v.p, t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
+__device__ __forceinline__ KP kp_of(const MemberDesc& d, int k) {
+  KP p;
+  p.nx = d.nx; p.ny = d.ny; p.W = d.nx + 4; p.H = d.ny + 4; p.P = d.P;
+  p.q = d.q;
+  p.sig2dt = d.sig2dt; p.sigdt = d.sigdt; p.nu2dt = d.nu2dt; p.nu4dt = d.nu4dt;
+  p.k = k;
+  p.extra = d.extra;
+  p.wx = d.wx; p.wy = d.wy; p.hb = d.hb;
+  return p;
 }
 
-template <int SCH>
-__global__ void __launch_bounds__(NT) kb_main1(const MemberDesc* __restrict__ mem, const int4* __restrict__ tiles,
-                                               const long long* __restrict__ counter) {
-  const int4 t = tiles[blockIdx.x];
-  const MemberDesc& d = mem[t.x];
-  const View v = view_of(d, *counter);
+template <int N>
+__device__ __forceinline__ int4 tile_of(const int4* __restrict__ tiles) {
+  if constexpr (N == 1) return make_int4(0, blockIdx.x, blockIdx.y, 0);
+  else return tiles[blockIdx.x];
+}
+
+template <int N>
+__global__ void __launch_bounds__(NT) kb_lap1(const __grid_constant__ DescSet<N> ds,
+                                              const int4* __restrict__ tiles, const int* __restrict__ counter) {
+  const int4 t = tile_of<N>(tiles);
+  const int n = *counter;
+  const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
+  const View v = view_of(d, n);
+  d_lap1(kp_of(d, v.k), t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
+}
+
+template <int SCH, int N>
+__global__ void __launch_bounds__(NT) kb_main1(const __grid_constant__ DescSet<N> ds,
+                                               const int4* __restrict__ tiles, const int* __restrict__ counter) {
+  const int4 t = tile_of<N>(tiles);
+  const int n = *counter;
+  const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
+  const View v = view_of(d, n);
   const Main1Io o{d.eta[v.cur], d.es[v.cur], d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv, d.heta[v.h1], d.heta[v.h2],
                   d.eta[1 - v.cur], d.es[1 - v.cur], d.heta[v.w], d.dup, d.dvp, d.cfl + 2 * v.slot,
                   d.bad + v.slot};
-  d_main1<SCH>(v.p, t.y, t.z, o);
+  d_main1<SCH>(kp_of(d, v.k), t.y, t.z, o);
 }
 
-__global__ void __launch_bounds__(NT) kb_main2(const MemberDesc* __restrict__ mem, const int4* __restrict__ tiles,
-                                               const long long* __restrict__ counter) {
-  const int4 t = tiles[blockIdx.x];
-  const MemberDesc& d = mem[t.x];
-  const View v = view_of(d, *counter);
+template <int N>
+__global__ void __launch_bounds__(NT) kb_main2(const __grid_constant__ DescSet<N> ds,
+                                               const int4* __restrict__ tiles, const int* __restrict__ counter) {
+  const int4 t = tile_of<N>(tiles);
+  const int n = *counter;
+  const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
+  const View v = view_of(d, n);
   const Main2Io io{d.es[1 - v.cur], d.u[v.cur], d.v[v.cur], d.us[v.cur], d.vs[v.cur], d.u[1 - v.cur],
                    d.v[1 - v.cur], d.us[1 - v.cur], d.vs[1 - v.cur], d.dup, d.dvp, d.hu[v.h1], d.hu[v.h2],
                    d.hv[v.h1], d.hv[v.h2], d.hu[v.w], d.hv[v.w], d.bad + v.slot};
-  d_main2(v.p, t.y, t.z, io);
+  d_main2(kp_of(d, v.k), t.y, t.z, io);
 }
 
-__global__ void kb_advance(long long* counter) { *counter += 1; }
+__global__ void kb_advance(int* counter) { *counter += 1; }
 
 // FP32 shadow of an FP64 field over all padded cells (pitch W -> pitch P).
 __global__ void k_shadow(float* dst, const double* src, int nx, int ny, int W, int P) {
@@ -622,8 +646,9 @@ void fp32_tiles(int nx, int ny, int* nbx, int* nby) {
   *nby = (ny + TH - 1) / TH;
 }
 
-MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k0) {
-  MemberDesc d{};
+MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
+  MemberDesc d;
+  std::memset(&d, 0, sizeof d);  // padding included, so descriptors compare with memcmp
   d.nx = c.nx; d.ny = c.ny; d.P = c.P;
   d.extra = c.extra;
   d.sig2dt = c.sig2dt; d.sigdt = c.sigdt; d.nu2dt = c.nu2dt; d.nu4dt = c.nu4dt;
@@ -633,30 +658,41 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k0) {
     d.eta[q] = e.eta[q]; d.u[q] = e.u[q]; d.v[q] = e.v[q];
     d.es[q] = e.es[q]; d.us[q] = e.us[q]; d.vs[q] = e.vs[q];
   }
-  // ring: slot 0 is written at n = 0, slot 2 holds step n-1, slot 1 step n-2
-  d.heta[0] = e.heta[0]; d.heta[2] = e.heta[1]; d.heta[1] = e.heta[2];
-  d.hu[0] = e.hu[0]; d.hu[2] = e.hu[1]; d.hu[1] = e.hu[2];
-  d.hv[0] = e.hv[0]; d.hv[2] = e.hv[1]; d.hv[1] = e.hv[2];
+  for (int q = 0; q < 3; q++) {
+    d.heta[q] = e.heta[q]; d.hu[q] = e.hu[q]; d.hv[q] = e.hv[q];
+  }
   d.Lu = e.Lu; d.Lv = e.Lv; d.dup = e.dup; d.dvp = e.dvp;
   d.cfl = e.cfl; d.bad = e.bad;
   d.cur0 = e.cur;
-  d.k0 = k0 > 2 ? 2 : k0;
+  d.w0 = e.w;
+  d.k0 = k > 2 ? 2 : k;
   return d;
+}
+
+MemberDesc fp32_desc_after(const MemberDesc& d, int n) {
+  MemberDesc a = d;
+  a.cur0 = d.cur0 ^ (n & 1);
+  a.w0 = (d.w0 + n % 3) % 3;
+  a.k0 = (n >= 2 - d.k0) ? 2 : d.k0 + n;
+  return a;
 }
 
 void Fp32Engine::advance_host(long long nsteps) {
   if (nsteps & 1) cur = 1 - cur;
-  for (long long s = 0; s < nsteps % 3; s++) {
-    float* t;
-    t = heta[2]; heta[2] = heta[1]; heta[1] = heta[0]; heta[0] = t;
-    t = hu[2]; hu[2] = hu[1]; hu[1] = hu[0]; hu[0] = t;
-    t = hv[2]; hv[2] = hv[1]; hv[1] = hv[0]; hv[0] = t;
-  }
+  w = (int)((w + nsteps % 3) % 3);
 }
 
-// Enqueues the four launches of one step of a batch; returns kernel launches.
-int fp32_batch_step(int sch, const MemberDesc* mem, const int4* tiles, int ntiles, long long* counter,
-                    cudaStream_t st, Timers* tm) {
+namespace {
+
+template <int N>
+int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
+                 int* counter, cudaStream_t st, Timers* tm) {
+  static_assert(sizeof(DescSet<N>) + 3 * sizeof(void*) <= 32760, "launch parameters are limited to 32 KB");
+  std::vector<DescSet<N>> hold(1);  // heap: up to ~28 KB
+  DescSet<N>& ds = hold[0];
+  std::memset(&ds, 0, sizeof ds);
+  for (int m = 0; m < nmem; m++) ds.m[m] = desc[m];
+  const dim3 g = (N == 1) ? dim3(nbx, nby) : dim3(ntiles);
   int nl = 0;
 #define LAUNCH(tag, ...)                        \
   do {                                          \
@@ -665,26 +701,36 @@ int fp32_batch_step(int sch, const MemberDesc* mem, const int4* tiles, int ntile
     if (tm && tm->on) tm->end(st);              \
     nl++;                                       \
   } while (0)
-  const dim3 g(ntiles);
-  LAUNCH("f32_lap1", kb_lap1<<<g, NT, 0, st>>>(mem, tiles, counter));
+#define MAIN1(S) LAUNCH("f32_main1", (kb_main1<S, N><<<g, NT, 0, st>>>(ds, tiles, counter)))
+  LAUNCH("f32_lap1", kb_lap1<N><<<g, NT, 0, st>>>(ds, tiles, counter));
   switch (sch) {
-    case 0: LAUNCH("f32_main1", kb_main1<0><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 1: LAUNCH("f32_main1", kb_main1<1><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 2: LAUNCH("f32_main1", kb_main1<2><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 3: LAUNCH("f32_main1", kb_main1<3><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 4: LAUNCH("f32_main1", kb_main1<4><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 5: LAUNCH("f32_main1", kb_main1<5><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 6: LAUNCH("f32_main1", kb_main1<6><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 7: LAUNCH("f32_main1", kb_main1<7><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 8: LAUNCH("f32_main1", kb_main1<8><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    case 9: LAUNCH("f32_main1", kb_main1<9><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
-    default: LAUNCH("f32_main1", kb_main1<kVanLeerSafe><<<g, NT, 0, st>>>(mem, tiles, counter)); break;
+    case 0: MAIN1(0); break;
+    case 1: MAIN1(1); break;
+    case 2: MAIN1(2); break;
+    case 3: MAIN1(3); break;
+    case 4: MAIN1(4); break;
+    case 5: MAIN1(5); break;
+    case 6: MAIN1(6); break;
+    case 7: MAIN1(7); break;
+    case 8: MAIN1(8); break;
+    case 9: MAIN1(9); break;
+    default: MAIN1(kVanLeerSafe); break;
   }
-  LAUNCH("f32_main2", kb_main2<<<g, NT, 0, st>>>(mem, tiles, counter));
+  LAUNCH("f32_main2", kb_main2<N><<<g, NT, 0, st>>>(ds, tiles, counter));
   kb_advance<<<1, 1, 0, st>>>(counter);
   nl++;
+#undef MAIN1
 #undef LAUNCH
   return nl;
+}
+
+}  // namespace
+
+int fp32_batch_step(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
+                    int* counter, cudaStream_t st, Timers* tm) {
+  if (nmem == 1) return batch_step_n<1>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+  if (nmem <= 16) return batch_step_n<16>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+  return batch_step_n<kMaxBatch>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
 }
 
 }  // namespace sw2g

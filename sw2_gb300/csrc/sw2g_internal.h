@@ -131,23 +131,28 @@ struct Fp32Engine {
   float* us[2] = {nullptr, nullptr};
   float* vs[2] = {nullptr, nullptr};
   int cur = 0;
-  float* heta[3] = {nullptr, nullptr, nullptr};  // [0] slot for step n, [1] n-1, [2] n-2
+  // Adams-Bashforth histories: a ring of three slots; the next step writes
+  // slot w, step n-1 is in slot (w+2)%3 and step n-2 in slot (w+1)%3.
+  float* heta[3] = {nullptr, nullptr, nullptr};
   float* hu[3] = {nullptr, nullptr, nullptr};
   float* hv[3] = {nullptr, nullptr, nullptr};
+  int w = 0;
   float* Lu = nullptr; float* Lv = nullptr;
   float* dup = nullptr; float* dvp = nullptr;
   unsigned* cfl = nullptr;  // 2 per step (float bits)
   int* bad = nullptr;       // 1 per step
-  // host view after nsteps more steps: state buffer and AB history rotation
+  // host view after nsteps more steps: state buffer and history ring position
   void advance_host(long long nsteps);
 };
 
 // Steps whose checks are kept on the device before the host reads them back.
 constexpr int kCheckSlots = 1024;
 
-// Device descriptor of one member of an FP32-form batch (a context is a batch
-// of one). Pointers are fixed; the per-step rotation is derived in-kernel from
-// the step counter (state buffers alternate, AB slots form a ring).
+// Descriptor of one member of an FP32-form batch (a context is a batch of
+// one), passed to the kernels in their launch parameters. Pointers are fixed;
+// the per-step rotation is derived in-kernel from a device step counter n:
+// state buffer cur0 ^ (n & 1), history slot (w0 + n) % 3 written, AB index
+// min(k0 + n, 2), checks in slot n % kCheckSlots.
 struct MemberDesc {
   int nx, ny, P;
   int extra;
@@ -156,16 +161,26 @@ struct MemberDesc {
   const float* wx; const float* wy; const float* hb;
   double* eta[2]; double* u[2]; double* v[2];
   float* es[2]; float* us[2]; float* vs[2];
-  float* heta[3]; float* hu[3]; float* hv[3];  // ring: slot n%3 written at step n
+  float* heta[3]; float* hu[3]; float* hv[3];
   float* Lu; float* Lv; float* dup; float* dvp;
   unsigned* cfl; int* bad;
-  int cur0, k0;
+  int cur0, w0, k0, pad;
 };
 
-MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k0);
+// Most members of one batch: their descriptors fill at most ~28 KB of the
+// 32 KB kernel parameter space.
+constexpr int kMaxBatch = 96;
+
+// Descriptor of a context's engine at its current step (counter n = 0).
+MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k);
+// The same descriptor seen n steps after it was taken (what the kernels derive).
+MemberDesc fp32_desc_after(const MemberDesc& d, int n);
 void fp32_tiles(int nx, int ny, int* nbx, int* nby);
-int fp32_batch_step(int sch, const MemberDesc* mem, const int4* tiles, int ntiles, long long* counter,
-                    cudaStream_t st, Timers* tm);
+// Enqueues one step of a batch of nmem members (host descriptors, passed by
+// value); tiles is the device tile table (unused for one member, whose grid
+// is nbx x nby). Returns the number of kernel launches.
+int fp32_batch_step(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
+                    int* counter, cudaStream_t st, Timers* tm);
 
 // FP32 shadow (pitch P) of an FP64 padded field (pitch nx+4), all padded cells.
 void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStream_t st);

@@ -21,6 +21,7 @@ OK, ERR_BAD_ARG, ERR_CFL, ERR_NONFINITE, ERR_TIMEOUT, ERR_CUDA, ERR_NOMEM, ERR_S
 FP64, FP32 = 0, 1
 FLAG_VANLEER_SAFE = 0x1
 UPLOAD_RAW, UPLOAD_FRAME, UPLOAD_CONTINUE = 0, 1, 2
+BATCH_MAX = 96
 
 SYMBOLS = [
     "sw2g_status_string", "sw2g_create", "sw2g_upload", "sw2g_step", "sw2g_error_step", "sw2g_download",

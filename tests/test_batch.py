@@ -103,3 +103,56 @@ def test_batch_rejects_mixed_members():
         lib.Batch([s32, s64])
     with pytest.raises(lib.SW2GError):
         lib.Batch([s32, s32])
+
+
+def fresh(c):
+    s = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+    s.upload(*c.fields())
+    return s
+
+
+def test_members_stepped_alone_between_batch_steps():
+    # a member stepped through its own context (or re-uploaded) between batch
+    # steps must be picked up where it is, not where the batch left it
+    cs = members(seed=11)
+    ss = [fresh(c) for c in cs]
+    b = lib.Batch(ss)
+    assert b.step(4) == lib.OK
+    assert ss[0].step(3) == lib.OK
+    ss[1].upload(*cs[1].fields())
+    assert b.step(5) == lib.OK
+    expect = [solo(cs[0], 12), solo(cs[1], 5), solo(cs[2], 9)]
+    for s, ref in zip(ss, expect):
+        got = s.download()
+        for k in ("eta", "u", "v"):
+            assert np.array_equal(got[k], ref[k]), k
+
+
+def test_large_batch():
+    # more than 16 members: the widest descriptor set of the launch
+    cs = [cases.make_case(nx=40 + 8 * (k % 3), ny=16 + 8 * (k % 2), sch=3, seed=100 + k, bumps=1,
+                          amp=(0.01, 0.08), sigma_km=(1000.0, 3000.0)) for k in range(20)]
+    ss = [fresh(c) for c in cs]
+    b = lib.Batch(ss)
+    assert b.step(6) == lib.OK
+    for k in (0, 7, 19):
+        got, ref = ss[k].download(), solo(cs[k], 6)
+        for f in ("eta", "u", "v"):
+            assert np.array_equal(got[f], ref[f]), (k, f)
+
+
+def test_check_slots_wrap():
+    # per-step checks live in a ring of 1024 slots on the device: runs that
+    # cross the end of the ring give the same state and still catch a failure
+    c = members(seed=13)[0]
+    a, one = fresh(c), fresh(c)
+    assert a.step(1000) == lib.OK
+    assert a.step(30) == lib.OK
+    assert one.step(1030) == lib.OK
+    ga, go = a.download(), one.download()
+    for k in ("eta", "u", "v"):
+        assert np.array_equal(ga[k], go[k]), k
+    # a state far beyond the CFL bound, continued from step 1030 (slot 6 of the ring)
+    a.upload(ga["eta"], ga["u"] * 1e3, ga["v"], mode=lib.UPLOAD_CONTINUE)
+    assert a.step(5) == lib.ERR_CFL
+    assert a.error_step() == 1030
