@@ -135,13 +135,6 @@ class ClockSampler:
                 "samples": len(rows), "samples_under_load": len(busy)}
 
 
-def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
-
-
 def make_workload(name: str, seed: int):
     from sw2_gb300 import cases
 
@@ -329,6 +322,8 @@ def main():
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
+    from sw2_gb300.replicas import aggregate, dist_env
+
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference_arm(args, ws, rank)
@@ -354,18 +349,12 @@ def main():
         if pg:
             pg.barrier()
 
-    def max_over_ranks(x):
-        if not pg:
-            return x
-        t = torch.tensor([x], device=f"cuda:{local}", dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
-
     # headline: the FP64 reference-exact step on the drop-in configuration
     clk = ClockSampler(local).__enter__()
     m64 = measure(lib, case, lib.FP64, args.steps, args.warmup, local, barrier)
-    ms = max_over_ranks(m64["ms"])
-    value = cells * args.steps * ws / (ms * 1e-3)
+    dev = f"cuda:{local}"
+    value, _, secs = aggregate(cells * args.steps, m64["ms"] * 1e-3, dev)
+    ms = secs * 1e3
     s = m64["solver"]
 
     # end to end through the C ABI: every step uploads the state from pinned
@@ -383,8 +372,7 @@ def main():
             raise RuntimeError("e2e step failed")
         lib.load().sw2g_download(s.h, *[lib._ptr(h) for h in host], None)
     barrier()
-    e2e_s = max_over_ranks(time.perf_counter() - t0)
-    e2e = cells * args.steps * ws / e2e_s
+    e2e, _, _ = aggregate(cells * args.steps, time.perf_counter() - t0, dev)
     bytes_io = 3 * W * H * 8
     s.close()
 
@@ -394,8 +382,12 @@ def main():
     c32, desc32 = make_workload(args.fp32_config, seed=1 + rank)
     m32b = measure(lib, c32, lib.FP32, args.steps, args.warmup, local, barrier)
     m32b["solver"].close()
+    m64b = measure(lib, c32, lib.FP64, args.steps, args.warmup, local, barrier)
+    m64b["solver"].close()
     clk.__exit__(None, None, None)
-    acc = accuracy(lib, case, args.accuracy_steps, local) if args.accuracy_steps > 0 else None
+    acc = accuracy(lib, c32, args.accuracy_steps, local) if args.accuracy_steps > 0 else None
+    if acc:
+        acc["workload"] = args.fp32_config
     ens = ensemble(lib, args.ensemble_steps, 5, min(args.ensemble_steps, 1000), local) if args.ensemble_steps > 0 else None
 
     if rank != 0:
@@ -442,8 +434,10 @@ def main():
             "fp64": form_line(m64, args.config, cells),
             "fp32": form_line(m32, args.config, cells),
             "fp32_large": form_line(m32b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
+            "fp64_large": form_line(m64b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
         },
         "fp32_over_fp64": m32["value"] / m64["value"],
+        "fp32_over_fp64_large": m32b["value"] / m64b["value"],
         "accuracy_fp32_vs_fp64": acc,
         "ensemble_fp32_batched": ens,
         "fp32_batched_over_fp64": (ens["value"] / m64["value"]) if ens else None,

@@ -45,17 +45,22 @@ typedef enum {
 
 /* Behaviour flags (sw2g_case.flags). Zero reproduces the reference exactly. */
 #define SW2G_FLAG_VANLEER_SAFE 0x1u  /* Van Leer limiter gives 0 (its limit) at r = -1 instead of 0/0 */
+/* Input conventions, for callers that fill sw2g_case from the reference's own
+ * sw struct rather than from the .sw file: */
+#define SW2G_FLAG_RADIANS 0x2u /* lon0..lat1 are in radians, as the sw struct holds them (init.c:56-58) */
+#define SW2G_FLAG_SIGMA 0x4u   /* tau holds sigma_dis (0 = no damping), as the sw struct holds it (init.c:110-114) */
 
 /* The parsed case, as the reference's initialize() stores it in the sw struct
  * (init.c:48-161). Angles are in degrees, as in the .sw file. Polar 0 only. */
 typedef struct {
   int nx, ny;                    /* interior cells; each >= 3 (sppde_core.c:431-459) */
   int sch;                       /* limiter 0..9 (calc.c:262-273) */
-  double lon0, lon1, lat0, lat1; /* degrees */
+  double lon0, lon1, lat0, lat1; /* degrees (radians with SW2G_FLAG_RADIANS) */
   double Omega, rE, rP, gE, depth;
   double Dt;                     /* time step (s) */
   double courant;                /* CFL: Dt must not exceed courant / max(|u|/dx + |v|/dy) */
-  double tau;                    /* Tau: sigma = 1/tau, 0 when tau > 1e10 (init.c:110-114) */
+  double tau;                    /* Tau: sigma = 1/tau, 0 when tau > 1e10 (init.c:110-114);
+                                    sigma itself with SW2G_FLAG_SIGMA */
   double tracer_dis;             /* TracerDis */
   double hypernu[3];             /* Hypernu as entered: nu2, nu4 (positive), nu6 */
   unsigned flags;                /* SW2G_FLAG_* */

@@ -191,10 +191,12 @@ bool case_ok(const sw2g_case* c) {
   if ((long long)(c->nx + 4) * (c->ny + 4) > (1LL << 31) - 1) return false;
   if (!(c->rE > 0) || !(c->rP > 0) || !(c->Dt > 0) || !(c->courant > 0)) return false;
   if (!(c->lon1 > c->lon0) || !(c->lat1 > c->lat0)) return false;
-  if (!(c->lat0 > -90.0) || !(c->lat1 < 90.0)) return false;
+  const double pole = (c->flags & SW2G_FLAG_RADIANS) ? 2.0 * std::atan(1.0) : 90.0;
+  if (!(c->lat0 > -pole) || !(c->lat1 < pole)) return false;
   // init.c:122: hyperviscosity coefficients are entered as non-negative
   if (c->hypernu[0] < 0 || c->hypernu[1] < 0 || c->hypernu[2] < 0) return false;
-  if (c->flags & ~SW2G_FLAG_VANLEER_SAFE) return false;
+  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA)) return false;
+  if ((c->flags & SW2G_FLAG_SIGMA) && !(c->tau >= 0)) return false;
   return true;
 }
 
@@ -483,7 +485,8 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   s.H = c->ny + 4;
   s.depth = c->depth;
   s.Dt = c->Dt;
-  s.sigma = c->tau > 1e10 ? 0 : 1.0 / c->tau;  // init.c:110-114
+  if (c->flags & SW2G_FLAG_SIGMA) s.sigma = c->tau;  // already sigma_dis
+  else s.sigma = c->tau > 1e10 ? 0 : 1.0 / c->tau;     // init.c:110-114
   s.sigma_tr = c->tracer_dis;
   s.nu2 = c->hypernu[0];
   s.nu4 = -c->hypernu[1];  // init.c:120

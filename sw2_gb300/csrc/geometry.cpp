@@ -37,13 +37,17 @@ double g_eff(const Planet& p, double pc) {                                      
 }
 double fcor(const Planet& p, double lat) { return 2.0 * p.Omega * std::sin(lat); }  // sw.h:193
 
+// Band limits in radians: as the .sw file gives them (degrees, converted as
+// init.c:56-58 does), or already converted (SW2G_FLAG_RADIANS).
+double angle(const sw2g_case& c, double a) { return (c.flags & SW2G_FLAG_RADIANS) ? a : deg2rad(a); }
+
 }  // namespace
 
 void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, double* rest_my) {
   const int ny = c.ny, H = c.ny + 4;
   Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};  // init.c:150
-  const double lon0 = deg2rad(c.lon0), lon1 = deg2rad(c.lon1);
-  const double lat0 = deg2rad(c.lat0), lat1 = deg2rad(c.lat1);
+  const double lon0 = angle(c, c.lon0), lon1 = angle(c, c.lon1);
+  const double lat0 = angle(c, c.lat0), lat1 = angle(c, c.lat1);
   const double dlon = (lon1 - lon0) / ((double)c.nx);                    // coords.c:36
   const double dlat = (lat1 - lat0) / ((double)ny);
   auto latn = [&](int j) { return linspace_val(j, lat0, lat1, ny); };    // sw.h:116
@@ -105,8 +109,8 @@ void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, 
 // same expressions as build_rows and allocates nothing.
 void energy_row_geometry(const sw2g_case& c, int j0, int n, double* surf, double* gc) {
   Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};
-  const double lon0 = deg2rad(c.lon0), lon1 = deg2rad(c.lon1);
-  const double lat0 = deg2rad(c.lat0), lat1 = deg2rad(c.lat1);
+  const double lon0 = angle(c, c.lon0), lon1 = angle(c, c.lon1);
+  const double lat0 = angle(c, c.lat0), lat1 = angle(c, c.lat1);
   const double dlon = (lon1 - lon0) / ((double)c.nx);
   const double dlat = (lat1 - lat0) / ((double)c.ny);
   for (int q = 0; q < n; q++) {

@@ -20,6 +20,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libsw2g.so")
 OK, ERR_BAD_ARG, ERR_CFL, ERR_NONFINITE, ERR_TIMEOUT, ERR_CUDA, ERR_NOMEM, ERR_STATE = range(8)
 FP64, FP32 = 0, 1
 FLAG_VANLEER_SAFE = 0x1
+FLAG_RADIANS = 0x2
+FLAG_SIGMA = 0x4
 UPLOAD_RAW, UPLOAD_FRAME, UPLOAD_CONTINUE = 0, 1, 2
 BATCH_MAX = 96
 

@@ -5,6 +5,8 @@ must equal the CPU oracle's, and the interiors must equal the frames the
 reference itself wrote (tests/golden). Energy diagnostics use compensated
 sums instead of the reference's sequential ones: relative tolerance 1e-12.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -164,3 +166,21 @@ def test_gpu_band2048_matches_oracle():
     got = s.download()
     for k in ("eta", "u", "v"):
         assert same(got[k], o.field(k)), k
+
+
+def test_sw_struct_conventions():
+    # a caller that fills the case from the reference's sw struct passes the
+    # band limits in radians and sigma_dis instead of Tau: same bits
+    case = cases.make_case(nx=40, ny=18, sch=2, seed=31, Tau=4e5)
+    a = lib.Solver(case.params)
+    a.upload(*case.fields())
+    assert a.step(9) == lib.OK
+    p = case.params
+    q = dataclasses.replace(p, Tau=1.0 / p.Tau)
+    q.lon0, q.lon1, q.lat0, q.lat1 = (cases.deg2rad(x) for x in (p.lon0, p.lon1, p.lat0, p.lat1))
+    b = lib.Solver(q, flags=lib.FLAG_RADIANS | lib.FLAG_SIGMA)
+    b.upload(*case.fields())
+    assert b.step(9) == lib.OK
+    ga, gb = a.download(), b.download()
+    for k in FIELDS:
+        assert same(ga[k], gb[k]), k
