@@ -67,6 +67,10 @@ KERNEL_BYTES = {
     "f32_main1": 8 * 3 + 4 * 2 + 4 * 2 + 8 + 4 + 4 * 2,  # eta u v, L, 2 hist -> eta, hist, partial Du Dv
     "f32_main2": 8 * 3 + 4 * 2 + 4 * 4 + 8 * 2 + 4 * 2,  # eta u v, partials, 4 hist -> u v, 2 hist
 }
+# DRAM bytes (read + write) of one launch of the dominant kernels on the
+# 2048x1024 workload, from an ncu capture of the same step (one launch each;
+# fast bodies read u, v and the two wind fields once, as the reference does).
+NCU_TRAFFIC = {("band2048", "mass"): 122.29e6, ("band2048", "adv_u"): 74.12e6, ("band2048", "adv_v"): 73.55e6}
 # The whole step: read eta u v, write eta u v, read two history levels of
 # three tendencies, write one (SURVEY-style count for the FP64 form).
 STEP_BYTES = 120
@@ -422,9 +426,10 @@ def main():
         "hbm_gbs_step": STEP_BYTES * value / 1e9,
         "roofline": {"bound": "hbm", "kernel": m64["kernel"], "achieved": m64["achieved_gbs"], "peak": peak,
                      "unit": "GB/s", "frac": (m64["achieved_gbs"] / peak) if m64["achieved_gbs"] else None,
-                     "traffic": None, "peak_kind": peak_kind, "bytes_per_cell": m64["bytes_per_cell"],
+                     "traffic": NCU_TRAFFIC.get((args.config, m64["kernel"])), "peak_kind": peak_kind,
+                     "bytes_per_cell": m64["bytes_per_cell"],
                      "per_launch_ms": m64["per_launch_ms"], "kernel_share": m64["kernel_share"],
-                     "note": "the FP64 form is FP64-issue bound on GB300 (~0.5 T FP64 op/s)"},
+                     "note": "the FP64 form is bound by GB300's FP64 unit (85 % busy in ncu), not by HBM"},
         "kernels_ms_per_step": m64["kernels_ms_per_step"],
         "gpu_launches": m64["launches"],
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},

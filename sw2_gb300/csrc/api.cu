@@ -789,6 +789,37 @@ sw2g_status sw2g_timer_read(const sw2g_ctx* x, int idx, const char** name, long 
 
 }  // extern "C"
 
+extern "C" sw2g_status sw2g_selfcheck_division(const double* divisors, int n, long long samples,
+                                              unsigned long long seed, int device, long long* mismatches) {
+  if (!divisors || n < 1 || samples < 1 || !mismatches) return SW2G_ERR_BAD_ARG;
+  for (int k = 0; k < n; k++)
+    if (!(divisors[k] > 0) || !std::isfinite(divisors[k]) || divisors[k] < 1e-300) return SW2G_ERR_BAD_ARG;
+  CK(cudaSetDevice(device));
+  double* d = nullptr;
+  unsigned long long* bad = nullptr;
+  cudaStream_t st = nullptr;
+  sw2g_status rc = SW2G_OK;
+  auto run = [&]() -> sw2g_status {
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CK(cudaMalloc((void**)&d, sizeof(double) * n));
+    CK(cudaMalloc((void**)&bad, sizeof(unsigned long long)));
+    CK(cudaMemcpyAsync(d, divisors, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st));
+    fp64_check_division(d, n, samples, seed, bad, st);
+    CK(cudaGetLastError());
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *mismatches = (long long)h;
+    return SW2G_OK;
+  };
+  rc = run();
+  if (d) cudaFree(d);
+  if (bad) cudaFree(bad);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}
+
 // ------------------------------------------------------------------ batches
 struct sw2g_batch {
   std::vector<sw2g_ctx*> mem;

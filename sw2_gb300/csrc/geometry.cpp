@@ -92,6 +92,11 @@ void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, 
     R(R_DXE2, j) = R(R_DXE, j) + R(R_DXE, j);
     R(R_DYNS, j) = (j + 1 <= ny + 2) ? R(R_DYN, j) + R(R_DYN, j + 1) : 0.0;
     R(R_SURF, j) = R(R_DXC, j) * R(R_DYC, j);
+    R(R_IDYV, j) = 1.0 / R(R_DYV, j);
+    R(R_IDXE2, j) = 1.0 / R(R_DXE2, j);
+    R(R_IDYNS, j) = (j + 1 <= ny + 2) ? 1.0 / R(R_DYNS, j) : 0.0;
+    R(R_IRZC, j) = 1.0 / R(R_RZC, j);
+    R(R_IRZN, j) = 1.0 / R(R_RZN, j);
   }
   // compute_Dt fallback for a flow at rest (calc.c:715-725): depends on geometry only
   double mx = 0, my = 0;

@@ -2,7 +2,9 @@
 // order (core.c:134-338). Compiled with -fmad=false so that no a*b+c is fused:
 // every expression below keeps the association of the reference expression it
 // restates, which makes the results bit-identical to the reference's own
-// single-rank run (divisions and square roots are IEEE-rounded by default).
+// single-rank run (divisions and square roots are IEEE-rounded by default;
+// a division by a per-row metric factor goes through div_rcp, which returns
+// the same IEEE quotient with fewer FP64 instructions).
 #include <cuda_runtime.h>
 
 #include "sw2g_internal.h"
@@ -14,6 +16,28 @@ constexpr int TX = 128;
 
 __device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
 __device__ __forceinline__ double RW(const DevState& s, int t, int j) { return s.rows[t * s.H + j + 1]; }
+
+__device__ __forceinline__ int dexp(double x) {
+  return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffULL);
+}
+
+// Correctly rounded a/b given y = RN(1/b), b a positive normal number, with
+// multiplications and fused multiply-adds (Markstein's method: P. Markstein,
+// IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook of
+// Floating-Point Arithmetic, ch. "division with an FMA"): q1 is within one
+// ulp of a/b, so r1 = a - b*q1 is exact and RN(q1 + r1*y) = RN(a/b).
+// Numerators outside [2^-900, 2^776] (zeros, subnormals: remainders could
+// underflow) use the IEEE division. The row tables hold y = 1.0/b computed
+// by IEEE division on the host. fp64_check_division compares this with the
+// IEEE quotient on random and near-halfway numerators.
+__device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  if ((unsigned)(dexp(a) - 123) > 1799u - 123u) return a / b;
+  const double q0 = __dmul_rn(a, y);
+  const double r0 = __fma_rn(-b, q0, a);
+  const double q1 = __fma_rn(r0, y, q0);
+  const double r1 = __fma_rn(-b, q1, a);
+  return __fma_rn(r1, y, q1);
+}
 
 // calc.c:54-63 with sw.h:104-105 MIN/MAX as ternaries (NaN order as written).
 template <int SCH>
@@ -81,10 +105,10 @@ struct F7 {
   const int j = blockIdx.y + 1;                       \
   if (i > s.nx) return;
 
-// BODYH + damping (calc.c:70-113)
+// BODYH + damping (calc.c:70-113), one cell
 template <int SCH>
-__global__ void k_mass(DevState s, F7 f, double* out) {
-  INTERIOR_IJ
+__device__ __forceinline__ double mass_cell(const DevState& s, const F7& f, int i, int j) {
+  const int W = s.W;
   const double Dt = s.Dt, dxe = RW(s, R_DXE, j), dyn = RW(s, R_DYN, j);
   double qx[5], qy[5];
 #pragma unroll
@@ -93,7 +117,13 @@ __global__ void k_mass(DevState s, F7 f, double* out) {
   double acc = tvd_sum<SCH>(qx, qy, cpos(a, Dt, dxe), cneg(a, Dt, dxe), cpos(b, Dt, dxe), cneg(b, Dt, dxe),
                             cpos(c, Dt, dyn), cneg(c, Dt, dyn), cpos(d, Dt, dyn), cneg(d, Dt, dyn));
   acc -= 2.0 * Dt * (s.sigma) * f.eta[IX(W, i, j)];
-  out[IX(W, i, j)] = acc;
+  return acc;
+}
+
+template <int SCH>
+__global__ void k_mass(DevState s, F7 f, double* out) {
+  INTERIOR_IJ
+  out[IX(W, i, j)] = mass_cell<SCH>(s, f, i, j);
 }
 
 // BODYTRACER (calc.c:117-163)
@@ -115,10 +145,10 @@ __global__ void k_tracer(DevState s, F7 f, double* out) {
   out[IX(W, i, j)] = acc;
 }
 
-// BODYU (calc.c:168-200)
+// BODYU (calc.c:168-200), one cell
 template <int SCH>
-__global__ void k_adv_u(DevState s, F7 f, double* out) {
-  INTERIOR_IJ
+__device__ __forceinline__ double advu_cell(const DevState& s, const F7& f, int i, int j) {
+  const int W = s.W;
   const double Dt = s.Dt, dxc = RW(s, R_DXC, j), dyv = RW(s, R_DYV, j);
   double qx[5], qy[5];
 #pragma unroll
@@ -129,13 +159,19 @@ __global__ void k_adv_u(DevState s, F7 f, double* out) {
                                  cneg2(u0, uep, Dt, dxc), cpos2(vs0, vs1, Dt, dyv), cneg2(vs0, vs1, Dt, dyv),
                                  cpos2(vn0, vn1, Dt, dyv), cneg2(vn0, vn1, Dt, dyv));
   const double p2 = Dt * (u0 * (uep - uwm) / RW(s, R_DXE2, j) + u0 * ((vn0 + vn1) / 2. - (vs0 + vs1) / 2.) / dyv);
-  out[IX(W, i, j)] = p1 + p2;
+  return p1 + p2;
 }
 
-// BODYV (calc.c:205-237)
 template <int SCH>
-__global__ void k_adv_v(DevState s, F7 f, double* out) {
+__global__ void k_adv_u(DevState s, F7 f, double* out) {
   INTERIOR_IJ
+  out[IX(W, i, j)] = advu_cell<SCH>(s, f, i, j);
+}
+
+// BODYV (calc.c:205-237), one cell
+template <int SCH>
+__device__ __forceinline__ double advv_cell(const DevState& s, const F7& f, int i, int j) {
+  const int W = s.W;
   const double Dt = s.Dt, dxv = RW(s, R_DXV, j), dyc = RW(s, R_DYC, j);
   double qx[5], qy[5];
 #pragma unroll
@@ -146,7 +182,416 @@ __global__ void k_adv_v(DevState s, F7 f, double* out) {
                                  cneg2(ue1, ue0, Dt, dxv), cpos2(vsm, v0, Dt, dyc), cneg2(vsm, v0, Dt, dyc),
                                  cpos2(v0, vnp, Dt, dyc), cneg2(v0, vnp, Dt, dyc));
   const double p2 = Dt * (v0 * ((ue0 + ue1) / 2. - (uw0 + uw1) / 2.) / dxv + v0 * (vnp - vsm) / RW(s, R_DYNS, j));
-  out[IX(W, i, j)] = p1 + p2;
+  return p1 + p2;
+}
+
+template <int SCH>
+__global__ void k_adv_v(DevState s, F7 f, double* out) {
+  INTERIOR_IJ
+  out[IX(W, i, j)] = advv_cell<SCH>(s, f, i, j);
+}
+
+// Literal cells for the fast kernels' fallback, kept out of line.
+template <int SCH>
+__device__ __noinline__ double mass_cell_ool(const DevState& s, const F7& f, int i, int j) {
+  return mass_cell<SCH>(s, f, i, j);
+}
+template <int SCH>
+__device__ __noinline__ double advu_cell_ool(const DevState& s, const F7& f, int i, int j) {
+  return advu_cell<SCH>(s, f, i, j);
+}
+template <int SCH>
+__device__ __noinline__ double advv_cell_ool(const DevState& s, const F7& f, int i, int j) {
+  return advv_cell<SCH>(s, f, i, j);
+}
+
+// ------------------------------------------------------------ fast TVD bodies
+// The same values as k_mass, k_adv_u and k_adv_v, bit for bit, with about a
+// third of their FP64 operations. Three properties of the reference formulas
+// (calc.c:41-49, 70-237) make that possible:
+//  (1) x faces. With polar 0 the metric factors DXE, DXC, DXV depend on j
+//      only, so the Courant numbers, limiter ratios and limited values of the
+//      face between columns i-1 and i are the same operations on the same
+//      operands for cell i (its west face) and cell i-1 (its east face). Each
+//      lane of a warp computes the face west of its column; a warp covers 31
+//      cells with 32 faces and takes the east face from the next lane.
+//  (2) y faces. The ratios and limiter values of the face between rows j and
+//      j+1 are shared by both cells; only the Courant numbers differ, since
+//      each cell divides by its own DYN, DYV or DYC. A warp marches up its
+//      rows and carries the face's shared part from one row to the next.
+//  (3) Upwind split. C+ = 0.5(U+|U|)*Dt/DX is +0 when U <= 0, and C- is a
+//      zero when U >= 0 (for the two-velocity averages, when both are), so
+//      the term C*B of an unused side is a zero whenever B is finite, and
+//      0.5(U+|U|) = U exactly when U > 0 (0.5(U-|U|) = U when U < 0). Leaving
+//      zero terms out of a sum of otherwise identical terms, in the same
+//      order, can change only the sign of a zero result. So the unused side
+//      is skipped, and a cell is recomputed literally when its sum is zero,
+//      when an input is not finite, or when the skipped side's limiter ratio
+//      could exceed 2^498 (the bound under which every limiter gives a finite
+//      value, squares included).
+// The Van Leer limiter in its reference form (0/0 at r = -1) keeps the
+// literal kernels.
+constexpr int FW = 31;      // cells per strip along x (32 faces)
+constexpr int FK = 8;       // rows per strip
+constexpr int FWARPS = 4;   // warps per block; each warp takes strips in turn
+constexpr unsigned FULL = 0xffffffffu;
+
+
+// Comparisons on the integer pipe (GB300 issues FP64 compares on its narrow
+// FP64 unit). For finite values they agree with the IEEE comparisons except
+// that -0 orders below +0; on the fast path that can only change the sign of
+// a zero, which cannot reach a nonzero sum (see above), and non-finite inputs
+// are recomputed literally.
+__device__ __forceinline__ long long key(double x) {  // order-preserving integer image
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) & 0x7fffffffffffffffLL) != 0; }
+__device__ __forceinline__ bool gt0(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool lt0(double x) { return key(x) < -1; }
+__device__ __forceinline__ double mn(double a, double b) { return key(a) < key(b) ? a : b; }  // sw.h MIN
+__device__ __forceinline__ double mx(double a, double b) { return key(a) > key(b) ? a : b; }  // sw.h MAX
+
+// The limiters of calc.c:54-63 with the comparisons above.
+template <int SCH>
+__device__ __forceinline__ double limiter_fast(double r) {
+  if constexpr (SCH == 0) return mx(0.0, mn(mn((1 + r) / 2.0, 2.0 * r), 2.0));
+  else if constexpr (SCH == 1) return mx(mx(0.0, mn(2.0 * r, 1.0)), mx(0.0, mn(r, 2.0)));
+  else if constexpr (SCH == 2) return mn(r, 1.0);
+  else if constexpr (SCH == 4) return mx(0.0, mn(2.0 * r, mn((1 + 2.0 * r) / 3.0, 2.0)));
+  else if constexpr (SCH == 7) return mx(0.0, mn(mn(2.0, 2.0 * r), mn(0.25 + 0.75 * r, 0.75 + 0.25 * r)));
+  else if constexpr (SCH == kVanLeerSafe)
+    return (__double_as_longlong(r) == __double_as_longlong(-1.0)) ? 0.0 : (r + fabs(r)) / (1.0 + r);
+  else return limiter<SCH>(r);
+}
+
+
+template <int SCH>
+__device__ __forceinline__ double half_psi(double n, double d) {
+  const double r = nz(d) ? (n / d) : 0.0;  // r2rP / r2rM (calc.c:42-43)
+  return limiter_fast<SCH>(r) * 0.5;
+}
+
+// c*B of one side: B2BP (pos) = q0 + psi*0.5*(1-c)*(q1-q0), or B2BM =
+// q1 - psi*0.5*(1+c)*(q1-q0); 1 + c = 1 - (-c) and q1 - X = q1 + (-X) exactly.
+__device__ __forceinline__ double side_term(bool pos, double c, double hpsi, double q0, double q1, double d) {
+  const double g = 1.0 - (pos ? c : -c);
+  const double X = (hpsi * g) * d;
+  return c * ((pos ? q0 : q1) + (pos ? X : -X));
+}
+
+// Shared part of a face q0|q1 (outer neighbours qm, q2), with the Courant
+// numerators pn = 0.5(...+|...|) >= 0 and mn <= 0 before "*Dt/dx".
+struct Face {
+  double d, q0, q1, pn, mn, hp1, hp2;
+  bool pos1, act, both, ok;
+};
+
+template <int SCH>
+__device__ __forceinline__ Face make_face(double qm, double q0, double q1, double q2, double pn, double mn,
+                                          bool cfin) {
+  Face F;
+  F.d = q1 - q0;
+  F.q0 = q0;
+  F.q1 = q1;
+  F.pn = pn;
+  F.mn = mn;
+  const bool aP = nz(pn), aM = nz(mn);
+  F.pos1 = aP;  // the side computed first: + if in use, else -
+  F.act = aP || aM;
+  F.both = aP && aM;
+  F.hp1 = half_psi<SCH>(aP ? (q0 - qm) : (q2 - q1), F.d);
+  F.hp2 = 0.0;
+  if (__any_sync(FULL, F.both)) {
+    if (F.both) F.hp2 = half_psi<SCH>(q2 - q1, F.d);
+  }
+  const int E = max(max(dexp(qm), dexp(q0)), max(dexp(q1), dexp(q2)));
+  F.ok = cfin && (E < 0x7ff) && (!nz(F.d) || dexp(F.d) + 498 > E);
+  return F;
+}
+
+// The face's two terms for a cell whose metric divisor is dx (idx = 1.0/dx).
+__device__ __forceinline__ void face_terms(const Face& F, double Dt, double dx, double idx, double& tP,
+                                           double& tM) {
+  const double c1 = div_rcp((F.pos1 ? F.pn : F.mn) * Dt, dx, idx);
+  const double t1 = F.act ? side_term(F.pos1, c1, F.hp1, F.q0, F.q1, F.d) : 0.0;
+  tP = F.pos1 ? t1 : 0.0;
+  tM = F.pos1 ? 0.0 : t1;
+  if (__any_sync(FULL, F.both)) {
+    if (F.both) tM = side_term(false, div_rcp(F.mn * Dt, dx, idx), F.hp2, F.q0, F.q1, F.d);
+  }
+}
+#define ROW2(t, it, j) RW(s, t, j), RW(s, it, j)
+
+// Upwind halves of one velocity: 0.5(a+|a|) and 0.5(a-|a|) up to the sign of a zero.
+__device__ __forceinline__ double up_p(double a) { return gt0(a) ? a : 0.0; }
+__device__ __forceinline__ double up_m(double a) { return lt0(a) ? a : 0.0; }
+__device__ __forceinline__ bool fin(double a) { return dexp(a) != 0x7ff; }
+
+// Values of the lane's x neighbours at one row: own value v of column i,
+// aux = the value of column base-2 (lane 0), base-1 (lane 1) or base+32 (lane 31).
+struct XN {
+  double m2, m1, p1;
+};
+__device__ __forceinline__ XN x_neighbours(double v, double aux, int lane) {
+  XN n;
+  n.m2 = __shfl_sync(FULL, v, (lane + 30) & 31);
+  n.m1 = __shfl_sync(FULL, v, (lane + 31) & 31);
+  n.p1 = __shfl_sync(FULL, v, (lane + 1) & 31);
+  const double a1 = __shfl_sync(FULL, aux, 1);
+  if (lane < 2) n.m2 = aux;
+  if (lane == 0) n.m1 = a1;
+  if (lane == 31) n.p1 = aux;
+  return n;
+}
+
+// A strip is 31 columns x FK rows; the warps of the grid take strips in turn
+// (strip = warp id + k * warps in the grid), so a grid sized to the resident
+// warps keeps every SM busy to the end.
+#define FAST_SETUP                                                                          \
+  const int W = s.W, nx = s.nx, ny = s.ny;                                                  \
+  const int lane = threadIdx.x & 31;                                                        \
+  const int nsx = (nx + FW - 1) / FW, nstrips = nsx * ((ny + FK - 1) / FK);                  \
+  const double Dt = s.Dt;                                                                   \
+  for (int strip = blockIdx.x * FWARPS + (threadIdx.x >> 5); strip < nstrips;               \
+       strip += gridDim.x * FWARPS) {                                                       \
+    const int j0 = (strip / nsx) * FK + 1;                                                  \
+    const int jn = min(j0 + FK - 1, ny);                                                    \
+    const int base = (strip % nsx) * FW + 1;                                                \
+    const int i = base + lane;                                                              \
+    const int ic = min(i, nx + 2);                                                          \
+    const int ia = (lane == 0) ? base - 2 : (lane == 1) ? base - 1 : min(base + 32, nx + 2); \
+    const bool own = (lane < FW) && (i <= nx);
+#define FAST_END }
+
+// BODYH + damping, fast form.
+template <int SCH>
+__global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, double* out) {
+  FAST_SETUP
+  const int iu = min(i - 1, nx + 2);
+  const double damp = 2.0 * Dt * (s.sigma);  // calc.c:112: (2.0*Dt*sigma)*ETA
+  // H at this lane's column, rows j-1 .. j+1 (window), and the face south of j0
+  double h1 = HH(ic, j0 - 1), h2 = HH(ic, j0), h3 = HH(ic, j0 + 1);
+  double tsP, tsM;
+  bool oks;
+  {
+    const double b = VW(ic, j0 - 1);
+    const Face F = make_face<SCH>(HH(ic, j0 - 2), h1, h2, h3, up_p(b), up_m(b), fin(b));
+    face_terms(F, Dt, ROW2(R_DYN, R_IDYN, j0), tsP, tsM);
+    oks = F.ok;
+  }
+  for (int j = j0; j <= jn; j++) {
+    const double h4 = HH(ic, j + 2);
+    // x face west of column i, row j
+    const XN xn = x_neighbours(h2, HH(ia, j), lane);
+    const double a = UW(iu, j);
+    const Face FX = make_face<SCH>(xn.m2, xn.m1, h2, xn.p1, up_p(a), up_m(a), fin(a));
+    double twP, twM;
+    face_terms(FX, Dt, ROW2(R_DXE, R_IDXE, j), twP, twM);
+    const double teP = __shfl_sync(FULL, twP, (lane + 1) & 31);
+    const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
+    const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
+    // y face north of row j: shared by this cell and the cell above
+    const double b = VW(ic, j);
+    const Face FY = make_face<SCH>(h1, h2, h3, h4, up_p(b), up_m(b), fin(b));
+    double tnP, tnM, nsP, nsM;
+    face_terms(FY, Dt, ROW2(R_DYN, R_IDYN, j), tnP, tnM);
+    face_terms(FY, Dt, ROW2(R_DYN, R_IDYN, j + 1), nsP, nsM);
+    // calc.c:100 in its order: +w -e +s -n
+    double S = twP + twM;
+    S = S - teP;
+    S = S - teM;
+    S = S + tsP;
+    S = S + tsM;
+    S = S - tnP;
+    S = S - tnM;
+    const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
+    if (own) {
+      double r;
+      if (slow) r = mass_cell_ool<SCH>(s, f, i, j);
+      else r = S - damp * f.eta[IX(W, i, j)];
+      out[IX(W, i, j)] = r;
+    }
+    tsP = nsP;
+    tsM = nsM;
+    oks = FY.ok;
+    h1 = h2;
+    h2 = h3;
+    h3 = h4;
+  }
+  FAST_END
+}
+
+// BODYU, fast form.
+template <int SCH>
+__global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, double* out) {
+  FAST_SETUP
+  const int ic1 = min(i + 1, nx + 2);
+  // U at this lane's column, rows j-1 .. j+1, and V at columns i, i+1 of row j-1
+  double u1 = UW(ic, j0 - 1), u2 = UW(ic, j0), u3 = UW(ic, j0 + 1);
+  double vs0 = VW(ic, j0 - 1), vs1 = VW(ic1, j0 - 1);
+  double tsP, tsM;
+  bool oks;
+  {
+    const Face F = make_face<SCH>(UW(ic, j0 - 2), u1, u2, u3, 0.5 * (up_p(vs0) + up_p(vs1)),
+                                  0.5 * (up_m(vs0) + up_m(vs1)), fin(vs0) && fin(vs1));
+    face_terms(F, Dt, ROW2(R_DYV, R_IDYV, j0), tsP, tsM);
+    oks = F.ok;
+  }
+  for (int j = j0; j <= jn; j++) {
+    const double u4 = UW(ic, j + 2);
+    // x face west of column i, row j: velocities u(i-1), u(i)
+    const XN xn = x_neighbours(u2, UW(ia, j), lane);
+    const Face FX = make_face<SCH>(xn.m2, xn.m1, u2, xn.p1, 0.5 * (up_p(xn.m1) + up_p(u2)),
+                                   0.5 * (up_m(xn.m1) + up_m(u2)), true);
+    double twP, twM;
+    face_terms(FX, Dt, ROW2(R_DXC, R_IDXC, j), twP, twM);
+    const double teP = __shfl_sync(FULL, twP, (lane + 1) & 31);
+    const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
+    const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
+    // y face north of row j: velocities v(i, j), v(i+1, j)
+    const double vn0 = VW(ic, j), vn1 = VW(ic1, j);
+    const Face FY = make_face<SCH>(u1, u2, u3, u4, 0.5 * (up_p(vn0) + up_p(vn1)), 0.5 * (up_m(vn0) + up_m(vn1)),
+                                   fin(vn0) && fin(vn1));
+    double tnP, tnM, nsP, nsM;
+    face_terms(FY, Dt, ROW2(R_DYV, R_IDYV, j), tnP, tnM);
+    face_terms(FY, Dt, ROW2(R_DYV, R_IDYV, j + 1), nsP, nsM);
+    double S = twP + twM;
+    S = S - teP;
+    S = S - teM;
+    S = S + tsP;
+    S = S + tsM;
+    S = S - tnP;
+    S = S - tnM;
+    const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
+    if (own) {
+      double r;
+      if (slow) {
+        r = advu_cell_ool<SCH>(s, f, i, j);
+      } else {
+        const double uwm = xn.m1, u0 = u2, uep = xn.p1;  // calc.c:198
+        const double p2 = Dt * (div_rcp(u0 * (uep - uwm), ROW2(R_DXE2, R_IDXE2, j)) +
+                                div_rcp(u0 * ((vn0 + vn1) / 2. - (vs0 + vs1) / 2.), ROW2(R_DYV, R_IDYV, j)));
+        r = S + p2;
+      }
+      out[IX(W, i, j)] = r;
+    }
+    tsP = nsP;
+    tsM = nsM;
+    oks = FY.ok;
+    vs0 = vn0;
+    vs1 = vn1;
+    u1 = u2;
+    u2 = u3;
+    u3 = u4;
+  }
+  FAST_END
+}
+
+// BODYV, fast form.
+template <int SCH>
+__global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, double* out) {
+  FAST_SETUP
+  const int iu = min(i - 1, nx + 2);
+  // V at this lane's column, rows j-1 .. j+1; U at column i-1, row j
+  double v1 = VW(ic, j0 - 1), v2 = VW(ic, j0), v3 = VW(ic, j0 + 1);
+  double uw0 = UW(iu, j0);
+  double tsP, tsM;
+  bool oks;
+  {
+    const Face F = make_face<SCH>(VW(ic, j0 - 2), v1, v2, v3, 0.5 * (up_p(v1) + up_p(v2)),
+                                  0.5 * (up_m(v1) + up_m(v2)), true);
+    face_terms(F, Dt, ROW2(R_DYC, R_IDYC, j0), tsP, tsM);
+    oks = F.ok;
+  }
+  for (int j = j0; j <= jn; j++) {
+    const double v4 = VW(ic, j + 2);
+    const double uw1 = UW(iu, j + 1);
+    // x face west of column i, row j: velocities u(i-1, j+1), u(i-1, j)
+    const XN xn = x_neighbours(v2, VW(ia, j), lane);
+    const Face FX = make_face<SCH>(xn.m2, xn.m1, v2, xn.p1, 0.5 * (up_p(uw1) + up_p(uw0)),
+                                   0.5 * (up_m(uw1) + up_m(uw0)), fin(uw1) && fin(uw0));
+    double twP, twM;
+    face_terms(FX, Dt, ROW2(R_DXV, R_IDXV, j), twP, twM);
+    const double teP = __shfl_sync(FULL, twP, (lane + 1) & 31);
+    const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
+    const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
+    const double ue0 = __shfl_sync(FULL, uw0, (lane + 1) & 31);  // u(i, j), u(i, j+1)
+    const double ue1 = __shfl_sync(FULL, uw1, (lane + 1) & 31);
+    // y face north of row j: velocities v(i, j), v(i, j+1)
+    const Face FY = make_face<SCH>(v1, v2, v3, v4, 0.5 * (up_p(v2) + up_p(v3)), 0.5 * (up_m(v2) + up_m(v3)), true);
+    double tnP, tnM, nsP, nsM;
+    face_terms(FY, Dt, ROW2(R_DYC, R_IDYC, j), tnP, tnM);
+    face_terms(FY, Dt, ROW2(R_DYC, R_IDYC, j + 1), nsP, nsM);
+    double S = twP + twM;
+    S = S - teP;
+    S = S - teM;
+    S = S + tsP;
+    S = S + tsM;
+    S = S - tnP;
+    S = S - tnM;
+    const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
+    if (own) {
+      double r;
+      if (slow) {
+        r = advv_cell_ool<SCH>(s, f, i, j);
+      } else {
+        const double vsm = v1, v0 = v2, vnp = v3;  // calc.c:235
+        const double p2 = Dt * (div_rcp(v0 * ((ue0 + ue1) / 2. - (uw0 + uw1) / 2.), ROW2(R_DXV, R_IDXV, j)) +
+                                div_rcp(v0 * (vnp - vsm), ROW2(R_DYNS, R_IDYNS, j)));
+        r = S + p2;
+      }
+      out[IX(W, i, j)] = r;
+    }
+    tsP = nsP;
+    tsM = nsM;
+    oks = FY.ok;
+    uw0 = uw1;
+    v1 = v2;
+    v2 = v3;
+    v3 = v4;
+  }
+  FAST_END
+}
+#undef FAST_SETUP
+#undef FAST_END
+#undef ROW2
+
+// Self-check of div_rcp: for each divisor b, `samples` numerators a drawn
+// from a SplitMix64 stream (random significands over exponents 2^-950..2^60,
+// both signs, and numerators whose quotient lies within a few ulps of a
+// rounding midpoint), compared bit for bit with the IEEE quotient a/b.
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long& x) {
+  unsigned long long z = (x += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__global__ void k_check_division(const double* div, int n, long long samples, unsigned long long seed,
+                                 unsigned long long* bad) {
+  const long long total = (long long)n * samples;
+  unsigned long long miss = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double b = div[t / samples];
+    const double y = 1.0 / b;
+    unsigned long long st = seed ^ (unsigned long long)t * 0xD1B54A32D192ED03ULL;
+    const unsigned long long r1 = splitmix(st), r2 = splitmix(st);
+    double a;
+    if (r2 & 1) {  // random significand and exponent
+      const unsigned long long e = 73 + (r2 >> 1) % 1010;  // 2^-950 .. 2^59
+      a = __longlong_as_double((long long)((e << 52) | (r1 & 0xFFFFFFFFFFFFFULL) | (r2 & 2 ? 1ULL << 63 : 0)));
+    } else {  // a = b * (q + half an ulp of q + small offset): quotient near a midpoint
+      const unsigned long long e = 523 + (r2 >> 1) % 500;
+      const double q = __longlong_as_double((long long)((e << 52) | (r1 & 0xFFFFFFFFFFFFFULL)));
+      const double h = __longlong_as_double((long long)(((e - 53) << 52))) * (double)(((r2 >> 10) & 7) + 1) * 0.5;
+      a = __dmul_rn(b, q + h);
+    }
+    const double want = a / b, got = div_rcp(a, b, y);
+    if (__double_as_longlong(want) != __double_as_longlong(got)) miss++;
+  }
+  if (miss) atomicAdd(bad, miss);
 }
 
 // do_AdamsBashforth (calc.c:651-699) via copy_scaf/linop_scaf (sppde_core.c:247-298)
@@ -174,16 +619,16 @@ __global__ void k_add(DevState s, double* x, const double* dx) {
 __global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* xi) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
-  psi[q] = RW(s, R_KX, j) * (e[IX(W, i + 1, j)] - e[q]) / (RW(s, R_DXC, j));
-  xi[q] = RW(s, R_KY, j) * (e[IX(W, i, j + 1)] - e[q]) / (RW(s, R_DYC, j));
+  psi[q] = div_rcp(RW(s, R_KX, j) * (e[IX(W, i + 1, j)] - e[q]), RW(s, R_DXC, j), RW(s, R_IDXC, j));
+  xi[q] = div_rcp(RW(s, R_KY, j) * (e[IX(W, i, j + 1)] - e[q]), RW(s, R_DYC, j), RW(s, R_IDYC, j));
 }
 
 // laplacian_eta second pass (laplacian.c:125-127)
 __global__ void k_lape_pass2(DevState s, const double* psi, const double* xi, double* eo) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
-  eo[q] = RW(s, R_KC, j) * ((psi[q] - psi[IX(W, i - 1, j)]) / (RW(s, R_DXE, j)) +
-                            (xi[q] - xi[IX(W, i, j - 1)]) / (RW(s, R_DYN, j)));
+  eo[q] = RW(s, R_KC, j) * (div_rcp(psi[q] - psi[IX(W, i - 1, j)], RW(s, R_DXE, j), RW(s, R_IDXE, j)) +
+                            div_rcp(xi[q] - xi[IX(W, i, j - 1)], RW(s, R_DYN, j), RW(s, R_IDYN, j)));
 }
 
 // laplacian_eta wall rows after its halo update (laplacian.c:131-146)
@@ -219,8 +664,9 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double* e = f.eta;
-  const double dup = RW(s, R_MGEDT, j) * (e[IX(W, i + 1, j)] - e[q]) / RW(s, R_DXC, j);
-  const double dvp = RW(s, R_MGNDT, j) * (e[IX(W, i, j + 1)] - e[q]) / RW(s, R_DYC, j + 1);
+  const double dup = div_rcp(RW(s, R_MGEDT, j) * (e[IX(W, i + 1, j)] - e[q]), RW(s, R_DXC, j), RW(s, R_IDXC, j));
+  const double dvp =
+      div_rcp(RW(s, R_MGNDT, j) * (e[IX(W, i, j + 1)] - e[q]), RW(s, R_DYC, j + 1), RW(s, R_IDYC, j + 1));
   double a = duadv[q] + dup;
   double b = dvadv[q] + dvp;
   a -= f.u[q] * s.sigma * s.Dt;
@@ -276,7 +722,7 @@ __global__ void k_coriolis_u(DevState s, double* u, const double* v, const doubl
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
-  const double al = RW(s, R_DTFE, j) + (s.Dt * u[q] * RW(s, R_SINC, j)) / RW(s, R_RZC, j);
+  const double al = RW(s, R_DTFE, j) + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
   const double be = 0.25 * al * al;
   u[q] = (u[q] + duab[q] - be * u[q] + al * semi) / (1.0 + be);
 }
@@ -286,7 +732,7 @@ __global__ void k_coriolis_v(DevState s, const double* u, double* v, const doubl
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
-  const double al = RW(s, R_DTFN, j) + (s.Dt * semi * RW(s, R_SINN, j)) / RW(s, R_RZN, j);
+  const double al = RW(s, R_DTFN, j) + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
   const double be = 0.25 * al * al;
   v[q] = (v[q] + dvab[q] - be * v[q] - al * semi) / (1.0 + be);
 }
@@ -337,8 +783,8 @@ __global__ void k_cfl(DevState s, F7 f, unsigned long long* out) {
   const int j = blockIdx.y + 1;
   double mx = 0, my = 0;
   if (i <= s.nx) {
-    const double ax = fabs(UW(i, j)) / RW(s, R_DXE, j);
-    const double ay = fabs(VW(i, j)) / RW(s, R_DYN, j);
+    const double ax = div_rcp(fabs(UW(i, j)), RW(s, R_DXE, j), RW(s, R_IDXE, j));
+    const double ay = div_rcp(fabs(VW(i, j)), RW(s, R_DYN, j), RW(s, R_IDYN, j));
     mx = (ax > mx) ? ax : mx;
     my = (ay > my) ? ay : my;
   }
@@ -368,8 +814,27 @@ __global__ void k_range(DevState s, const double* x, int* bad) {
 #undef VW
 #undef HH
 
+// Grid of a fast body: the blocks resident on the device at once, or fewer
+// when the grid has fewer strips.
+template <typename K>
+int fast_grid(K kernel, const DevState& s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * FWARPS, 0);
+  const long long strips = (long long)((s.nx + FW - 1) / FW) * ((s.ny + FK - 1) / FK);
+  const long long need = (strips + FWARPS - 1) / FWARPS;
+  const long long full = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+  return (int)(need < full ? need : full);
+}
+
 template <int SCH>
 void launch_bodies(int which, dim3 g, cudaStream_t st, const DevState& s, const F7& f, double* out) {
+  if constexpr (SCH != 3) {
+    if (which == 0) { k_mass_fast<SCH><<<fast_grid(k_mass_fast<SCH>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+    if (which == 2) { k_adv_u_fast<SCH><<<fast_grid(k_adv_u_fast<SCH>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+    if (which == 3) { k_adv_v_fast<SCH><<<fast_grid(k_adv_v_fast<SCH>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+  }
   if (which == 0) k_mass<SCH><<<g, TX, 0, st>>>(s, f, out);
   else if (which == 1) k_tracer<SCH><<<g, TX, 0, st>>>(s, f, out);
   else if (which == 2) k_adv_u<SCH><<<g, TX, 0, st>>>(s, f, out);
@@ -400,6 +865,11 @@ void rotate3(double** h) {
 }
 
 }  // namespace
+
+void fp64_check_division(const double* d_div, int n, long long samples, unsigned long long seed,
+                         unsigned long long* bad, cudaStream_t st) {
+  k_check_division<<<152 * 8, 256, 0, st>>>(d_div, n, samples, seed, bad);
+}
 
 void halo_wrap(double* x, int nx, int ny, cudaStream_t st) {
   const int nh = 4 * (nx + 4) + 4 * ny;

@@ -31,6 +31,7 @@ enum Row {
   R_DXE2,  // DXE+DXE                      calc.c:197
   R_DYNS,  // DYN(j)+DYN(j+1)              calc.c:234
   R_SURF,  // DXC*DYC                      energy.c:40
+  R_IDYV, R_IDXE2, R_IDYNS, R_IRZC, R_IRZN,  // 1.0/x of DYV, DXE2, DYNS, rZ(latc), rZ(latn): divisors of div_rcp
   R_NUM
 };
 
@@ -98,6 +99,11 @@ class Timers {
 
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int step_slot,
               cudaStream_t st, Timers* tm);
+// Compares the step's division by a row metric (div_rcp) with IEEE division
+// on `samples` random numerators per divisor; returns the mismatch count in
+// *bad (device pointer) once the stream is done.
+void fp64_check_division(const double* d_div, int n, long long samples, unsigned long long seed,
+                         unsigned long long* bad, cudaStream_t st);
 // FP32 precision form (step_fp32.cu). Per-row FP32 constants, index j+1.
 enum Q32 {
   Q_KXE, Q_KYN, Q_KXC, Q_KYV, Q_KXV, Q_KYC,  // Dt/DXE, Dt/DYN, Dt/DXC, Dt/DYV, Dt/DXV, Dt/DYC

@@ -29,7 +29,7 @@ SYMBOLS = [
     "sw2g_status_string", "sw2g_create", "sw2g_upload", "sw2g_step", "sw2g_error_step", "sw2g_download",
     "sw2g_diag", "sw2g_reset_ab", "sw2g_steps_done", "sw2g_device_field", "sw2g_stream", "sw2g_last_launches",
     "sw2g_destroy", "sw2g_last_step_ms", "sw2g_timers_enable", "sw2g_timers_reset", "sw2g_timers_count",
-    "sw2g_timer_read",
+    "sw2g_timer_read", "sw2g_selfcheck_division",
 ]
 
 
@@ -90,6 +90,19 @@ def load():
                                       ctypes.POINTER(ctypes.c_longlong), dp]
         _lib = L
     return _lib
+
+
+def selfcheck_division(divisors, samples: int, seed: int = 1, device: int = 0) -> int:
+    """Mismatches of the step's metric division against IEEE division."""
+    L = load()
+    L.sw2g_selfcheck_division.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_longlong,
+                                          ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]
+    d = np.ascontiguousarray(divisors, dtype=np.float64)
+    out = ctypes.c_longlong()
+    rc = L.sw2g_selfcheck_division(_ptr(d), len(d), int(samples), int(seed), int(device), ctypes.byref(out))
+    if rc != OK:
+        raise SW2GError(rc, "sw2g_selfcheck_division")
+    return out.value
 
 
 def status_string(code: int) -> str:
