@@ -70,7 +70,7 @@ KERNEL_BYTES = {
 # DRAM bytes (read + write) of one launch of the dominant kernels on the
 # 2048x1024 workload, from an ncu capture of the same step (one launch each;
 # fast bodies read u, v and the two wind fields once, as the reference does).
-NCU_TRAFFIC = {("band2048", "mass"): 122.29e6, ("band2048", "adv_u"): 74.12e6, ("band2048", "adv_v"): 73.55e6}
+NCU_TRAFFIC = {("band2048", "mass"): 121.04e6, ("band2048", "adv_u"): 76.42e6, ("band2048", "adv_v"): 76.31e6}
 # The whole step: read eta u v, write eta u v, read two history levels of
 # three tendencies, write one (SURVEY-style count for the FP64 form).
 STEP_BYTES = 120
