@@ -98,6 +98,15 @@ sw2g_status sw2g_upload(sw2g_ctx *ctx, const double *eta, const double *u, const
  * is then unspecified. */
 sw2g_status sw2g_step(sw2g_ctx *ctx, int nsteps);
 
+/* One step in two halves, for callers that add the reference's forcing where
+ * it adds it (core.c:292-294): sw2g_step_open runs the step through the
+ * velocity halo update (core.c:134-290); the forcing calls below may then
+ * change eta, u, v and the tracer; sw2g_step_close applies do_channel and the
+ * range checks (core.c:303-312) and returns the step's status as sw2g_step
+ * does. FP64 contexts only; no other step call may come in between. */
+sw2g_status sw2g_step_open(sw2g_ctx *ctx);
+sw2g_status sw2g_step_close(sw2g_ctx *ctx);
+
 /* Step index of the last CFL/range failure, -1 if none. */
 int sw2g_error_step(const sw2g_ctx *ctx);
 
@@ -114,6 +123,23 @@ sw2g_status sw2g_reset_ab(sw2g_ctx *ctx);
 
 /* Steps taken since the last upload. */
 long long sw2g_steps_done(const sw2g_ctx *ctx);
+
+/* Forcing between steps, for the reference's time-dependent perturbations
+ * (add_Gaussians and add_vortices, perturbs.c:22-477), which it applies after
+ * a step's velocity update. FP64 contexts only; `which` is 0 eta, 1 u, 2 v,
+ * 3 tracer; arrays are padded host arrays of which the interior is read; each
+ * call ends with the single-rank halo wrap of the field.
+ *   sw2g_add_field:       field(i,j) += scale * delta(i,j)   (perturbs.c:308, 474-481)
+ *   sw2g_set_field_where: field(i,j) = value(i,j) where mask(i,j) != 0 (perturbs.c:356-358)
+ *   sw2g_apply_channel:   do_channel on u, v, windx and windy (calc.c:600-649), for
+ *                         the forcing at t0, which the reference follows with it
+ *                         (core.c:96-101).
+ * During a run, apply the forcing between sw2g_step_open and sw2g_step_close:
+ * the reference's halo update copies wall-row values into the x halos before
+ * its do_channel, so the order is part of the result. */
+sw2g_status sw2g_add_field(sw2g_ctx *ctx, int which, const double *delta, double scale);
+sw2g_status sw2g_set_field_where(sw2g_ctx *ctx, int which, const double *value, const unsigned char *mask);
+sw2g_status sw2g_apply_channel(sw2g_ctx *ctx);
 
 /* Device pointer of a padded state field (0 eta, 1 u, 2 v, 3 tracer) for
  * callers that keep data on the GPU; NULL on a bad index. */

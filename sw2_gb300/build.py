@@ -1,4 +1,7 @@
-"""Builds libsw2g.so in-tree (sw2_gb300/_build/) for sm_103a.
+"""Builds, in-tree (sw2_gb300/_build/):
+  libsw2g.so    the GPU step behind the C ABI, for sm_103a;
+  libsw2host.so the case reader and forcing restatement (plain C, no CUDA);
+  sw2g-run      the command-line runner of SW2 case files (host/swmain.c).
 
 Translation units compile in parallel; the FP64 step is compiled with
 -fmad=false (no contraction, for bit-identity with the reference) and host
@@ -19,6 +22,11 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libsw2g.so")
+HOSTDIR = os.path.join(HERE, "host")
+HOSTLIB = os.path.join(OUT, "libsw2host.so")
+RUNNER = os.path.join(OUT, "sw2g-run")
+HOST_SRC = ["swcase.c", "swforce.c"]
+HOST_C = ["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST = "-fPIC,-ffp-contract=off,-O2"
@@ -58,11 +66,30 @@ def _compile(src: str, extra) -> str:
 
 
 def _stale() -> bool:
-    if not os.path.exists(LIB):
+    outs = [LIB, HOSTLIB, RUNNER]
+    if not all(os.path.exists(o) for o in outs):
         return True
-    t = os.path.getmtime(LIB)
-    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "sw2g.h"), __file__]
+    t = min(os.path.getmtime(o) for o in outs)
+    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HOSTDIR, f) for f in os.listdir(HOSTDIR)]
+    srcs += [os.path.join(ROOT, "include", "sw2g.h"), __file__]
     return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+
+
+def build_host() -> None:
+    """libsw2host.so and sw2g-run (the runner links libsw2g.so, found next to it)."""
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", HOSTDIR]
+    srcs = [os.path.join(HOSTDIR, f) for f in HOST_SRC]
+    _run([*HOST_C, "-shared", *inc, *srcs, "-o", HOSTLIB + ".tmp", "-lm"])
+    os.replace(HOSTLIB + ".tmp", HOSTLIB)
+    run_srcs = srcs + [os.path.join(HOSTDIR, "swrun.c"), os.path.join(HOSTDIR, "swmain.c")]
+    _run([*HOST_C, *inc, *run_srcs, "-o", RUNNER + ".tmp", "-L", OUT, "-lsw2g", "-Wl,-rpath,$ORIGIN", "-lm"])
+    os.replace(RUNNER + ".tmp", RUNNER)
 
 
 def build(force: bool = False) -> str:
@@ -77,6 +104,7 @@ def build(force: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_host()
     return LIB
 
 

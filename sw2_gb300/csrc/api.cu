@@ -158,6 +158,7 @@ struct sw2g_ctx {
   long long steps = 0;
   int err_step = -1;
   long long last_launches = 0;
+  bool open = false;  // between sw2g_step_open and sw2g_step_close
   // FP32 precision form
   Fp32Engine e32;
   Fp32Ctx c32{};
@@ -169,6 +170,9 @@ struct sw2g_ctx {
   float* d_aux32[3] = {nullptr, nullptr, nullptr};   // the same in FP32 for the stencils
   double* d_tmp = nullptr;         // full eta for download and diagnostics
   BatchExec run32;                 // this context as a batch of one
+  // forcing between steps (FP64 form): staging of one padded field and a mask
+  double* d_force = nullptr;
+  void* d_mask = nullptr;
 };
 
 namespace {
@@ -591,7 +595,7 @@ sw2g_status sw2g_upload(sw2g_ctx* x, const double* eta, const double* u, const d
 
 sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
   if (!x || nsteps < 0) return SW2G_ERR_BAD_ARG;
-  if (!x->uploaded) return SW2G_ERR_STATE;
+  if (!x->uploaded || x->open) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
   x->last_launches = 0;
   std::vector<unsigned long long> cfl(2 * kChunk);
@@ -673,6 +677,57 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
   return SW2G_OK;
 }
 
+sw2g_status sw2g_step_open(sw2g_ctx* x) {
+  if (!x) return SW2G_ERR_BAD_ARG;
+  if (x->precision != SW2G_FP64) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded || x->open) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  CK(cudaMemsetAsync(x->d_cfl, 0, sizeof(unsigned long long) * 2, x->stream));
+  CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int), x->stream));
+  StepChecks chk{x->d_cfl, x->d_bad};
+  CK(cudaEventRecord(x->ev[0], x->stream));
+  x->last_launches = fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, 0, x->stream, &x->timers, STEP_HEAD);
+  CK(cudaGetLastError());
+  x->k++;
+  x->open = true;
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_step_close(sw2g_ctx* x) {
+  if (!x) return SW2G_ERR_BAD_ARG;
+  if (!x->open) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  StepChecks chk{x->d_cfl, x->d_bad};
+  x->last_launches += fp64_step(x->s, x->b, x->sch, x->k - 1, x->tracer_active, chk, 0, x->stream, &x->timers,
+                                STEP_TAIL);
+  CK(cudaEventRecord(x->ev[1], x->stream));
+  CK(cudaGetLastError());
+  x->open = false;
+  unsigned long long cfl[2] = {0, 0};
+  int bad = 0;
+  CK(cudaMemcpyAsync(cfl, x->d_cfl, sizeof cfl, cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaMemcpyAsync(&bad, x->d_bad, sizeof bad, cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
+  x->last_step_ms = ms;
+  if (x->timers.on) x->timers.collect();
+  double mx, my;
+  std::memcpy(&mx, &cfl[0], sizeof(double));
+  std::memcpy(&my, &cfl[1], sizeof(double));
+  if (mx + my == 0) { mx = x->rest_mx; my = x->rest_my; }
+  if (x->c.Dt > (x->c.courant / (mx + my))) {  // core.c:158
+    x->err_step = (int)x->steps;
+    return SW2G_ERR_CFL;
+  }
+  x->steps += 1;
+  if (bad) {
+    x->err_step = (int)(x->steps - 1);
+    return SW2G_ERR_NONFINITE;
+  }
+  return SW2G_OK;
+}
+
 int sw2g_error_step(const sw2g_ctx* x) { return x ? x->err_step : -1; }
 long long sw2g_steps_done(const sw2g_ctx* x) { return x ? x->steps : 0; }
 long long sw2g_last_launches(const sw2g_ctx* x) { return x ? x->last_launches : 0; }
@@ -736,6 +791,76 @@ sw2g_status sw2g_reset_ab(sw2g_ctx* x) {
   return SW2G_OK;
 }
 
+namespace {
+// Forcing calls are for uploaded FP64 contexts; the staging field is
+// allocated on first use.
+sw2g_status force_ready(sw2g_ctx* x, int which) {
+  if (!x || which < 0 || which > 3) return SW2G_ERR_BAD_ARG;
+  if (x->precision != SW2G_FP64) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  if (!x->d_force) {
+    sw2g_status st = dalloc(x, &x->d_force, (size_t)x->s.W * x->s.H);
+    if (st != SW2G_OK) return st;
+  }
+  return SW2G_OK;
+}
+}  // namespace
+
+sw2g_status sw2g_add_field(sw2g_ctx* x, int which, const double* delta, double scale) {
+  sw2g_status st = force_ready(x, which);
+  if (st != SW2G_OK) return st;
+  if (!delta) return SW2G_ERR_BAD_ARG;
+  const size_t S = (size_t)x->s.W * x->s.H;
+  CK(cudaMemcpyAsync(x->d_force, delta, S * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  fp64_add_scaled(x->b.f[which], x->d_force, scale, x->s.nx, x->s.ny, x->stream);
+  CK(cudaGetLastError());
+  if (which == 3 && !x->tracer_active) {
+    // the tracer step runs once any interior tracer value can be nonzero
+    for (int j = 1; j <= x->s.ny && !x->tracer_active; j++)
+      for (int i = 1; i <= x->s.nx; i++)
+        if (delta[(i + 1) + (size_t)(j + 1) * x->s.W] != 0.0 || std::signbit(delta[(i + 1) + (size_t)(j + 1) * x->s.W])) {
+          x->tracer_active = true;
+          break;
+        }
+  }
+  CK(cudaStreamSynchronize(x->stream));
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_set_field_where(sw2g_ctx* x, int which, const double* value, const unsigned char* mask) {
+  sw2g_status st = force_ready(x, which);
+  if (st != SW2G_OK) return st;
+  if (!value || !mask) return SW2G_ERR_BAD_ARG;
+  const size_t S = (size_t)x->s.W * x->s.H;
+  if (!x->d_mask) CK(cudaMalloc(&x->d_mask, S));
+  CK(cudaMemcpyAsync(x->d_force, value, S * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->d_mask, mask, S, cudaMemcpyHostToDevice, x->stream));
+  fp64_set_where(x->b.f[which], x->d_force, (const unsigned char*)x->d_mask, x->s.nx, x->s.ny, x->stream);
+  CK(cudaGetLastError());
+  if (which == 3 && !x->tracer_active) {
+    for (int j = 1; j <= x->s.ny && !x->tracer_active; j++)
+      for (int i = 1; i <= x->s.nx; i++) {
+        const size_t q = (i + 1) + (size_t)(j + 1) * x->s.W;
+        if (mask[q] && (value[q] != 0.0 || std::signbit(value[q]))) {
+          x->tracer_active = true;
+          break;
+        }
+      }
+  }
+  CK(cudaStreamSynchronize(x->stream));
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_apply_channel(sw2g_ctx* x) {
+  sw2g_status st = force_ready(x, 0);
+  if (st != SW2G_OK) return st;
+  fp64_channel(x->b.f[1], x->b.f[2], x->b.f[4], x->b.f[5], x->s.nx, x->s.ny, x->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(x->stream));
+  return SW2G_OK;
+}
+
 void* sw2g_device_field(sw2g_ctx* x, int which) {
   if (!x || which < 0 || which > 3) return nullptr;
   if (x->precision == SW2G_FP32) {
@@ -756,6 +881,7 @@ void sw2g_destroy(sw2g_ctx* x) {
   for (void* p : x->allocs32) cudaFree(p);
   if (x->d_cfl) cudaFree(x->d_cfl);
   if (x->d_bad) cudaFree(x->d_bad);
+  if (x->d_mask) cudaFree(x->d_mask);
   x->timers.release();
   x->run32.release();
   for (int e = 0; e < 2; e++)

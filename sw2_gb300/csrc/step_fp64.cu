@@ -866,6 +866,43 @@ void rotate3(double** h) {
 
 }  // namespace
 
+namespace {
+// Forcing between steps (perturbs.c): field += scale * delta, or field =
+// value where mask, over the interior cells.
+__global__ void k_add_scaled(int nx, int ny, double* f, const double* d, double scale) {
+  const int W = nx + 4;
+  const int n = nx * ny;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int q = IX(W, t % nx + 1, t / nx + 1);
+    f[q] += scale * d[q];
+  }
+}
+__global__ void k_set_where(int nx, int ny, double* f, const double* val, const unsigned char* mask) {
+  const int W = nx + 4;
+  const int n = nx * ny;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int q = IX(W, t % nx + 1, t / nx + 1);
+    if (mask[q]) f[q] = val[q];
+  }
+}
+}  // namespace
+
+void fp64_add_scaled(double* f, const double* d, double scale, int nx, int ny, cudaStream_t st) {
+  const int n = nx * ny, blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_add_scaled<<<blocks, 256, 0, st>>>(nx, ny, f, d, scale);
+  halo_wrap(f, nx, ny, st);
+}
+
+void fp64_set_where(double* f, const double* val, const unsigned char* mask, int nx, int ny, cudaStream_t st) {
+  const int n = nx * ny, blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_set_where<<<blocks, 256, 0, st>>>(nx, ny, f, val, mask);
+  halo_wrap(f, nx, ny, st);
+}
+
+void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, cudaStream_t st) {
+  k_channel<<<(nx + 127) / 128, 128, 0, st>>>(nx, ny, u, v, wx, wy);
+}
+
 void fp64_check_division(const double* d_div, int n, long long samples, unsigned long long seed,
                          unsigned long long* bad, cudaStream_t st) {
   k_check_division<<<152 * 8, 256, 0, st>>>(d_div, n, samples, seed, bad);
@@ -878,7 +915,7 @@ void halo_wrap(double* x, int nx, int ny, cudaStream_t st) {
 
 // One reference time step; returns the number of kernels launched.
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
-              cudaStream_t st, Timers* tm) {
+              cudaStream_t st, Timers* tm, int parts) {
 #define LAUNCH(tag, ...)                          \
   do {                                            \
     if (tm && tm->on) tm->begin(tag, st);         \
@@ -893,6 +930,7 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
   const bool hyper = (s.nu2 != 0 || s.nu4 != 0 || s.nu6 != 0);
 
+  if (parts & STEP_HEAD) {
   // compute_Dt (core.c:155-159): maxima at the start of the step
   LAUNCH("cfl", k_cfl<<<g, TX, 0, st>>>(s, F(), chk.cfl + 2 * slot));
 
@@ -961,9 +999,14 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   LAUNCH("coriolis_u", k_coriolis_u<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.duAB));
   LAUNCH("coriolis_v", k_coriolis_v<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dvAB));
 
-  // halos and walls (core.c:287-307); the tracer and eta refresh is idempotent
+  // halos (core.c:287-290)
   LAUNCH("halo", halo_wrap(b.f[1], s.nx, s.ny, st));
   LAUNCH("halo", halo_wrap(b.f[2], s.nx, s.ny, st));
+  }
+  if (!(parts & STEP_TAIL)) return nl;
+  // here the reference adds its time-dependent forcing (core.c:292-294);
+  // the halo refresh of tracer and eta that follows it (core.c:296-300) is
+  // done by the forcing calls themselves, so the tail is the walls and checks
   LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
 
   // range checks of tracer, eta, u, v (core.c:309-312)

@@ -97,8 +97,17 @@ class Timers {
   cudaEvent_t open_ev_ = nullptr;
 };
 
+// Parts of one step: the head runs through the velocity halos (core.c:134-290),
+// the tail the wall fixes and range checks (core.c:303-312); the reference's
+// forcing goes between them.
+constexpr int STEP_HEAD = 1, STEP_TAIL = 2, STEP_FULL = 3;
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int step_slot,
-              cudaStream_t st, Timers* tm);
+              cudaStream_t st, Timers* tm, int parts = STEP_FULL);
+// Forcing between steps on FP64 fields (interior cells, then the halo wrap;
+// fp64_channel is do_channel on u, v and the winds).
+void fp64_add_scaled(double* f, const double* d, double scale, int nx, int ny, cudaStream_t st);
+void fp64_set_where(double* f, const double* val, const unsigned char* mask, int nx, int ny, cudaStream_t st);
+void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, cudaStream_t st);
 // Compares the step's division by a row metric (div_rcp) with IEEE division
 // on `samples` random numerators per divisor; returns the mismatch count in
 // *bad (device pointer) once the stream is done.

@@ -46,6 +46,11 @@ class CaseParams:
     depth: float = 2.5e4
     TracerDis: float = 0.0
     wind: np.ndarray | None = None  # (n, 2) table: latitude deg, u m/s
+    # forcing tables (perturbs.c): rows of 7 vortex values
+    # (t0, lon, lat, a, b, Umax, n) and 12 Gaussian values (t0, t1, tau, lon,
+    # lat, isdegvel, vel, Q, isdegsize, sigma, radius, inject_tracer)
+    vortices: list = field(default_factory=list)
+    gaussians: list = field(default_factory=list)
     extra: dict = field(default_factory=dict)
 
     @property
@@ -86,8 +91,10 @@ def write_sw(path: str, p: CaseParams) -> None:
         f"gE {_g(p.gE)}",
         f"depth {_g(p.depth)}",
         "geoeq 0",
-        "0", "7",          # vortex table: empty
-        "0", "12",         # Gaussian table: empty
+        str(len(p.vortices)), "7",
+        *[" ".join(_g(x) for x in row) for row in p.vortices],
+        str(len(p.gaussians)), "12",
+        *[" ".join(_g(x) for x in row) for row in p.gaussians],
         f"TracerDis {_g(p.TracerDis)}",
     ]
     # a zero table wide enough for the halo-row latitudes of any band (io.c:201-203)

@@ -1,0 +1,294 @@
+/*
+ * sw2g-run: runs an SW2 case file on the GPU step, as the reference's
+ * executable runs it on one rank:
+ *
+ *     sw2g-run [--fp32] [--quiet] NPX NPY CASE OUTDIR      (NPX = NPY = 1)
+ *
+ * reads CASE.sw (swcase.c), builds the initial fields of initialize() and
+ * loop() (init.c:48-237, core.c:88-131: zero state, zonal wind from the
+ * table, the forcing at t0, LoadFrom or frame 0), then runs the time loop of
+ * core.c:131-338 with the step on the GPU (include/sw2g.h) and, after each
+ * step, the reference's forcing (swforce.c), frames every SaveEvery steps
+ * (MAGICSW2, io.c:27-58) and "ENERGY t ke ape ke+ape" lines every IteInfo
+ * steps (energy.c:21-23).
+ *
+ * Differences from the reference: energy sums are compensated (the printed
+ * digits agree); the range check of a step runs before that step's forcing
+ * (the reference checks after it); a flow-rate ramp that covers none of its
+ * three phases injects nothing (the reference leaves the rate unset).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include "sw2g.h"
+#include "swcase.h"
+#include "swforce.h"
+
+#define MAGIC_SW1 27
+#define MAGIC_SW2 28
+#define MAGIC_FIELD 15
+
+static const char *base_name(const char *p) {
+  const char *s = strrchr(p, '/');
+  return s ? s + 1 : p;
+}
+
+/* save_binary_sw (io.c:27-58): the reference writes the gathered interior of
+ * each field with zero halos (sppde_binary_files.c:36-60); so does this. */
+static int write_frame(const char *outdir, const char *bname, int frame, int nstep, double t, int nx, int ny,
+                       double *const f[5]) {
+  for (int k = 0; k < 5; k++)
+    for (int j = -1; j <= ny + 2; j++)
+      for (int i = -1; i <= nx + 2; i++)
+        if (i < 1 || i > nx || j < 1 || j > ny) f[k][(size_t)(i + 1) + (size_t)(j + 1) * (nx + 4)] = 0.0;
+  char path[4096];
+  snprintf(path, sizeof path, "%s/%s.%04d.bin", outdir, base_name(bname), frame);
+  FILE *fo = fopen(path, "wb");
+  if (!fo) {
+    fprintf(stderr, "sw2g-run: cannot write %s\n", path);
+    return -1;
+  }
+  const int magic = MAGIC_SW2, fm = MAGIC_FIELD;
+  const size_t S = (size_t)(nx + 4) * (ny + 4);
+  int ok = fwrite(&magic, sizeof(int), 1, fo) == 1 && fwrite(&nstep, sizeof(int), 1, fo) == 1 &&
+           fwrite(&t, sizeof(double), 1, fo) == 1 && fwrite(&nx, sizeof(int), 1, fo) == 1 &&
+           fwrite(&ny, sizeof(int), 1, fo) == 1;
+  for (int k = 0; k < 5 && ok; k++)
+    ok = fwrite(&fm, sizeof(int), 1, fo) == 1 && fwrite(f[k], sizeof(double), S, fo) == S;
+  fclose(fo);
+  if (!ok) fprintf(stderr, "sw2g-run: short write on %s\n", path);
+  return ok ? 0 : -1;
+}
+
+/* load_binary_sw (io.c:115-171): fields eta, u, v, tracer, perturbs (tracer
+ * absent in MAGICSW1 frames); returns 1 if the file does not exist. */
+static int read_frame(const char *outdir, const char *bname, int frame, int nx, int ny, int *nstep, double *t,
+                      double *const f[5]) {
+  char path[4096];
+  snprintf(path, sizeof path, "%s/%s.%04d.bin", outdir, base_name(bname), frame);
+  FILE *fi = fopen(path, "rb");
+  if (!fi) return 1;
+  int magic = 0, nxr = 0, nyr = 0;
+  int ok = fread(&magic, sizeof(int), 1, fi) == 1 && fread(nstep, sizeof(int), 1, fi) == 1 &&
+           fread(t, sizeof(double), 1, fi) == 1 && fread(&nxr, sizeof(int), 1, fi) == 1 &&
+           fread(&nyr, sizeof(int), 1, fi) == 1;
+  if (!ok || (magic != MAGIC_SW1 && magic != MAGIC_SW2) || nxr != nx || nyr != ny) {
+    fprintf(stderr, "sw2g-run: %s is not a frame of this grid\n", path);
+    fclose(fi);
+    return -1;
+  }
+  const size_t S = (size_t)(nx + 4) * (ny + 4);
+  const int order2[5] = {0, 1, 2, 3, 4}, order1[4] = {0, 1, 2, 4};
+  const int nf = (magic == MAGIC_SW2) ? 5 : 4;
+  for (int k = 0; k < nf && ok; k++) {
+    int fm = 0;
+    ok = fread(&fm, sizeof(int), 1, fi) == 1 && fread(f[magic == MAGIC_SW2 ? order2[k] : order1[k]], sizeof(double), S, fi) == S;
+  }
+  if (magic == MAGIC_SW1) memset(f[3], 0, S * sizeof(double));
+  fclose(fi);
+  if (!ok) fprintf(stderr, "sw2g-run: %s is truncated\n", path);
+  return ok ? 0 : -1;
+}
+
+static int ck(sw2g_status st, const char *what) {
+  if (st == SW2G_OK) return 0;
+  fprintf(stderr, "sw2g-run: %s: %s\n", what, sw2g_status_string(st));
+  return -1;
+}
+
+/* The forcing of the step that ends at time t (core.c:292-302, perturbs.c):
+ * Gaussians, then vortices. During the run it is applied between
+ * sw2g_step_open and sw2g_step_close, where the reference applies it (after
+ * the velocity halos, before do_channel); at t0 it is followed by
+ * sw2g_apply_channel (core.c:96-101). */
+static int apply_forcing(const swcase *c, sw2g_ctx *g, swforce *w, double Dt, double t, char *err, size_t errlen) {
+  const size_t S = (size_t)(c->nx + 4) * (c->ny + 4);
+  memset(w->perturbs, 0, S * sizeof(double));
+  for (int k = 0; k < c->num_gaussians; k++) {
+    double rf = 0;
+    const int rc = swforce_gaussian(c, k, Dt, t, w, &rf, err, errlen);
+    if (rc < 0) return -1;
+    if (rc == 1) continue;
+    if (ck(sw2g_set_field_where(g, 3, w->tracer, w->mask), "tracer")) return -1;
+    if (rf != 0.0 && ck(sw2g_add_field(g, 0, w->pert, rf), "eta")) return -1;
+  }
+  for (int k = 0; k < c->num_vortices; k++) {
+    if (!swforce_vortex_due(c, k, Dt, t)) continue;
+    swforce_vortex(c, k, w);
+    if (ck(sw2g_add_field(g, 0, w->deta, 1.0), "eta") || ck(sw2g_add_field(g, 1, w->du, 1.0), "u") ||
+        ck(sw2g_add_field(g, 2, w->dv, 1.0), "v"))
+      return -1;
+  }
+  return 0;
+}
+
+static int forcing_active(const swcase *c, double Dt, double t) {
+  for (int k = 0; k < c->num_gaussians; k++) {
+    const double *G = c->gaussians + (size_t)k * SWC_GAUSS_COLS;
+    if (G[0] <= t && G[1] >= t) return 1;
+  }
+  for (int k = 0; k < c->num_vortices; k++)
+    if (swforce_vortex_due(c, k, Dt, t)) return 1;
+  return 0;
+}
+
+static int print_energy(sw2g_ctx *g, double t) {
+  double ke, ape, mass;
+  if (ck(sw2g_diag(g, &ke, &ape, &mass), "energy")) return -1;
+  printf("ENERGY %e %e %e %e\n", t, ke, ape, ke + ape);
+  fflush(stdout);
+  return 0;
+}
+
+int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
+  char err[512] = {0}, path[4096];
+  snprintf(path, sizeof path, "%s.sw", bname);
+  swcase c;
+  if (swcase_read(path, &c, err, sizeof err)) {
+    fprintf(stderr, "sw2g-run: %s: %s\n", path, err);
+    return 2;
+  }
+  int rc = 1;
+  sw2g_ctx *g = NULL;
+  swforce w = {0};
+  double *f[5] = {NULL, NULL, NULL, NULL, NULL}, *windx = NULL, *zero = NULL;
+  if (c.polar != 0) {
+    fprintf(stderr, "sw2g-run: polar geometries are not supported\n");
+    goto done;
+  }
+  if (c.reftype != 0 && !quiet) fprintf(stderr, "sw2g-run: reftype %d: the comparison is not run\n", c.reftype);
+  if (fp32 && (c.num_gaussians || c.num_vortices || c.nu6 != 0)) {
+    fprintf(stderr, "sw2g-run: the FP32 form runs cases without forcing and without nu6\n");
+    goto done;
+  }
+  mkdir(outdir, 0775);
+  const int nx = c.nx, ny = c.ny;
+  const size_t S = (size_t)(nx + 4) * (ny + 4);
+  for (int k = 0; k < 5; k++) f[k] = (double *)calloc(S, sizeof(double));
+  windx = (double *)calloc(S, sizeof(double));
+  zero = (double *)calloc(S, sizeof(double));
+  if (!f[0] || !f[1] || !f[2] || !f[3] || !f[4] || !windx || !zero || swforce_init(&w, nx, ny)) {
+    fprintf(stderr, "sw2g-run: out of host memory\n");
+    goto done;
+  }
+  if (swforce_windx(&c, windx, err, sizeof err)) {
+    fprintf(stderr, "sw2g-run: %s\n", err);
+    goto done;
+  }
+  sw2g_case sc;
+  memset(&sc, 0, sizeof sc);
+  sc.nx = nx;
+  sc.ny = ny;
+  sc.sch = c.sch;
+  sc.lon0 = c.lon0;
+  sc.lon1 = c.lon1;
+  sc.lat0 = c.lat0;
+  sc.lat1 = c.lat1;
+  sc.Omega = c.Omega;
+  sc.rE = c.rE;
+  sc.rP = c.rP;
+  sc.gE = c.gE;
+  sc.depth = c.depth;
+  sc.Dt = c.Dt;
+  sc.courant = c.CFL;
+  sc.tau = c.sigma_dis;
+  sc.tracer_dis = c.tracer_dis;
+  sc.hypernu[0] = c.nu2;
+  sc.hypernu[1] = c.nu4;
+  sc.hypernu[2] = c.nu6;
+  sc.flags = SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | (fp32 ? SW2G_FLAG_VANLEER_SAFE : 0u);
+  if (ck(sw2g_create(&sc, fp32 ? SW2G_FP32 : SW2G_FP64, 0, &g), "create")) goto done;
+  /* zero state, winds, zero bottom, all halos already wrapped (core.c:88-94) */
+  if (ck(sw2g_upload(g, zero, zero, zero, zero, windx, zero, zero, SW2G_UPLOAD_RAW), "upload")) goto done;
+  const double Dt = c.Dt;
+  double t = c.t0;
+  /* forcing at t0 and the wall fixes (core.c:96-101) */
+  if (!fp32) {
+    if (apply_forcing(&c, g, &w, Dt, t, err, sizeof err)) {
+      if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
+      goto done;
+    }
+    if (ck(sw2g_apply_channel(g), "channel")) goto done;
+  }
+  int frame = 0, nstart = 0;
+  if (c.loadFrom != 0) {  /* core.c:115-118 */
+    frame = c.loadFrom;
+    int ns = 0;
+    const int lr = read_frame(outdir, bname, frame, nx, ny, &ns, &t, f);
+    if (lr != 0) {
+      if (lr == 1) fprintf(stderr, "sw2g-run: frame %d to be loaded not found\n", frame);
+      goto done;
+    }
+    nstart = ns;
+    memcpy(w.perturbs, f[4], S * sizeof(double));
+    if (ck(sw2g_upload(g, f[0], f[1], f[2], f[3], windx, zero, zero, SW2G_UPLOAD_FRAME), "load")) goto done;
+  } else {
+    if (ck(sw2g_download(g, f[0], f[1], f[2], f[3]), "download")) goto done;
+    memcpy(f[4], w.perturbs, S * sizeof(double));
+    if (write_frame(outdir, bname, frame, 0, t, nx, ny, f)) goto done;
+  }
+  if (print_energy(g, t)) goto done;
+  frame++;
+  nstart++;
+  if (!quiet)
+    fprintf(stderr, "sw2g-run: %s %dx%d, steps %d..%d, Dt %g, %s\n", bname, nx, ny, nstart, c.N, Dt,
+            fp32 ? "FP32 form" : "FP64");
+  for (int n = nstart; n <= c.N;) {
+    /* steps without output or forcing are run in one call */
+    int k = 1;
+    double tk = t + Dt;
+    while (n + k <= c.N && !(n + k - 1 == nstart || (n + k - 1) % c.IteInfo == 0) &&
+           (n + k - 1) % c.saveEvery != 0 && !forcing_active(&c, Dt, tk)) {
+      /* step n+k-1 ends without output and forcing: it can join the next */
+      tk += Dt;
+      k++;
+    }
+    /* the last step of the group takes its forcing between its two halves */
+    const int forced = !fp32 && forcing_active(&c, Dt, tk);
+    sw2g_status st = SW2G_OK;
+    if (k > 1 || !forced) st = sw2g_step(g, forced ? k - 1 : k);
+    if (st == SW2G_OK && forced) {
+      st = sw2g_step_open(g);
+      if (st == SW2G_OK) {
+        if (apply_forcing(&c, g, &w, Dt, tk, err, sizeof err)) {
+          if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
+          goto done;
+        }
+        st = sw2g_step_close(g);
+      }
+    }
+    if (st == SW2G_ERR_CFL || st == SW2G_ERR_NONFINITE) {
+      /* error steps count from the last upload, which preceded step nstart */
+      fprintf(stderr, "sw2g-run: %s at step %d\n",
+              st == SW2G_ERR_CFL ? "Dt exceeds the CFL bound" : "nonsense value detected",
+              nstart + sw2g_error_step(g));
+      rc = 3;
+      goto done;
+    }
+    if (ck(st, "step")) goto done;
+    for (int q = 0; q < k; q++) t += Dt;  /* core.c:145 */
+    n += k;
+    const int m = n - 1;  /* the step just finished */
+    if (!forced) memset(w.perturbs, 0, S * sizeof(double));  /* core.c:292 */
+    if (m % c.saveEvery == 0) {  /* core.c:315-320 */
+      if (ck(sw2g_download(g, f[0], f[1], f[2], f[3]), "download")) goto done;
+      memcpy(f[4], w.perturbs, S * sizeof(double));
+      if (write_frame(outdir, bname, frame, m, t, nx, ny, f)) goto done;
+      frame++;
+    }
+    if (m == nstart || m % c.IteInfo == 0) {  /* core.c:136, 329-332 */
+      if (print_energy(g, t)) goto done;
+    }
+  }
+  rc = 0;
+done:
+  if (g) sw2g_destroy(g);
+  swforce_free(&w);
+  for (int k = 0; k < 5; k++) free(f[k]);
+  free(windx);
+  free(zero);
+  swcase_free(&c);
+  return rc;
+}

@@ -29,7 +29,8 @@ SYMBOLS = [
     "sw2g_status_string", "sw2g_create", "sw2g_upload", "sw2g_step", "sw2g_error_step", "sw2g_download",
     "sw2g_diag", "sw2g_reset_ab", "sw2g_steps_done", "sw2g_device_field", "sw2g_stream", "sw2g_last_launches",
     "sw2g_destroy", "sw2g_last_step_ms", "sw2g_timers_enable", "sw2g_timers_reset", "sw2g_timers_count",
-    "sw2g_timer_read", "sw2g_selfcheck_division",
+    "sw2g_timer_read", "sw2g_selfcheck_division", "sw2g_add_field", "sw2g_set_field_where",
+    "sw2g_apply_channel", "sw2g_step_open", "sw2g_step_close",
 ]
 
 
@@ -212,6 +213,28 @@ class Solver:
                         "sw2g_timer_read")
             out[nm.value.decode()] = (n.value, ms.value)
         return out
+
+    def add_field(self, which: int, delta, scale: float = 1.0):
+        L = load()
+        L.sw2g_add_field.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_double]
+        d = self._arr(delta)
+        self._check(L.sw2g_add_field(self.h, int(which), _ptr(d), float(scale)), "sw2g_add_field")
+
+    def set_field_where(self, which: int, value, mask):
+        L = load()
+        L.sw2g_set_field_where.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_ubyte)]
+        v = self._arr(value)
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        if m.shape != v.shape:
+            raise ValueError("mask shape")
+        self._check(L.sw2g_set_field_where(self.h, int(which), _ptr(v), m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))),
+                    "sw2g_set_field_where")
+
+    def apply_channel(self):
+        L = load()
+        L.sw2g_apply_channel.argtypes = [ctypes.c_void_p]
+        self._check(L.sw2g_apply_channel(self.h), "sw2g_apply_channel")
 
     def device_field(self, which: int) -> int:
         return load().sw2g_device_field(self.h, which)

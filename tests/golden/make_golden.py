@@ -10,6 +10,7 @@ it prints. It then checks the C restatement in oracle/ against the same
 frames bit for bit (the oracle pin) before writing anything.
 
     python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py --forcing  # the forcing cases only
 """
 from __future__ import annotations
 
@@ -30,6 +31,7 @@ from sw2_gb300 import cases, formats  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "SW")
+REF_DIR = os.environ.get("REF", "/root/reference")
 REF_PATH = os.path.join(ROOT, "oracle", "_ref", "bin")
 
 
@@ -71,6 +73,80 @@ CRASH_CASES = {
 HASH_CASES = {
     "h01_band256": (dict(nx=256, ny=128, sch=2, seed=1), 500, 500),
 }
+
+
+# Cases with the reference's time-dependent forcing, run from the reference's
+# own initial state (LoadFrom 0: zero state, winds, forcing at t0, frame 0):
+# golden vectors for the case-file runner (sw2_gb300/host). Each entry gives
+# make_case keyword arguments (for the grid and physics; its fields are not
+# used), the number of steps, SaveEvery, IteInfo and a function that adds
+# the forcing tables.
+def _f01(p):
+    p.gaussians = [[0.0, 20 * p.Dt, 0.0, 100.0, 10.0, 0, 0.0, 2.5e13 / p.Dt, 0, 2.0e6, 5.0e6, 0.0]]
+
+
+def _f02(p):
+    # moving, ramped (rise, plateau, decay), sized in degrees, across the
+    # periodic seam, injecting tracer
+    p.gaussians = [[0.0, 40 * p.Dt, 3 * p.Dt, 2.0, -5.0, 0, -40.0, 1.5e13 / p.Dt, 1, 3.0, 8.0, 1.0]]
+    p.TracerDis = 1.0e-6
+
+
+def _f03(p):
+    p.vortices = [[0.0, 60.0, -20.0, 7.4, 4.7, -100.0, 2.0],
+                  [10.5 * p.Dt, 200.0, 25.0, 6.0, 4.0, 80.0, 1.5]]
+
+
+def _f04(p):
+    # the physics of the reference's examples/JupiterEnergyTest (its .sw and
+    # .planet values): a moving injection on a 90 x 25 degree box
+    p.gaussians = [[0.0, 7 * 86400.0, 0.0, 45.0, -22.5, 0, -3.6, 4.52e11, 0, 3.5e6, 3.5e6, 0.0]]
+
+
+FORCING_CASES = {
+    "f01_gauss_static": (dict(nx=48, ny=24, sch=2, seed=31, jet="none", bumps=0, lat0=-60.0, lat1=60.0),
+                         60, 20, 10, _f01),
+    "f02_gauss_moving_tracer": (dict(nx=64, ny=24, sch=1, seed=32, jet="none", bumps=0, lat0=-50.0, lat1=40.0,
+                                     hyper=False), 60, 20, 5, _f02),
+    "f03_vortices_wind": (dict(nx=60, ny=30, sch=7, seed=33, jet="none", bumps=0, wind="table"), 40, 10, 10, _f03),
+    "f04_jupiter_box": (dict(nx=50, ny=50, sch=1, seed=34, jet="none", bumps=0, hyper=False, lon0=0.0, lon1=90.0,
+                             lat0=-35.0, lat1=-10.0, Dt=50.0, h0=1000.0), 2000, 500, 100, _f04),
+}
+
+
+def forcing_params(name):
+    """CaseParams of a forcing case (also used by the tests to write the .sw)."""
+    kw, nsteps, every, ite, add = FORCING_CASES[name]
+    kw = dict(kw)
+    wind = kw.pop("wind", None)
+    if wind == "table":
+        kw["wind"] = wind_table(30.0, 3.0)
+    case = cases.make_case(**kw, nsteps=nsteps)
+    p = case.params
+    p.nsteps, p.SaveEvery, p.IteInfo, p.LoadFrom = nsteps, every, ite, 0
+    if name == "f04_jupiter_box":
+        p.Omega, p.rE, p.rP, p.gE, p.depth = 0.000176, 7.1492e7, 6.6852e7, 22.58, 1000.0
+        p.CFL, p.Tau, p.hypernu = 0.25, 1e7, (0.0, 0.0, 0.0)
+        p.wind = np.array([[-81.58, 0.0], [78.72, 0.0]])
+    add(p)
+    return p
+
+
+def run_reference_forcing(name, p, workdir):
+    """Run the reference from its own initial state; frames 0.. and ENERGY lines."""
+    os.makedirs(os.path.join(workdir, "out"), exist_ok=True)
+    formats.write_sw(os.path.join(workdir, name + ".sw"), p)
+    env = dict(os.environ, PATH=REF_PATH + os.pathsep + os.environ["PATH"])
+    r = subprocess.run([REF_BIN, "1", "1", name, "out"], cwd=workdir, env=env, capture_output=True, text=True)
+    if r.returncode != 0 or "CRASH" in r.stdout + r.stderr:
+        raise RuntimeError(f"reference failed on {name}:\n{r.stdout[-3000:]}\n{r.stderr[-2000:]}")
+    energy = [ln.split(None, 1)[1].strip() for ln in r.stdout.splitlines() if ln.startswith("ENERGY")]
+    frames = []
+    k = 0
+    while os.path.exists(os.path.join(workdir, "out", f"{name}.{k:04d}.bin")):
+        frames.append(formats.read_frame(os.path.join(workdir, "out", f"{name}.{k:04d}.bin")))
+        k += 1
+    return energy, frames
 
 
 def tweak(name, case):
@@ -177,7 +253,14 @@ def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
     if not os.path.exists(REF_BIN):
         raise SystemExit("reference not built (sources absent?)")
+    only_forcing = "--forcing" in sys.argv  # regenerate the forcing cases only
     manifest = {}
+    if only_forcing:
+        with open(os.path.join(OUT, "manifest.json")) as fh:
+            manifest = {k: v for k, v in json.load(fh).items() if not v.get("forcing")}
+        CRASH_CASES.clear()
+        CASES.clear()
+        HASH_CASES.clear()
     for name, (kw, nsteps) in CRASH_CASES.items():
         case = cases.make_case(**dict(kw, nsteps=nsteps))
         with tempfile.TemporaryDirectory() as wd:
@@ -225,6 +308,32 @@ def main():
             entry["make_case"] = {k: v for k, v in kw.items()}
         manifest[name] = entry
         print(f"{name}: reference and oracle agree bit for bit over {nsteps} steps")
+    for name in FORCING_CASES:
+        p = forcing_params(name)
+        with tempfile.TemporaryDirectory() as wd:
+            energy, frames = run_reference_forcing(name, p, wd)
+        nframes = p.nsteps // p.SaveEvery + 1
+        assert len(frames) == nframes, (name, len(frames), nframes)
+        arrs = {}
+        for fi, (nstep, t, nx, ny, fl) in enumerate(frames):
+            for k in ("eta", "u", "v", "tracer", "perturbs"):
+                arrs[f"f{fi}_{k}"] = np.ascontiguousarray(fl[k])
+            arrs[f"f{fi}_t"] = np.array(t)
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrs)
+        manifest[name] = {"params": params_json(p), "vortices": p.vortices, "gaussians": p.gaussians,
+                          "nsteps": p.nsteps, "save_every": p.SaveEvery, "ite_info": p.IteInfo,
+                          "frames": nframes, "energy_printed": energy, "forcing": True}
+        print(f"{name}: {nframes} reference frames, {len(energy)} ENERGY lines")
+    # the reference's only known-answer file: ENERGY lines of its
+    # examples/JupiterEnergyTest run (an older version of the code), which
+    # f04_jupiter_box mirrors; kept for its first 1e5 s
+    kat = os.path.join(REF_DIR, "examples", "JupiterEnergyTest", "enou.txt")
+    if os.path.exists(kat):
+        with open(kat) as fh:
+            lines = [ln.split(None, 1)[1].strip() for ln in fh if ln.startswith("ENERGY")]
+        manifest["kat_enou"] = {"source": "examples/JupiterEnergyTest/enou.txt",
+                                "energy_printed": [ln for ln in lines if float(ln.split()[0]) <= 1.0e5],
+                                "forcing": True}
     with open(os.path.join(OUT, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1)
 

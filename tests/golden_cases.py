@@ -53,3 +53,27 @@ def load_case(name):
 
 def array_cases():
     return sorted(n for n in manifest() if n.startswith("g"))
+
+
+def forcing_cases():
+    """Cases run by the reference from its own initial state, with forcing."""
+    return sorted(n for n, e in manifest().items() if e.get("forcing") and n.startswith("f"))
+
+
+def forcing_params(name) -> CaseParams:
+    entry = manifest()[name]
+    p = params_of(entry)
+    p.vortices = [list(r) for r in entry["vortices"]]
+    p.gaussians = [list(r) for r in entry["gaussians"]]
+    p.nsteps = entry["nsteps"]
+    return p
+
+
+def forcing_frames(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    frames = []
+    k = 0
+    while f"f{k}_eta" in z:
+        frames.append({n: z[f"f{k}_{n}"] for n in ("eta", "u", "v", "tracer", "perturbs", "t")})
+        k += 1
+    return frames

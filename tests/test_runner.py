@@ -1,0 +1,124 @@
+"""The case-file runner (sw2g-run: C front end + GPU step) against runs of
+the reference executable on the same case files (tests/golden):
+
+* forcing cases (f*): the reference starts from its own initial state
+  (zero fields, zonal wind, forcing at t0, frame 0) and injects Gaussians
+  and vortices during the run; every field of every frame must be bit for bit
+  the reference's, and the ENERGY lines equal to their printed digits;
+* restart cases (g*): the reference loads frame 1 (LoadFrom 1) and saves the
+  following frames; the runner must reproduce them bit for bit;
+* the reference's known-answer file (examples/JupiterEnergyTest/enou.txt, an
+  older version of the code) is met within the reference's own agreement;
+* the FP32 form runs a case file within tolerance of the FP64 step.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from sw2_gb300 import formats, hostlib
+from tests import golden_cases as gc
+
+pytestmark = pytest.mark.gpu
+
+
+def run(workdir, name, args=()):
+    r = subprocess.run([hostlib.RUNNER, "--quiet", *args, "1", "1", name, "out"], cwd=workdir, capture_output=True,
+                       text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    energy = [ln.split(None, 1)[1].strip() for ln in r.stdout.splitlines() if ln.startswith("ENERGY")]
+    frames = {}
+    k = 0
+    while True:
+        path = os.path.join(workdir, "out", f"{name}.{k:04d}.bin")
+        if os.path.exists(path):
+            frames[k] = formats.read_frame(path)
+        elif k > 1:
+            break
+        k += 1
+    return energy, frames
+
+
+def same_energy(a, b, rel=1.5e-6):
+    va, vb = [float(x) for x in a.split()], [float(x) for x in b.split()]
+    return va[0] == vb[0] and all(abs(x - y) <= rel * abs(y) for x, y in zip(va[1:], vb[1:]))
+
+
+@pytest.mark.parametrize("name", gc.forcing_cases())
+def test_forcing_cases_match_the_reference(tmp_path, name):
+    p = gc.forcing_params(name)
+    formats.write_sw(str(tmp_path / f"{name}.sw"), p)
+    energy, frames = run(tmp_path, name)
+    ref = gc.forcing_frames(name)
+    assert sorted(frames) == list(range(len(ref)))
+    for k, rf in enumerate(ref):
+        nstep, t, nx, ny, fl = frames[k]
+        assert t == float(rf["t"]), (k, t, float(rf["t"]))
+        for f in ("eta", "u", "v", "tracer", "perturbs"):
+            d = np.max(np.abs(fl[f] - rf[f]))
+            assert np.array_equal(fl[f], rf[f]), f"frame {k} {f}: max|d|={d}"
+    printed = gc.manifest()[name]["energy_printed"]
+    assert len(energy) == len(printed)
+    for a, b in zip(energy, printed):
+        assert same_energy(a, b), (a, b)
+
+
+@pytest.mark.parametrize("name", ["g01_minmod_nu4", "g11_wind_tracer", "g13_saturn_superbee"])
+def test_restart_cases_match_the_reference(tmp_path, name):
+    entry, case, ref = gc.load_case(name)
+    p = case.params
+    p.LoadFrom = 1
+    formats.write_sw(str(tmp_path / f"{name}.sw"), p)
+    os.makedirs(tmp_path / "out")
+    z = np.zeros_like(case.eta)
+    fr = [np.zeros_like(case.eta) for _ in range(4)]
+    for dst, src in zip(fr, (case.eta, case.u, case.v, case.tracer)):
+        dst[2:-2, 2:-2] = src[2:-2, 2:-2]
+    formats.write_frame(str(tmp_path / "out" / f"{name}.0001.bin"), 0, 0.0, p.nx, p.ny, fr + [z])
+    energy, frames = run(tmp_path, name)
+    assert sorted(k for k in frames if k >= 2) == list(range(2, 2 + len(ref)))
+    for k, rf in enumerate(ref):
+        fl = frames[k + 2][4]
+        for f in ("eta", "u", "v", "tracer"):
+            assert np.array_equal(fl[f][2:-2, 2:-2], rf[f]), f"frame {k + 2} {f}"
+    printed = entry["energy_printed"]
+    assert len(energy) == len(printed)
+    for a, b in zip(energy, printed):
+        assert same_energy(a, "%e %e %e %e" % tuple(b)), (a, b)
+
+
+def test_known_answer_file(tmp_path):
+    name = "f04_jupiter_box"
+    formats.write_sw(str(tmp_path / f"{name}.sw"), gc.forcing_params(name))
+    energy, _ = run(tmp_path, name)
+    kat = gc.manifest()["kat_enou"]["energy_printed"]
+    assert len(energy) >= len(kat)
+    for a, b in zip(energy, kat):
+        t, ke, ape, tot = (float(x) for x in a.split())
+        tk, kek, apek, totk = (float(x) for x in b.split())
+        assert t == tk
+        assert abs(ke - kek) <= 5.5e-4 * abs(kek)
+        assert abs(tot - totk) <= 2.0e-5 * abs(totk)
+
+
+def test_fp32_form_runs_a_case_file(tmp_path):
+    entry, case, ref = gc.load_case("g12_minmod_long")
+    p = case.params
+    p.LoadFrom = 1
+    for sub in ("a", "b"):
+        d = tmp_path / sub
+        os.makedirs(d / "out")
+        formats.write_sw(str(d / "g12.sw"), p)
+        z = np.zeros_like(case.eta)
+        fr = [np.zeros_like(case.eta) for _ in range(4)]
+        for dst, src in zip(fr, (case.eta, case.u, case.v, case.tracer)):
+            dst[2:-2, 2:-2] = src[2:-2, 2:-2]
+        formats.write_frame(str(d / "out" / "g12.0001.bin"), 0, 0.0, p.nx, p.ny, fr + [z])
+    _, f64 = run(tmp_path / "a", "g12")
+    _, f32 = run(tmp_path / "b", "g12", ["--fp32"])
+    last = max(f64)
+    a, b = f64[last][4], f32[last][4]
+    h = a["eta"][2:-2, 2:-2] + p.depth
+    err = np.linalg.norm((b["eta"] - a["eta"])[2:-2, 2:-2]) / np.linalg.norm(h)
+    assert err <= 1e-6, err
