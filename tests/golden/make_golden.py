@@ -103,6 +103,10 @@ def _f04(p):
     p.gaussians = [[0.0, 7 * 86400.0, 0.0, 45.0, -22.5, 0, -3.6, 4.52e11, 0, 3.5e6, 3.5e6, 0.0]]
 
 
+def _f05(p):
+    _f04(p)
+
+
 FORCING_CASES = {
     "f01_gauss_static": (dict(nx=48, ny=24, sch=2, seed=31, jet="none", bumps=0, lat0=-60.0, lat1=60.0),
                          60, 20, 10, _f01),
@@ -111,7 +115,12 @@ FORCING_CASES = {
     "f03_vortices_wind": (dict(nx=60, ny=30, sch=7, seed=33, jet="none", bumps=0, wind="table"), 40, 10, 10, _f03),
     "f04_jupiter_box": (dict(nx=50, ny=50, sch=1, seed=34, jet="none", bumps=0, hyper=False, lon0=0.0, lon1=90.0,
                              lat0=-35.0, lat1=-10.0, Dt=50.0, h0=1000.0), 2000, 500, 100, _f04),
+    # the whole 20-day run of that example (34,560 steps, frames every 12 h),
+    # kept as the ENERGY lines and SHA-256 digests of the last frame
+    "f05_jupiter_example": (dict(nx=50, ny=50, sch=1, seed=34, jet="none", bumps=0, hyper=False, lon0=0.0,
+                                 lon1=90.0, lat0=-35.0, lat1=-10.0, Dt=50.0, h0=1000.0), 34560, 864, 100, _f05),
 }
+HASH_ONLY = {"f05_jupiter_example"}
 
 
 def forcing_params(name):
@@ -124,7 +133,7 @@ def forcing_params(name):
     case = cases.make_case(**kw, nsteps=nsteps)
     p = case.params
     p.nsteps, p.SaveEvery, p.IteInfo, p.LoadFrom = nsteps, every, ite, 0
-    if name == "f04_jupiter_box":
+    if name in ("f04_jupiter_box", "f05_jupiter_example"):
         p.Omega, p.rE, p.rP, p.gE, p.depth = 0.000176, 7.1492e7, 6.6852e7, 22.58, 1000.0
         p.CFL, p.Tau, p.hypernu = 0.25, 1e7, (0.0, 0.0, 0.0)
         p.wind = np.array([[-81.58, 0.0], [78.72, 0.0]])
@@ -314,15 +323,21 @@ def main():
             energy, frames = run_reference_forcing(name, p, wd)
         nframes = p.nsteps // p.SaveEvery + 1
         assert len(frames) == nframes, (name, len(frames), nframes)
-        arrs = {}
-        for fi, (nstep, t, nx, ny, fl) in enumerate(frames):
-            for k in ("eta", "u", "v", "tracer", "perturbs"):
-                arrs[f"f{fi}_{k}"] = np.ascontiguousarray(fl[k])
-            arrs[f"f{fi}_t"] = np.array(t)
-        np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrs)
         manifest[name] = {"params": params_json(p), "vortices": p.vortices, "gaussians": p.gaussians,
                           "nsteps": p.nsteps, "save_every": p.SaveEvery, "ite_info": p.IteInfo,
                           "frames": nframes, "energy_printed": energy, "forcing": True}
+        if name in HASH_ONLY:
+            nstep, t, nx, ny, fl = frames[-1]
+            manifest[name]["last_frame"] = {"t": t, "sha256": {
+                k: hashlib.sha256(np.ascontiguousarray(fl[k]).tobytes()).hexdigest()
+                for k in ("eta", "u", "v", "tracer", "perturbs")}}
+        else:
+            arrs = {}
+            for fi, (nstep, t, nx, ny, fl) in enumerate(frames):
+                for k in ("eta", "u", "v", "tracer", "perturbs"):
+                    arrs[f"f{fi}_{k}"] = np.ascontiguousarray(fl[k])
+                arrs[f"f{fi}_t"] = np.array(t)
+            np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrs)
         print(f"{name}: {nframes} reference frames, {len(energy)} ENERGY lines")
     # the reference's only known-answer file: ENERGY lines of its
     # examples/JupiterEnergyTest run (an older version of the code), which

@@ -7,10 +7,13 @@ the reference executable on the same case files (tests/golden):
   the reference's, and the ENERGY lines equal to their printed digits;
 * restart cases (g*): the reference loads frame 1 (LoadFrom 1) and saves the
   following frames; the runner must reproduce them bit for bit;
-* the reference's known-answer file (examples/JupiterEnergyTest/enou.txt, an
-  older version of the code) is met within the reference's own agreement;
+* the reference's own example (examples/JupiterEnergyTest, 34,560 steps) gives
+  the reference's ENERGY lines and last frame, and its known-answer file
+  (enou.txt, from an older version of the code) is met within the reference's
+  own agreement;
 * the FP32 form runs a case file within tolerance of the FP64 step.
 """
+import hashlib
 import os
 import subprocess
 
@@ -45,7 +48,11 @@ def same_energy(a, b, rel=1.5e-6):
     return va[0] == vb[0] and all(abs(x - y) <= rel * abs(y) for x, y in zip(va[1:], vb[1:]))
 
 
-@pytest.mark.parametrize("name", gc.forcing_cases())
+FULL = [n for n in gc.forcing_cases() if "last_frame" not in gc.manifest()[n]]
+HASHED = [n for n in gc.forcing_cases() if "last_frame" in gc.manifest()[n]]
+
+
+@pytest.mark.parametrize("name", FULL)
 def test_forcing_cases_match_the_reference(tmp_path, name):
     p = gc.forcing_params(name)
     formats.write_sw(str(tmp_path / f"{name}.sw"), p)
@@ -62,6 +69,21 @@ def test_forcing_cases_match_the_reference(tmp_path, name):
     assert len(energy) == len(printed)
     for a, b in zip(energy, printed):
         assert same_energy(a, b), (a, b)
+
+
+@pytest.mark.parametrize("name", HASHED)
+def test_reference_example_run(tmp_path, name):
+    """The reference's examples/JupiterEnergyTest case, all 34,560 steps:
+    every ENERGY line and the last frame must be the reference's."""
+    entry = gc.manifest()[name]
+    formats.write_sw(str(tmp_path / f"{name}.sw"), gc.forcing_params(name))
+    energy, frames = run(tmp_path, name)
+    assert energy == entry["energy_printed"]
+    assert len(frames) == entry["frames"]
+    nstep, t, nx, ny, fl = frames[max(frames)]
+    assert t == entry["last_frame"]["t"]
+    for k, h in entry["last_frame"]["sha256"].items():
+        assert hashlib.sha256(np.ascontiguousarray(fl[k]).tobytes()).hexdigest() == h, k
 
 
 @pytest.mark.parametrize("name", ["g01_minmod_nu4", "g11_wind_tracer", "g13_saturn_superbee"])
