@@ -914,8 +914,10 @@ void halo_wrap(double* x, int nx, int ny, cudaStream_t st) {
 }
 
 // One reference time step; returns the number of kernels launched.
-int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
-              cudaStream_t st, Timers* tm, int parts) {
+namespace {
+
+// Launch bookkeeping shared by the two halves of a step: every tagged launch
+// is timed while the timers are on, and counted.
 #define LAUNCH(tag, ...)                          \
   do {                                            \
     if (tm && tm->on) tm->begin(tag, st);         \
@@ -923,6 +925,10 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     if (tm && tm->on) tm->end(st);                \
     nl++;                                         \
   } while (0)
+
+// Head of a step: core.c:134-290, through the velocity halos.
+int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
+              cudaStream_t st, Timers* tm) {
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   const int gw = (s.nx + 127) / 128;
   const size_t bytes = sizeof(double) * (size_t)s.W * s.H;
@@ -930,7 +936,6 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
   const bool hyper = (s.nu2 != 0 || s.nu4 != 0 || s.nu6 != 0);
 
-  if (parts & STEP_HEAD) {
   // compute_Dt (core.c:155-159): maxima at the start of the step
   LAUNCH("cfl", k_cfl<<<g, TX, 0, st>>>(s, F(), chk.cfl + 2 * slot));
 
@@ -1002,11 +1007,18 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   // halos (core.c:287-290)
   LAUNCH("halo", halo_wrap(b.f[1], s.nx, s.ny, st));
   LAUNCH("halo", halo_wrap(b.f[2], s.nx, s.ny, st));
-  }
-  if (!(parts & STEP_TAIL)) return nl;
-  // here the reference adds its time-dependent forcing (core.c:292-294);
-  // the halo refresh of tracer and eta that follows it (core.c:296-300) is
-  // done by the forcing calls themselves, so the tail is the walls and checks
+  return nl;
+}
+
+// Tail of a step: the reference adds its time-dependent forcing before it
+// (core.c:292-294); the halo refresh of tracer and eta that follows the
+// forcing (core.c:296-300) is done by the forcing calls themselves, so the
+// tail is do_channel and the range checks (core.c:303-312).
+int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, int slot, cudaStream_t st,
+              Timers* tm) {
+  const dim3 g((s.nx + TX - 1) / TX, s.ny);
+  const int gw = (s.nx + 127) / 128;
+  int nl = 0;
   LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
 
   // range checks of tracer, eta, u, v (core.c:309-312)
@@ -1016,10 +1028,60 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, b.f[order[q]], chk.bad + slot));
   }
   return nl;
+}
 #undef LAUNCH
+
+}  // namespace
+
+int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
+              cudaStream_t st, Timers* tm, int parts) {
+  int nl = 0;
+  if (parts & STEP_HEAD) nl += step_head(s, b, sch, k, tracer, chk, slot, st, tm);
+  if (parts & STEP_TAIL) nl += step_tail(s, b, tracer, chk, slot, st, tm);
+  return nl;
 }
 
-// Energy per interior row (energy.c:36-41), compensated (Neumaier) over i.
+// Compensated sums: each thread accumulates with Neumaier's method, then the
+// (sum, error) pairs are combined along a tree with Knuth's TwoSum, so the
+// result carries the rounding errors of every addition.
+struct Pair {
+  double hi, lo;
+};
+__device__ __forceinline__ Pair two_sum_add(Pair a, Pair b) {
+  const double s = a.hi + b.hi;
+  const double bb = s - a.hi;
+  const double err = (a.hi - (s - bb)) + (b.hi - bb);
+  return Pair{s, (a.lo + b.lo) + err};
+}
+__device__ __forceinline__ void neumaier(double& acc, double& cmp, double term) {
+  const double t = acc + term;
+  cmp += (fabs(acc) >= fabs(term)) ? ((acc - t) + term) : ((term - t) + acc);
+  acc = t;
+}
+// Block-wide combine of three pairs per thread (blockDim a multiple of 32, <= 1024);
+// thread 0 receives the totals.
+__device__ __forceinline__ void block_combine3(Pair v[3]) {
+  __shared__ double sh[3][2][32];
+  for (int o = 16; o > 0; o >>= 1)
+    for (int c = 0; c < 3; c++) {
+      const Pair w{__shfl_down_sync(0xffffffffu, v[c].hi, o), __shfl_down_sync(0xffffffffu, v[c].lo, o)};
+      v[c] = two_sum_add(v[c], w);
+    }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (lane == 0)
+    for (int c = 0; c < 3; c++) { sh[c][0][warp] = v[c].hi; sh[c][1][warp] = v[c].lo; }
+  __syncthreads();
+  if (warp == 0) {
+    for (int c = 0; c < 3; c++) v[c] = (lane < nw) ? Pair{sh[c][0][lane], sh[c][1][lane]} : Pair{0.0, 0.0};
+    for (int o = 16; o > 0; o >>= 1)
+      for (int c = 0; c < 3; c++) {
+        const Pair w{__shfl_down_sync(0xffffffffu, v[c].hi, o), __shfl_down_sync(0xffffffffu, v[c].lo, o)};
+        v[c] = two_sum_add(v[c], w);
+      }
+  }
+}
+
+// Energy per interior row (energy.c:36-41), compensated over i.
 __global__ void k_energy_rows(DevState s, F7 f, double* out) {
   const int W = s.W;
   const int j = blockIdx.x + 1;
@@ -1038,40 +1100,22 @@ __global__ void k_energy_rows(DevState s, F7 f, double* out) {
 #undef UW
 #undef VW
 #undef HH
-    for (int c = 0; c < 3; c++) {
-      const double t = acc[c] + term[c];
-      cmp[c] += (fabs(acc[c]) >= fabs(term[c])) ? ((acc[c] - t) + term[c]) : ((term[c] - t) + acc[c]);
-      acc[c] = t;
-    }
+    for (int c = 0; c < 3; c++) neumaier(acc[c], cmp[c], term[c]);
   }
-  __shared__ double sh[3][2][256];
-  for (int c = 0; c < 3; c++) { sh[c][0][threadIdx.x] = acc[c]; sh[c][1][threadIdx.x] = cmp[c]; }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    const int c = threadIdx.x;
-    double a = 0, e = 0;
-    for (int t = 0; t < (int)blockDim.x; t++) {
-      const double term = sh[c][0][t];
-      const double u = a + term;
-      e += (fabs(a) >= fabs(term)) ? ((a - u) + term) : ((term - u) + a);
-      a = u;
-      e += sh[c][1][t];
-    }
-    out[3 * (j - 1) + c] = a + e;
-  }
+  Pair v[3] = {{acc[0], cmp[0]}, {acc[1], cmp[1]}, {acc[2], cmp[2]}};
+  block_combine3(v);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; c++) out[3 * (j - 1) + c] = v[c].hi + v[c].lo;
 }
 
 __global__ void k_energy_sum(const double* rows, int ny, double* out) {
-  const int c = threadIdx.x;
-  if (c >= 3) return;
-  double a = 0, e = 0;
-  for (int j = 0; j < ny; j++) {
-    const double term = rows[3 * j + c];
-    const double u = a + term;
-    e += (fabs(a) >= fabs(term)) ? ((a - u) + term) : ((term - u) + a);
-    a = u;
-  }
-  out[c] = a + e;
+  double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+  for (int j = threadIdx.x; j < ny; j += blockDim.x)
+    for (int c = 0; c < 3; c++) neumaier(acc[c], cmp[c], rows[3 * j + c]);
+  Pair v[3] = {{acc[0], cmp[0]}, {acc[1], cmp[1]}, {acc[2], cmp[2]}};
+  block_combine3(v);
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; c++) out[c] = v[c].hi + v[c].lo;
 }
 
 void energy_rows(const DevState& s, const double* const* f, double* row_out, cudaStream_t st) {
@@ -1079,7 +1123,7 @@ void energy_rows(const DevState& s, const double* const* f, double* row_out, cud
 }
 
 void energy_sum(const double* row_in, int ny, double* out3, cudaStream_t st) {
-  k_energy_sum<<<1, 32, 0, st>>>(row_in, ny, out3);
+  k_energy_sum<<<1, 1024, 0, st>>>(row_in, ny, out3);
 }
 
 }  // namespace sw2g
