@@ -242,10 +242,19 @@ def make_case(nx, ny, *, planet="jupiter", jet="cos6", sch=2, nsteps=500, seed=1
     sl, cl = np.sin(jc)[:, None], np.cos(jc)[:, None]
     for b in blist:
         l0, p0 = deg2rad(b.lon), deg2rad(b.lat)
-        # window in latitude: beyond 6 sigma the bump is below 1.5e-8 of its amplitude
-        cosang = np.sin(p0) * sl + np.cos(p0) * cl * np.cos(lonc[None, :] - l0)
-        r = a * np.arccos(np.clip(cosang, -1.0, 1.0))
-        H = H + b.amp * np.exp(-(r * r) / (2.0 * b.sigma * b.sigma))
+        # exp(-x) is exactly 0.0 for x > 746, so beyond rc = sqrt(2*746) sigma
+        # (with a margin for rounding) the bump adds exactly 0: only the rows
+        # and cells that can be reached are evaluated, with the same result
+        rc = np.sqrt(2.0 * 746.0) * b.sigma * 1.001
+        rows_in = np.nonzero(np.abs(jc - p0) * a <= rc)[0]
+        if rows_in.size == 0:
+            continue
+        j0, j1 = rows_in[0], rows_in[-1] + 1
+        cosang = np.sin(p0) * sl[j0:j1] + np.cos(p0) * cl[j0:j1] * np.cos(lonc[None, :] - l0)
+        near = cosang >= np.cos(min(rc / a, np.pi))
+        r = a * np.arccos(np.clip(cosang[near], -1.0, 1.0))
+        block = H[j0:j1]
+        block[near] = block[near] + b.amp * np.exp(-(r * r) / (2.0 * b.sigma * b.sigma))
     if np.min(H) <= 0:
         raise ValueError("non-positive layer depth in synthetic case")
 
