@@ -51,9 +51,9 @@ typedef enum {
 #define SW2G_FLAG_SIGMA 0x4u   /* tau holds sigma_dis (0 = no damping), as the sw struct holds it (init.c:110-114) */
 
 /* The parsed case, as the reference's initialize() stores it in the sw struct
- * (init.c:48-161). Angles are in degrees, as in the .sw file. Polar 0 only. */
+ * (init.c:48-161). Angles are in degrees, as in the .sw file. */
 typedef struct {
-  int nx, ny;                    /* interior cells; each >= 3 (sppde_core.c:431-459) */
+  int nx, ny;                    /* interior cells; each >= 3 (sppde_core.c:431-459); nx = ny = n when polar */
   int sch;                       /* limiter 0..9 (calc.c:262-273) */
   double lon0, lon1, lat0, lat1; /* degrees (radians with SW2G_FLAG_RADIANS) */
   double Omega, rE, rP, gE, depth;
@@ -64,6 +64,14 @@ typedef struct {
   double tracer_dis;             /* TracerDis */
   double hypernu[3];             /* Hypernu as entered: nu2, nu4 (positive), nu6 */
   unsigned flags;                /* SW2G_FLAG_* */
+  /* Polar caps (init.c:66-79, 154-162, 243-277): polar = 1 (north) or -1
+   * (south) runs the square lon0..lon1 x lat0..lat1 = -angleSim..angleSim
+   * around the pole on the sphere of radius rE^2/rP, with gravity and
+   * Coriolis from each point's angular distance to the pole and a sponge of
+   * rate sigma_sponge beyond beta_sponge from it (degrees, radians with
+   * SW2G_FLAG_RADIANS); no walls. FP64 contexts only. polar = 0: the band. */
+  int polar;
+  double beta_sponge, sigma_sponge;
 } sw2g_case;
 
 typedef struct sw2g_ctx sw2g_ctx;
@@ -229,6 +237,9 @@ sw2g_status sw2g_selfcheck_division(const double *divisors, int n, long long sam
  * padded layout; windx, windy and hB may be NULL (read as zero). out3 is a
  * device pointer to three doubles (ke, ape, mass). Work is queued on `stream`
  * (a cudaStream_t; NULL is the default stream); out3 is valid once it is done.
+ *
+ * Band cases only (a polar cap gives SW2G_ERR_BAD_ARG: its gravity is a 2-D
+ * field; sw2g_diag covers caps).
  *
  * Limits and sharing: ny must not exceed SW2G_NOALLOC_MAX_ROWS (otherwise
  * SW2G_ERR_BAD_ARG and a message on stderr). The scratch is one fixed 320 KiB

@@ -287,6 +287,72 @@ def make_case(nx, ny, *, planet="jupiter", jet="cos6", sch=2, nsteps=500, seed=1
     return Case(p, eta, u, v, tr, wx, wy, hB, blist, seed)
 
 
+def channel_walls(wx, wy, nx, ny):
+    """do_channel's changes to the winds of a band (calc.c:600-649), which the
+    reference applies before its time loop (core.c:101); on a polar cap its
+    wall loops run over no cells (sppde_core.c:589)."""
+    I = slice(2, nx + 2)
+    wy[1, I] = 0.0
+    wy[0, I] = 0.0
+    wx[1, I] = wx[2, I]
+    wx[0, I] = wx[1, I]
+    wy[ny + 1, I] = 0.0
+    wy[ny + 2, I] = 0.0
+    wy[ny + 3, I] = 0.0
+    wx[ny + 2, I] = wx[ny + 1, I]
+    wx[ny + 3, I] = wx[ny + 2, I]
+
+
+def make_polar_case(n, polar, *, angle_sim=20.0, planet="jupiter", sch=2, nsteps=60, seed=1, h0=2.5e4,
+                    amp=0.05, sigma_km=2500.0, beta_sp=15.0, sig_sp=1e-5, wind=None, hyper=True, tracer=False,
+                    cfl=0.25, Tau=1e20, TracerDis=0.0) -> Case:
+    """A polar cap (polar = 1 north, -1 south): the square -angle_sim..angle_sim
+    degrees around the pole, n x n cells, at rest with a seeded Gaussian
+    height bump; winds from the table (turned around the pole, damped in the
+    sponge beyond beta_sp degrees) as the reference's reader builds them,
+    computed by the C restatement (sw2_gb300.hostlib). Dt from CFL `cfl` on
+    the gravity-wave speed plus the largest wind."""
+    import os
+    import tempfile
+
+    from . import formats, hostlib
+
+    pl = PLANETS[planet]
+    p = CaseParams(nx=n, ny=n, sch=sch, nsteps=nsteps, depth=h0, Tau=Tau, TracerDis=TracerDis, wind=wind, **pl)
+    p.polar, p.angleSim, p.BetaSp, p.SigSp = polar, angle_sim, beta_sp, sig_sp
+    p.lon0 = p.lat0 = -angle_sim
+    p.lon1 = p.lat1 = angle_sim
+    rng = SplitMix64(seed)
+    b = Bump(rng.uniform(-angle_sim / 2, angle_sim / 2), rng.uniform(-angle_sim / 2, angle_sim / 2), amp * h0,
+             sigma_km * 1e3)
+    d = deg2rad(2.0 * angle_sim) / n
+    lc = np.array([deg2rad(-angle_sim) + (k - 0.5) * d for k in range(1, n + 1)])
+    R = pl["rE"] * pl["rE"] / pl["rP"]
+    cosang = (np.sin(deg2rad(b.lat)) * np.sin(lc)[:, None] +
+              np.cos(deg2rad(b.lat)) * np.cos(lc)[:, None] * np.cos(lc[None, :] - deg2rad(b.lon)))
+    r = R * np.arccos(np.clip(cosang, -1.0, 1.0))
+    eta = np.zeros((n + 4, n + 4))
+    eta[2:-2, 2:-2] = b.amp * np.exp(-(r * r) / (2.0 * b.sigma * b.sigma))
+    u, v, tr = np.zeros_like(eta), np.zeros_like(eta), np.zeros_like(eta)
+    if tracer:
+        tr[2:-2, 2:-2] = np.exp(-(r * r) / (2.0 * (3 * b.sigma) ** 2))
+    for x in (eta, u, v, tr):
+        halo_wrap(x)
+    p.Dt = 100.0
+    with tempfile.TemporaryDirectory() as wd:
+        path = os.path.join(wd, "c.sw")
+        formats.write_sw(path, p)
+        wx, wy = hostlib.Case(path).winds(beta_sp)
+    g = float(pl["gE"]) * 1.2
+    dx = R * d * np.cos(deg2rad(angle_sim) * 1.5)
+    c = np.sqrt(g * h0 * (1 + amp)) + float(np.max(np.abs(wx)) + np.max(np.abs(wy)))
+    p.Dt = float(cfl * dx / (2 * c))
+    if hyper:
+        nu4 = 1.0 / (10.0 * p.Dt * (8.0 / dx ** 2) ** 2)
+        p.hypernu = (0.0, nu4, 0.0)
+    return Case(p, eta, u, v, tr, wx, wy, np.zeros_like(eta), [b], seed)
+
+
 def config_case(name: str, seed: int = 1, **over) -> Case:
     """The benchmark configurations by name (sizes, physics and step counts)."""
     if name == "band256":      # plain FP64, CPU-runnable

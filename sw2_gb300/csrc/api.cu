@@ -200,6 +200,11 @@ bool case_ok(const sw2g_case* c) {
   // init.c:122: hyperviscosity coefficients are entered as non-negative
   if (c->hypernu[0] < 0 || c->hypernu[1] < 0 || c->hypernu[2] < 0) return false;
   if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA)) return false;
+  if (c->polar != 0) {  // the square around the pole (init.c:66-79)
+    if ((c->polar != 1 && c->polar != -1) || c->nx != c->ny) return false;
+    if (!(c->lon1 > 0) || c->lon0 != -c->lon1 || c->lat0 != c->lon0 || c->lat1 != c->lon1) return false;
+    if (!(c->sigma_sponge >= 0)) return false;
+  }
   if ((c->flags & SW2G_FLAG_SIGMA) && !(c->tau >= 0)) return false;
   return true;
 }
@@ -463,7 +468,7 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   *out = nullptr;
   if (!case_ok(c) || (precision != SW2G_FP64 && precision != SW2G_FP32)) return SW2G_ERR_BAD_ARG;
   // the FP32 form covers nabla^2 and nabla^4 hyperviscosity (the configurations' operators)
-  if (precision == SW2G_FP32 && c->hypernu[2] != 0) return SW2G_ERR_BAD_ARG;
+  if (precision == SW2G_FP32 && (c->hypernu[2] != 0 || c->polar != 0)) return SW2G_ERR_BAD_ARG;
   sw2g_ctx* x = new (std::nothrow) sw2g_ctx();
   if (!x) return SW2G_ERR_NOMEM;
   x->c = *c;
@@ -501,6 +506,19 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
                                       cudaMemcpyHostToDevice, x->stream), "rows")) != SW2G_OK)
     return fail(st);
   s.rows = x->d_rows;
+  s.polar = c->polar;
+  s.pf = nullptr;
+  if (c->polar != 0) {  // gravity, Coriolis and sponge fields of the cap
+    std::vector<double> pf;
+    polar_fields(*c, pf, &x->rest_mx, &x->rest_my);
+    double* d_pf = nullptr;
+    if ((st = dalloc(x, &d_pf, pf.size())) != SW2G_OK) return fail(st);
+    if ((st = cuda_fail(cudaMemcpyAsync(d_pf, pf.data(), pf.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                        x->stream), "polar fields")) != SW2G_OK)
+      return fail(st);
+    if ((st = cuda_fail(cudaStreamSynchronize(x->stream), "polar fields")) != SW2G_OK) return fail(st);
+    s.pf = d_pf;
+  }
   if (precision == SW2G_FP64) {
     Fp64Buffers& b = x->b;
     double** all[] = {&b.f[0], &b.f[1], &b.f[2], &b.f[3], &b.f[4], &b.f[5], &b.f[6],
@@ -855,6 +873,7 @@ sw2g_status sw2g_set_field_where(sw2g_ctx* x, int which, const double* value, co
 sw2g_status sw2g_apply_channel(sw2g_ctx* x) {
   sw2g_status st = force_ready(x, 0);
   if (st != SW2G_OK) return st;
+  if (x->s.polar != 0) return SW2G_OK;  // periodic in y: the wall loops run over no cells (sppde_core.c:589)
   fp64_channel(x->b.f[1], x->b.f[2], x->b.f[4], x->b.f[5], x->s.nx, x->s.ny, x->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(x->stream));

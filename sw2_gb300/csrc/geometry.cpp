@@ -46,6 +46,14 @@ double angle(const sw2g_case& c, double a) { return (c.flags & SW2G_FLAG_RADIANS
 void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, double* rest_my) {
   const int ny = c.ny, H = c.ny + 4;
   Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};  // init.c:150
+  if (c.polar != 0) {
+    // init_polar_region (init.c:273-276) turns the spheroid into the sphere of
+    // radius rE^2/rP after the gravity and Coriolis fields; epsilon2 keeps its
+    // value, so the metric factors below use the new radius with the old ratio
+    const double r = (c.rE) * (c.rE) / (c.rP);
+    p.rE = r;
+    p.rP = r;
+  }
   const double lon0 = angle(c, c.lon0), lon1 = angle(c, c.lon1);
   const double lat0 = angle(c, c.lat0), lat1 = angle(c, c.lat1);
   const double dlon = (lon1 - lon0) / ((double)c.nx);                    // coords.c:36
@@ -104,6 +112,70 @@ void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, 
     double cx = std::sqrt((c.depth) * (R(R_GE, j))), cy = std::sqrt((c.depth) * (R(R_GN, j)));
     if (std::fabs(cx / R(R_DXE, j)) > mx) mx = std::fabs(cx) / R(R_DXE, j);
     if (std::fabs(cy / R(R_DYN, j)) > my) my = std::fabs(cy) / R(R_DYN, j);
+  }
+  *rest_mx = mx;
+  *rest_my = my;
+}
+
+namespace {
+double great_angle(double lon0, double lat0, double lon1, double lat1) {  // tools.c:122-136
+  return std::acos(std::sin(lat0) * std::sin(lat1) + std::cos(lat0) * std::cos(lat1) * std::cos(lon1 - lon0));
+}
+}  // namespace
+
+void polar_fields(const sw2g_case& c, std::vector<double>& f, double* rest_mx, double* rest_my) {
+  const int nx = c.nx, ny = c.ny, W = nx + 4, Hh = ny + 4;
+  const size_t S = (size_t)W * Hh;
+  f.assign((size_t)P_NUM * S, 0.0);
+  // init_polar_region runs on the spheroid as read (init.c:243-271)
+  const Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};
+  const double lon0 = angle(c, c.lon0), lon1 = angle(c, c.lon1);
+  const double lat0 = angle(c, c.lat0), lat1 = angle(c, c.lat1);
+  const double beta = angle(c, c.beta_sponge);
+  const double mlon = ((lon0) + (lon1)) / 2.0, mlat = ((lat0) + (lat1)) / 2.0;  // MEAN, sw.h:110
+  const double pi = ref_pi(), ns = (double)c.polar;
+  const double tau_sponge = -std::log(0.01) / (std::sqrt(2.0) * lat1 - beta);  // init.c:157
+  const double sigma_dis = (c.flags & SW2G_FLAG_SIGMA) ? c.tau : (c.tau > 1e10 ? 0 : 1.0 / c.tau);
+  auto lone = [&](int i) { return linspace_val(i, lon0, lon1, nx); };       // sw.h:113
+  auto lonc = [&](int i) { return (lone(i) + lone(i - 1)) / 2.; };          // sw.h:114
+  auto latn = [&](int j) { return linspace_val(j, lat0, lat1, ny); };       // sw.h:116
+  auto latc = [&](int j) { return (latn(j) + latn(j - 1)) / 2.; };          // sw.h:117
+  auto polar_lat = [&](double lon, double lat) {                            // sw.h:130-132
+    return (ns) * (pi / 2.0 - great_angle(lon, lat, mlon, mlat));
+  };
+  auto sponge = [&](double lon, double lat, double outside) {               // calc.c:102-111, 378-392
+    const double dist = great_angle(mlon, mlat, lon, lat) - beta;
+    return (dist > 0) ? c.sigma_sponge * (1.0 - std::exp(-tau_sponge * (dist))) : outside;
+  };
+  auto F = [&](int t, int i, int j) -> double& { return f[(size_t)t * S + (i + 1) + (size_t)(j + 1) * W]; };
+  for (int j = -1; j <= ny + 2; j++)
+    for (int i = -1; i <= nx + 2; i++) {
+      const double le = polar_lat(lone(i), latc(j)), ln = polar_lat(lonc(i), latn(j));
+      const double lc = polar_lat(lonc(i), latc(j));
+      F(P_GE, i, j) = g_eff(p, lat2pclat(p, le));                           // init.c:253-261
+      F(P_GN, i, j) = g_eff(p, lat2pclat(p, ln));
+      F(P_GC, i, j) = g_eff(p, lat2pclat(p, lc));
+      F(P_FE, i, j) = fcor(p, le);
+      F(P_FN, i, j) = fcor(p, ln);
+      F(P_SH, i, j) = sponge(lonc(i), latc(j), sigma_dis);
+      F(P_STR, i, j) = sponge(lonc(i), latc(j), c.tracer_dis);
+      F(P_SU, i, j) = sponge(lone(i), latc(j), sigma_dis);
+      F(P_SV, i, j) = sponge(lonc(i), latn(j), sigma_dis);
+    }
+  // compute_Dt for a flow at rest (calc.c:715-725) with these gravity fields
+  // and the metric factors of the sphere
+  std::vector<double> rows;
+  double mx0 = 0, my0 = 0;
+  build_rows(c, rows, &mx0, &my0);
+  const int H = ny + 4;
+  double mx = 0, my = 0;
+  for (int j = 1; j <= ny; j++) {
+    const double dxe = rows[(size_t)R_DXE * H + j + 1], dyn = rows[(size_t)R_DYN * H + j + 1];
+    for (int i = 1; i <= nx; i++) {
+      const double cx = std::sqrt((c.depth) * (F(P_GE, i, j))), cy = std::sqrt((c.depth) * (F(P_GN, i, j)));
+      if (std::fabs(cx / dxe) > mx) mx = std::fabs(cx) / dxe;
+      if (std::fabs(cy / dyn) > my) my = std::fabs(cy) / dyn;
+    }
   }
   *rest_mx = mx;
   *rest_my = my;

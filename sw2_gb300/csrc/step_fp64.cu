@@ -16,6 +16,8 @@ constexpr int TX = 128;
 
 __device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
 __device__ __forceinline__ double RW(const DevState& s, int t, int j) { return s.rows[t * s.H + j + 1]; }
+// A field of a polar cap at padded index q.
+__device__ __forceinline__ double PF(const DevState& s, int t, int q) { return s.pf[(size_t)t * s.W * s.H + q]; }
 
 __device__ __forceinline__ int dexp(double x) {
   return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffULL);
@@ -116,7 +118,8 @@ __device__ __forceinline__ double mass_cell(const DevState& s, const F7& f, int 
   const double a = UW(i - 1, j), b = UW(i, j), c = VW(i, j - 1), d = VW(i, j);
   double acc = tvd_sum<SCH>(qx, qy, cpos(a, Dt, dxe), cneg(a, Dt, dxe), cpos(b, Dt, dxe), cneg(b, Dt, dxe),
                             cpos(c, Dt, dyn), cneg(c, Dt, dyn), cpos(d, Dt, dyn), cneg(d, Dt, dyn));
-  acc -= 2.0 * Dt * (s.sigma) * f.eta[IX(W, i, j)];
+  const double sigma = s.polar ? PF(s, P_SH, IX(W, i, j)) : s.sigma;  // the sponge, calc.c:102-111
+  acc -= 2.0 * Dt * (sigma) * f.eta[IX(W, i, j)];
   return acc;
 }
 
@@ -141,7 +144,8 @@ __global__ void k_tracer(DevState s, F7 f, double* out) {
   double pv2 = Dt * t * (b - a) / dxe;
   pv2 += Dt * t * (d - c) / dyn;
   double acc = pv1 + pv2;
-  acc -= 2.0 * Dt * (s.sigma_tr) * t;
+  const double sigma = s.polar ? PF(s, P_STR, IX(W, i, j)) : s.sigma_tr;  // calc.c:152-161
+  acc -= 2.0 * Dt * (sigma) * t;
   out[IX(W, i, j)] = acc;
 }
 
@@ -409,7 +413,7 @@ __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, dou
     if (own) {
       double r;
       if (slow) r = mass_cell_ool<SCH>(s, f, i, j);
-      else r = S - damp * f.eta[IX(W, i, j)];
+      else r = S - (s.polar ? 2.0 * Dt * PF(s, P_SH, IX(W, i, j)) : damp) * f.eta[IX(W, i, j)];
       out[IX(W, i, j)] = r;
     }
     tsP = nsP;
@@ -664,13 +668,15 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double* e = f.eta;
-  const double dup = div_rcp(RW(s, R_MGEDT, j) * (e[IX(W, i + 1, j)] - e[q]), RW(s, R_DXC, j), RW(s, R_IDXC, j));
-  const double dvp =
-      div_rcp(RW(s, R_MGNDT, j) * (e[IX(W, i, j + 1)] - e[q]), RW(s, R_DYC, j + 1), RW(s, R_IDYC, j + 1));
+  const double mge = s.polar ? -PF(s, P_GE, q) * s.Dt : RW(s, R_MGEDT, j);  // -GE*Dt, calc.c:517
+  const double mgn = s.polar ? -PF(s, P_GN, q) * s.Dt : RW(s, R_MGNDT, j);
+  const double dup = div_rcp(mge * (e[IX(W, i + 1, j)] - e[q]), RW(s, R_DXC, j), RW(s, R_IDXC, j));
+  const double dvp = div_rcp(mgn * (e[IX(W, i, j + 1)] - e[q]), RW(s, R_DYC, j + 1), RW(s, R_IDYC, j + 1));
   double a = duadv[q] + dup;
   double b = dvadv[q] + dvp;
-  a -= f.u[q] * s.sigma * s.Dt;
-  b -= f.v[q] * s.sigma * s.Dt;
+  const double su = s.polar ? PF(s, P_SU, q) : s.sigma, sv = s.polar ? PF(s, P_SV, q) : s.sigma;  // calc.c:374-394
+  a -= f.u[q] * su * s.Dt;
+  b -= f.v[q] * sv * s.Dt;
   dun[q] = a;
   dvn[q] = b;
 }
@@ -722,7 +728,8 @@ __global__ void k_coriolis_u(DevState s, double* u, const double* v, const doubl
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
-  const double al = RW(s, R_DTFE, j) + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
+  const double dtf = s.polar ? s.Dt * PF(s, P_FE, q) : RW(s, R_DTFE, j);  // Dt*FE, calc.c:563
+  const double al = dtf + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
   const double be = 0.25 * al * al;
   u[q] = (u[q] + duab[q] - be * u[q] + al * semi) / (1.0 + be);
 }
@@ -732,7 +739,8 @@ __global__ void k_coriolis_v(DevState s, const double* u, double* v, const doubl
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
-  const double al = RW(s, R_DTFN, j) + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
+  const double dtf = s.polar ? s.Dt * PF(s, P_FN, q) : RW(s, R_DTFN, j);  // Dt*FN, calc.c:592
+  const double al = dtf + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
   const double be = 0.25 * al * al;
   v[q] = (v[q] + dvab[q] - be * v[q] - al * semi) / (1.0 + be);
 }
@@ -961,7 +969,8 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
       LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
       LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
       LAUNCH("halo", halo_wrap(b.Le[q], s.nx, s.ny, st));
-      LAUNCH("lape_fix", k_lape_fix<<<gw, 128, 0, st>>>(s.nx, s.ny, b.Le[q]));
+      // the wall rows of a band (laplacian.c:131-146); a polar cap is periodic in y and has none
+      if (s.polar == 0) LAUNCH("lape_fix", k_lape_fix<<<gw, 128, 0, st>>>(s.nx, s.ny, b.Le[q]));
     }
     LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
   }
@@ -986,11 +995,11 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
       LAUNCH("lapv_pass1", k_lapv_pass1<<<g, TX, 0, st>>>(s, uu, vv, b.ze, b.di));
       LAUNCH("halo", halo_wrap(b.ze, s.nx, s.ny, st));
       LAUNCH("halo", halo_wrap(b.di, s.nx, s.ny, st));
-      LAUNCH("lapv_fix1", k_lapv_fix1<<<gw, 128, 0, st>>>(s, uu, b.ze, b.di));
+      if (s.polar == 0) LAUNCH("lapv_fix1", k_lapv_fix1<<<gw, 128, 0, st>>>(s, uu, b.ze, b.di));
       LAUNCH("lapv_pass2", k_lapv_pass2<<<g, TX, 0, st>>>(s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
       LAUNCH("halo", halo_wrap(b.L[2 * q], s.nx, s.ny, st));
       LAUNCH("halo", halo_wrap(b.L[2 * q + 1], s.nx, s.ny, st));
-      LAUNCH("lapv_fix2", k_lapv_fix2<<<gw, 128, 0, st>>>(s.nx, s.ny, b.L[2 * q], b.L[2 * q + 1]));
+      if (s.polar == 0) LAUNCH("lapv_fix2", k_lapv_fix2<<<gw, 128, 0, st>>>(s.nx, s.ny, b.L[2 * q], b.L[2 * q + 1]));
     }
     LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.du[0], b.L[0], b.L[2], b.L[4]));
     LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.dv[0], b.L[1], b.L[3], b.L[5]));
@@ -1019,7 +1028,7 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   const int gw = (s.nx + 127) / 128;
   int nl = 0;
-  LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
+  if (s.polar == 0) LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
 
   // range checks of tracer, eta, u, v (core.c:309-312)
   const int order[4] = {3, 0, 1, 2};
@@ -1086,8 +1095,9 @@ __global__ void k_energy_rows(DevState s, F7 f, double* out) {
   const int W = s.W;
   const int j = blockIdx.x + 1;
   double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
-  const double surf = RW(s, R_SURF, j), gc = RW(s, R_GC, j), depth = s.depth;
+  const double surf = RW(s, R_SURF, j), gcrow = RW(s, R_GC, j), depth = s.depth;
   for (int i = threadIdx.x + 1; i <= s.nx; i += blockDim.x) {
+    const double gc = s.polar ? PF(s, P_GC, IX(W, i, j)) : gcrow;
 #define UW(i, j) (f.u[IX(W, i, j)] + f.wx[IX(W, i, j)])
 #define VW(i, j) (f.v[IX(W, i, j)] + f.wy[IX(W, i, j)])
 #define HH(i, j) (f.eta[IX(W, i, j)] + s.depth - f.hb[IX(W, i, j)])

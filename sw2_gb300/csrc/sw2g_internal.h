@@ -38,10 +38,18 @@ enum Row {
 // Internal limiter index: 0..9 as the reference, 10 = Van Leer made safe at r = -1.
 constexpr int kVanLeerSafe = 10;
 
+// Two-dimensional fields of a polar cap (padded, pitch W), index P_* * W*H:
+// gravity at E, N and C points, Coriolis at E and N points (init.c:243-261),
+// and the damping rates of h, tracer, u and v with the sponge
+// (calc.c:102-111, 152-161, 374-394).
+enum Polar { P_GE, P_GN, P_GC, P_FE, P_FN, P_SH, P_STR, P_SU, P_SV, P_NUM };
+
 struct DevState {
   int nx, ny, W, H;  // W = nx+4 (row pitch), H = ny+4
   const double* rows;  // R_NUM * H
   double depth, Dt, sigma, sigma_tr, nu2, nu4, nu6;
+  int polar;           // 0: band; +-1: polar cap, with the fields below
+  const double* pf;    // P_NUM * W * H (polar only)
 };
 
 struct Ctx;
@@ -49,6 +57,9 @@ struct Ctx;
 // Host geometry (geometry.cpp): fills rows[R_NUM*H]; returns the at-rest CFL
 // maxima used by compute_Dt when the flow is at rest (calc.c:715-725).
 void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, double* rest_my);
+// The fields of a polar cap (P_NUM x (nx+4)(ny+4)) and the at-rest CFL maxima
+// computed with them.
+void polar_fields(const sw2g_case& c, std::vector<double>& f, double* rest_mx, double* rest_my);
 
 // FP64 reference-exact step (step_fp64.cu).
 struct Fp64Buffers {

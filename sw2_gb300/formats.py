@@ -51,6 +51,13 @@ class CaseParams:
     # lat, isdegvel, vel, Q, isdegsize, sigma, radius, inject_tracer)
     vortices: list = field(default_factory=list)
     gaussians: list = field(default_factory=list)
+    # polar caps (init.c:66-79, 154-162): polar = +-1 replaces lon0..lat1 by
+    # -angleSim..angleSim (degrees) and nx, ny by n; BetaSp (degrees) and SigSp
+    # set the sponge
+    polar: int = 0
+    angleSim: float = 0.0
+    BetaSp: float = 0.0
+    SigSp: float = 0.0
     extra: dict = field(default_factory=dict)
 
     @property
@@ -66,15 +73,14 @@ def _g(x: float) -> str:
 def write_sw(path: str, p: CaseParams) -> None:
     """Write a fully expanded `.sw` case (no m4 macros needed)."""
     nu = p.hypernu
+    if p.polar:
+        geo = [f"polar {p.polar}", f"angleSim {_g(p.angleSim)}", f"n {p.nx}"]
+    else:
+        geo = ["polar 0", f"lon0 {_g(p.lon0)}", f"lon1 {_g(p.lon1)}", f"lat0 {_g(p.lat0)}", f"lat1 {_g(p.lat1)}",
+               f"nx {p.nx}", f"ny {p.ny}"]
     lines = [
         f"sch {p.sch}",
-        "polar 0",
-        f"lon0 {_g(p.lon0)}",
-        f"lon1 {_g(p.lon1)}",
-        f"lat0 {_g(p.lat0)}",
-        f"lat1 {_g(p.lat1)}",
-        f"nx {p.nx}",
-        f"ny {p.ny}",
+        *geo,
         f"t0 {_g(p.t0)}",
         f"t1 {_g(p.t1)}",
         f"Dt {_g(p.Dt)}",
@@ -90,6 +96,7 @@ def write_sw(path: str, p: CaseParams) -> None:
         f"rP {_g(p.rP)}",
         f"gE {_g(p.gE)}",
         f"depth {_g(p.depth)}",
+        *([f"BetaSp {_g(p.BetaSp)}", f"SigSp {_g(p.SigSp)}"] if p.polar else []),
         "geoeq 0",
         str(len(p.vortices)), "7",
         *[" ".join(_g(x) for x in row) for row in p.vortices],

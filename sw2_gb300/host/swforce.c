@@ -275,3 +275,59 @@ int swforce_windx(const swcase *c, double *windx, char *err, size_t errlen) {
   swf_halo_wrap(windx, c->nx, c->ny);
   return 0;
 }
+
+static double great_angle(double lon0, double lat0, double lon1, double lat1) {  /* tools.c:122-136 */
+  return acos(sin(lat0) * sin(lat1) + cos(lat0) * cos(lat1) * cos(lon1 - lon0));
+}
+
+/* read_wind for a polar cap (io.c:207-240): the zonal wind of the table at
+ * each point's polar latitude, turned around the pole, and damped beyond the
+ * sponge; no halo update follows (init.c:232-235). */
+static void polar_winds(const swcase *c, double beta, double *windx, double *windy) {
+  const int n = c->wind_rows;
+  const double *x = c->wind, *y = c->wind + n;
+  const double mlon = ((c->lon0) + (c->lon1)) / 2.0, mlat = ((c->lat0) + (c->lat1)) / 2.0;
+  const double k = log(0.01) / (sqrt(2.0) * c->lat1 - beta);
+  for (int j = -1; j <= c->ny + 2; j++)
+    for (int i = -1; i <= c->nx + 2; i++) {
+      const double LONC = swf_lonc(c, i), LATC = swf_latc(c, j);
+      const double plat = (c->polar) * (PI_() / 2.0 - great_angle(LONC, LATC, mlon, mlat));  /* sw.h:130 */
+      const size_t q = IXP(c->nx, i, j);
+      if (rad2deg(plat) < x[0] || rad2deg(plat) > x[n - 1]) {
+        windx[q] = 0;
+        windy[q] = 0;
+        continue;
+      }
+      double ang = acos((LATC - mlat) / sqrt(sq(LATC - mlat) + sq(LONC - mlon)));
+      if (!((LONC - mlon) >= 0)) ang = -ang;
+      const double w = linterp(rad2deg(plat), x, y, n);
+      if (c->polar == 1) {
+        windx[q] = -cos(ang) * w;
+        windy[q] = sin(ang) * w;
+      } else {
+        windx[q] = cos(ang) * w;
+        windy[q] = -sin(ang) * w;
+      }
+      const double dist = fabs(great_angle(mlon, mlat, LONC, LATC)) - beta;
+      if (dist >= 0) {
+        windx[q] = windx[q] * exp(k * dist);
+        windy[q] = windy[q] * exp(k * dist);
+      }
+    }
+}
+
+int swforce_winds(const swcase *c, double beta_sponge_deg, double *windx, double *windy, char *err,
+                  size_t errlen) {
+  const int n = c->wind_rows;
+  if (n < 2) {
+    set_err(err, errlen, "wind table needs at least 2 rows");
+    return -1;
+  }
+  if (c->polar != 0) {
+    polar_winds(c, deg2rad(beta_sponge_deg), windx, windy);
+    return 0;
+  }
+  memset(windy, 0, (size_t)(c->nx + 4) * (c->ny + 4) * sizeof(double));
+  return swforce_windx(c, windx, err, errlen);
+}
+

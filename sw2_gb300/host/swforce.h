@@ -63,6 +63,13 @@ void swforce_vortex(const swcase *c, int k, swforce *w);
  * (init.c:232-235). Returns -1 if the table does not cover the rows. */
 int swforce_windx(const swcase *c, double *windx, char *err, size_t errlen);
 
+/* windx and windy of the case over all padded cells as read_wind leaves them:
+ * the band's zonal wind (swforce_windx, windy zero), or a polar cap's wind
+ * turned around the pole and damped beyond the sponge (io.c:207-240), whose
+ * BetaSp in degrees the case reader does not keep. */
+int swforce_winds(const swcase *c, double beta_sponge_deg, double *windx, double *windy, char *err,
+                  size_t errlen);
+
 /* Single-rank halo update of a padded field (sppde_hupdate.c:274-342). */
 void swf_halo_wrap(double *x, int nx, int ny);
 

@@ -57,6 +57,7 @@ def load():
                                        ctypes.POINTER(_D), ctypes.c_char_p, ctypes.c_size_t]
         L.swforce_vortex.argtypes = [ctypes.POINTER(SwCase), ctypes.c_int, ctypes.POINTER(SwForce)]
         L.swforce_windx.argtypes = [ctypes.POINTER(SwCase), _P, ctypes.c_char_p, ctypes.c_size_t]
+        L.swforce_winds.argtypes = [ctypes.POINTER(SwCase), _D, _P, _P, ctypes.c_char_p, ctypes.c_size_t]
         libc = ctypes.CDLL(None)
         libc.free.argtypes = [ctypes.c_void_p]
         L._free = libc.free
@@ -109,6 +110,17 @@ class Case:
         if load().swforce_windx(ctypes.byref(c), out.ctypes.data_as(_P), err, 512) != 0:
             raise ValueError(err.value.decode())
         return out
+
+    def winds(self, beta_sponge_deg: float = 0.0):
+        """(windx, windy) over all padded cells as read_wind leaves them (io.c:199-240)."""
+        c = self.c
+        wx = np.zeros((c.ny + 4, c.nx + 4))
+        wy = np.zeros_like(wx)
+        err = ctypes.create_string_buffer(512)
+        if load().swforce_winds(ctypes.byref(c), beta_sponge_deg, wx.ctypes.data_as(_P), wy.ctypes.data_as(_P),
+                                err, 512) != 0:
+            raise ValueError(err.value.decode())
+        return wx, wy
 
     def close(self):
         if getattr(self, "c", None) is not None:

@@ -42,7 +42,8 @@ class Case(ctypes.Structure):
                 ("gE", ctypes.c_double), ("depth", ctypes.c_double),
                 ("Dt", ctypes.c_double), ("courant", ctypes.c_double),
                 ("tau", ctypes.c_double), ("tracer_dis", ctypes.c_double),
-                ("hypernu", ctypes.c_double * 3), ("flags", ctypes.c_uint)]
+                ("hypernu", ctypes.c_double * 3), ("flags", ctypes.c_uint),
+                ("polar", ctypes.c_int), ("beta_sponge", ctypes.c_double), ("sigma_sponge", ctypes.c_double)]
 
 
 class SW2GError(RuntimeError):
@@ -114,11 +115,17 @@ def case_struct(p: CaseParams, flags: int = 0) -> Case:
     c = Case()
     c.nx, c.ny, c.sch = p.nx, p.ny, p.sch
     c.lon0, c.lon1, c.lat0, c.lat1 = p.lon0, p.lon1, p.lat0, p.lat1
+    if getattr(p, "polar", 0):  # init.c:66-74: the square -angleSim..angleSim around the pole
+        c.lon0 = c.lat0 = -p.angleSim
+        c.lon1 = c.lat1 = p.angleSim
     c.Omega, c.rE, c.rP, c.gE, c.depth = p.Omega, p.rE, p.rP, p.gE, p.depth
     c.Dt, c.courant, c.tau, c.tracer_dis = p.Dt, p.CFL, p.Tau, p.TracerDis
     for k in range(3):
         c.hypernu[k] = p.hypernu[k]
     c.flags = flags
+    c.polar = getattr(p, "polar", 0)
+    c.beta_sponge = getattr(p, "BetaSp", 0.0)
+    c.sigma_sponge = getattr(p, "SigSp", 0.0)
     return c
 
 

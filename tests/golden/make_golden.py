@@ -10,7 +10,7 @@ it prints. It then checks the C restatement in oracle/ against the same
 frames bit for bit (the oracle pin) before writing anything.
 
     python tests/golden/make_golden.py            # all cases
-    python tests/golden/make_golden.py --forcing  # the forcing cases only
+    python tests/golden/make_golden.py --forcing  # the forcing and polar cases only
 """
 from __future__ import annotations
 
@@ -123,6 +123,30 @@ FORCING_CASES = {
 HASH_ONLY = {"f05_jupiter_example"}
 
 
+def polar_wind_table(amp=30.0, k=6.0):
+    lat = np.arange(-90.0, 90.5, 1.0)
+    return np.stack([lat, amp * np.cos(np.deg2rad(k * lat))], axis=1)
+
+
+# Polar caps (polar = 1 north, -1 south): run from an initial frame like CASES,
+# checked against the reference's frames directly (the C restatement in
+# oracle/ covers the band only).
+POLAR_CASES = {
+    "p01_north_minmod_nu4": (dict(n=40, polar=1, sch=2, seed=41, beta_sp=15.0, sig_sp=1e-5), 60, 20),
+    "p02_south_superbee_tracer": (dict(n=32, polar=-1, angle_sim=15.0, sch=1, seed=42, beta_sp=10.0, sig_sp=3e-5,
+                                       tracer=True, TracerDis=2e-6, Tau=3e5), 60, 20),
+}
+
+
+def polar_case(name):
+    kw, nsteps, every = POLAR_CASES[name]
+    case = cases.make_polar_case(**kw, nsteps=nsteps, wind=polar_wind_table())
+    if name == "p02_south_superbee_tracer":
+        nu4 = case.params.hypernu[1]
+        case.params.hypernu = (2.0e-3 * nu4 ** 0.5, nu4, 1.0e-4 * nu4 ** 1.5)
+    return case
+
+
 def forcing_params(name):
     """CaseParams of a forcing case (also used by the tests to write the .sw)."""
     kw, nsteps, every, ite, add = FORCING_CASES[name]
@@ -224,7 +248,7 @@ def interior(a):
 def params_json(p):
     d = {k: getattr(p, k) for k in ("nx", "ny", "sch", "lon0", "lon1", "lat0", "lat1", "t0", "nsteps", "Dt",
                                     "CFL", "Tau", "IteInfo", "SaveEvery", "LoadFrom", "Omega", "rE", "rP",
-                                    "gE", "depth", "TracerDis")}
+                                    "gE", "depth", "TracerDis", "polar", "angleSim", "BetaSp", "SigSp")}
     d["hypernu"] = list(p.hypernu)
     d["wind"] = None if p.wind is None else p.wind.tolist()
     return d
@@ -262,11 +286,11 @@ def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
     if not os.path.exists(REF_BIN):
         raise SystemExit("reference not built (sources absent?)")
-    only_forcing = "--forcing" in sys.argv  # regenerate the forcing cases only
+    only_forcing = "--forcing" in sys.argv  # regenerate the forcing and polar cases only
     manifest = {}
     if only_forcing:
         with open(os.path.join(OUT, "manifest.json")) as fh:
-            manifest = {k: v for k, v in json.load(fh).items() if not v.get("forcing")}
+            manifest = {k: v for k, v in json.load(fh).items() if not v.get("forcing") and not v.get("polar")}
         CRASH_CASES.clear()
         CASES.clear()
         HASH_CASES.clear()
@@ -317,6 +341,21 @@ def main():
             entry["make_case"] = {k: v for k, v in kw.items()}
         manifest[name] = entry
         print(f"{name}: reference and oracle agree bit for bit over {nsteps} steps")
+    for name in POLAR_CASES:
+        kw, nsteps, every = POLAR_CASES[name]
+        case = polar_case(name)
+        with tempfile.TemporaryDirectory() as wd:
+            energy, ref_frames = run_reference(name, case, nsteps, every, wd)
+        assert len(ref_frames) == nsteps // every, (name, len(ref_frames))
+        arrs = {"init_" + k: interior(getattr(case, k)) for k in ("eta", "u", "v", "tracer")}
+        arrs["windx"], arrs["windy"] = case.windx, case.windy
+        for fi, (nstep, t, rf) in enumerate(ref_frames):
+            for k in ("eta", "u", "v", "tracer"):
+                arrs[f"f{fi}_{k}"] = interior(rf[k])
+        np.savez_compressed(os.path.join(OUT, name + ".npz"), **arrs)
+        manifest[name] = {"params": params_json(case.params), "nsteps": nsteps, "save_every": every,
+                          "energy_printed": energy, "polar": True}
+        print(f"{name}: {len(ref_frames)} reference frames (polar {case.params.polar})")
     for name in FORCING_CASES:
         p = forcing_params(name)
         with tempfile.TemporaryDirectory() as wd:

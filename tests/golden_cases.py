@@ -55,6 +55,11 @@ def array_cases():
     return sorted(n for n in manifest() if n.startswith("g"))
 
 
+def polar_cases():
+    """Polar caps run by the reference from an initial frame (no oracle pin)."""
+    return sorted(n for n, e in manifest().items() if e.get("polar"))
+
+
 def forcing_cases():
     """Cases run by the reference from its own initial state, with forcing."""
     return sorted(n for n, e in manifest().items() if e.get("forcing") and n.startswith("f"))

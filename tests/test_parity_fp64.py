@@ -53,6 +53,28 @@ def test_gpu_matches_reference_frames(name):
             assert np.array_equal(g, fr[k]), f"{k}: max|d|={np.max(np.abs(g - fr[k]))}"
 
 
+@pytest.mark.parametrize("name", gc.polar_cases())
+def test_gpu_polar_caps_match_reference_frames(name):
+    """Polar caps (2-D gravity, Coriolis and sponge fields, turned winds, no
+    walls) against the reference's own frames, bit for bit, and its ENERGY
+    lines to their printed digits."""
+    entry, case, frames = gc.load_case(name)
+    s = lib.Solver(case.params)
+    s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    energies = [s.diag()]
+    for fr in frames:
+        assert s.step(entry["save_every"]) == lib.OK
+        got = s.download()
+        for k in FIELDS:
+            g = got[k][2:-2, 2:-2]
+            assert np.array_equal(g, fr[k]), f"{k}: max|d|={np.max(np.abs(g - fr[k]))}"
+        energies.append(s.diag())
+    printed = entry["energy_printed"]
+    printed = [printed[0]] + printed[2:]
+    for (t, ke, ape, tot), (gke, gape, _m) in zip(printed, energies):
+        assert float(f"{gke:e}") == ke and float(f"{gape:e}") == ape
+
+
 @pytest.mark.parametrize("sch", range(10))
 def test_gpu_matches_oracle_all_cells(sch):
     flags = lib.FLAG_VANLEER_SAFE if sch == 3 else 0
