@@ -69,7 +69,8 @@ typedef struct {
    * around the pole on the sphere of radius rE^2/rP, with gravity and
    * Coriolis from each point's angular distance to the pole and a sponge of
    * rate sigma_sponge beyond beta_sponge from it (degrees, radians with
-   * SW2G_FLAG_RADIANS); no walls. FP64 contexts only. polar = 0: the band. */
+   * SW2G_FLAG_RADIANS); no walls. rE and rP are the case file's values.
+   * FP64 contexts only. polar = 0: the band. */
   int polar;
   double beta_sponge, sigma_sponge;
 } sw2g_case;
@@ -141,7 +142,8 @@ long long sw2g_steps_done(const sw2g_ctx *ctx);
  *   sw2g_set_field_where: field(i,j) = value(i,j) where mask(i,j) != 0 (perturbs.c:356-358)
  *   sw2g_apply_channel:   do_channel on u, v, windx and windy (calc.c:600-649), for
  *                         the forcing at t0, which the reference follows with it
- *                         (core.c:96-101).
+ *                         (core.c:96-101); nothing for a polar cap, which has no
+ *                         walls.
  * During a run, apply the forcing between sw2g_step_open and sw2g_step_close:
  * the reference's halo update copies wall-row values into the x halos before
  * its do_channel, so the order is part of the result. */

@@ -734,8 +734,8 @@ int swcase_read(const char *path, swcase *c, char *err, size_t errlen) {
   RD(get_double(&r, "gE", &c->gE));
   RD(get_double(&r, "depth", &c->depth));
   if (c->polar != 0) {
-    RD(get_double(&r, "BetaSp", &v));
-    RD(get_double(&r, "SigSp", &v));
+    RD(get_double(&r, "BetaSp", &c->beta_sponge));
+    RD(get_double(&r, "SigSp", &c->sigma_sponge));
   }
   RD(get_int(&r, "geoeq", &c->geoeq));
   if (c->geoeq != 0 && c->geoeq != 1) {

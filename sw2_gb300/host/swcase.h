@@ -9,8 +9,7 @@
  *      comments cut at '#', empty lines skipped, each <...> replaced by its
  *      value printed with "%.15e" ('\<' and '\>' are literal);
  *   3. tagged values and tables (sppde_parser.c:160-320).
- * Polar geometries (polar = +-1) and reference-field comparison (reftype 1)
- * are read but not run.
+ * Reference-field comparison (reftype 1) is read but not run.
  */
 #ifndef SWCASE_H
 #define SWCASE_H
@@ -46,6 +45,8 @@ typedef struct {
   double tracer_dis;
   int wind_rows;
   double *wind;           /* wind_rows latitudes (deg), then wind_rows values (transposed table) */
+  double beta_sponge;     /* BetaSp as entered (degrees), polar caps only */
+  double sigma_sponge;    /* SigSp, polar caps only */
 } swcase;
 
 /* Reads `path` (the .sw file; includes are resolved against its directory).

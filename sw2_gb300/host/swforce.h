@@ -65,8 +65,8 @@ int swforce_windx(const swcase *c, double *windx, char *err, size_t errlen);
 
 /* windx and windy of the case over all padded cells as read_wind leaves them:
  * the band's zonal wind (swforce_windx, windy zero), or a polar cap's wind
- * turned around the pole and damped beyond the sponge (io.c:207-240), whose
- * BetaSp in degrees the case reader does not keep. */
+ * turned around the pole and damped beyond the sponge (io.c:207-240);
+ * beta_sponge_deg is the case's BetaSp in degrees (c->beta_sponge). */
 int swforce_winds(const swcase *c, double beta_sponge_deg, double *windx, double *windy, char *err,
                   size_t errlen);
 

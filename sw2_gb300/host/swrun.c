@@ -17,6 +17,7 @@
  * (the reference checks after it); a flow-rate ramp that covers none of its
  * three phases injects nothing (the reference leaves the rate unset).
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -153,9 +154,9 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
   int rc = 1;
   sw2g_ctx *g = NULL;
   swforce w = {0};
-  double *f[5] = {NULL, NULL, NULL, NULL, NULL}, *windx = NULL, *zero = NULL;
-  if (c.polar != 0) {
-    fprintf(stderr, "sw2g-run: polar geometries are not supported\n");
+  double *f[5] = {NULL, NULL, NULL, NULL, NULL}, *windx = NULL, *windy = NULL, *zero = NULL;
+  if (c.polar != 0 && (c.num_gaussians || c.num_vortices)) {
+    fprintf(stderr, "sw2g-run: forcing on a polar cap is not supported\n");
     goto done;
   }
   if (c.reftype != 0 && !quiet) fprintf(stderr, "sw2g-run: reftype %d: the comparison is not run\n", c.reftype);
@@ -173,8 +174,9 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
     fprintf(stderr, "sw2g-run: out of host memory\n");
     goto done;
   }
-  if (swforce_windx(&c, windx, err, sizeof err)) {
-    fprintf(stderr, "sw2g-run: %s\n", err);
+  windy = (double *)calloc(S, sizeof(double));
+  if (!windy || swforce_winds(&c, c.beta_sponge, windx, windy, err, sizeof err)) {
+    fprintf(stderr, "sw2g-run: %s\n", err[0] ? err : "out of host memory");
     goto done;
   }
   sw2g_case sc;
@@ -199,9 +201,12 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
   sc.hypernu[1] = c.nu4;
   sc.hypernu[2] = c.nu6;
   sc.flags = SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | (fp32 ? SW2G_FLAG_VANLEER_SAFE : 0u);
+  sc.polar = c.polar;
+  sc.beta_sponge = c.beta_sponge * ((4.0 * atan(1.0)) / 180.0);  /* init.c:155, radians like the angles */
+  sc.sigma_sponge = c.sigma_sponge;
   if (ck(sw2g_create(&sc, fp32 ? SW2G_FP32 : SW2G_FP64, 0, &g), "create")) goto done;
   /* zero state, winds, zero bottom, all halos already wrapped (core.c:88-94) */
-  if (ck(sw2g_upload(g, zero, zero, zero, zero, windx, zero, zero, SW2G_UPLOAD_RAW), "upload")) goto done;
+  if (ck(sw2g_upload(g, zero, zero, zero, zero, windx, windy, zero, SW2G_UPLOAD_RAW), "upload")) goto done;
   const double Dt = c.Dt;
   double t = c.t0;
   /* forcing at t0 and the wall fixes (core.c:96-101) */
@@ -223,7 +228,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
     }
     nstart = ns;
     memcpy(w.perturbs, f[4], S * sizeof(double));
-    if (ck(sw2g_upload(g, f[0], f[1], f[2], f[3], windx, zero, zero, SW2G_UPLOAD_FRAME), "load")) goto done;
+    if (ck(sw2g_upload(g, f[0], f[1], f[2], f[3], windx, windy, zero, SW2G_UPLOAD_FRAME), "load")) goto done;
   } else {
     if (ck(sw2g_download(g, f[0], f[1], f[2], f[3]), "download")) goto done;
     memcpy(f[4], w.perturbs, S * sizeof(double));
@@ -288,6 +293,7 @@ done:
   swforce_free(&w);
   for (int k = 0; k < 5; k++) free(f[k]);
   free(windx);
+  free(windy);
   free(zero);
   swcase_free(&c);
   return rc;

@@ -29,7 +29,8 @@ class SwCase(ctypes.Structure):
                 ("num_vortices", ctypes.c_int), ("vortices", _P),
                 ("num_gaussians", ctypes.c_int), ("gaussians", _P),
                 ("tracer_dis", _D),
-                ("wind_rows", ctypes.c_int), ("wind", _P)]
+                ("wind_rows", ctypes.c_int), ("wind", _P),
+                ("beta_sponge", _D), ("sigma_sponge", _D)]
 
 
 class SwForce(ctypes.Structure):

@@ -73,6 +73,24 @@ def test_reader_reads_what_the_writer_wrote(tmp_path, name):
     assert np.array_equal(c.table("wind"), w)
 
 
+@pytest.mark.parametrize("name", gc.polar_cases())
+def test_reader_reads_polar_caps(tmp_path, name):
+    """A polar cap's file (init.c:66-74, 154-157): the square -angleSim..angleSim
+    around the pole, n cells a side, the sponge values, and the turned winds
+    the reference ran the cap with."""
+    entry, case, _ = gc.load_case(name)
+    p = case.params
+    path = tmp_path / "c.sw"
+    formats.write_sw(str(path), p)
+    c = hostlib.Case(str(path))
+    a = p.angleSim * ((4.0 * math.atan(1.0)) / 180.0)
+    assert (c.nx, c.ny, c.polar) == (p.nx, p.ny, p.polar) and p.nx == p.ny
+    assert (c.lon0, c.lon1, c.lat0, c.lat1) == (-a, a, -a, a)
+    assert (c.beta_sponge, c.sigma_sponge) == (p.BetaSp, p.SigSp)
+    wx, wy = c.winds(c.beta_sponge)
+    assert np.array_equal(wx, case.windx) and np.array_equal(wy, case.windy)
+
+
 def test_windx_matches_the_python_restatement(tmp_path):
     p = gc.params_of(gc.manifest()["g11_wind_tracer"])
     path = tmp_path / "c.sw"

@@ -5,8 +5,9 @@ the reference executable on the same case files (tests/golden):
   (zero fields, zonal wind, forcing at t0, frame 0) and injects Gaussians
   and vortices during the run; every field of every frame must be bit for bit
   the reference's, and the ENERGY lines equal to their printed digits;
-* restart cases (g*): the reference loads frame 1 (LoadFrom 1) and saves the
-  following frames; the runner must reproduce them bit for bit;
+* restart cases (g* bands, p* polar caps): the reference loads frame 1
+  (LoadFrom 1) and saves the following frames; the runner must reproduce them
+  bit for bit;
 * the reference's own example (examples/JupiterEnergyTest, 34,560 steps) gives
   the reference's ENERGY lines and last frame, and its known-answer file
   (enou.txt, from an older version of the code) is met within the reference's
@@ -86,7 +87,7 @@ def test_reference_example_run(tmp_path, name):
         assert hashlib.sha256(np.ascontiguousarray(fl[k]).tobytes()).hexdigest() == h, k
 
 
-@pytest.mark.parametrize("name", ["g01_minmod_nu4", "g11_wind_tracer", "g13_saturn_superbee"])
+@pytest.mark.parametrize("name", ["g01_minmod_nu4", "g11_wind_tracer", "g13_saturn_superbee"] + gc.polar_cases())
 def test_restart_cases_match_the_reference(tmp_path, name):
     entry, case, ref = gc.load_case(name)
     p = case.params
