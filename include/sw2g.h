@@ -49,6 +49,9 @@ typedef enum {
  * sw struct rather than from the .sw file: */
 #define SW2G_FLAG_RADIANS 0x2u /* lon0..lat1 are in radians, as the sw struct holds them (init.c:56-58) */
 #define SW2G_FLAG_SIGMA 0x4u   /* tau holds sigma_dis (0 = no damping), as the sw struct holds it (init.c:110-114) */
+/* The hyperviscosity of eta takes eta as its source; the reference passes u
+ * (calc.c:332), which stays the default. FP64 contexts only. */
+#define SW2G_FLAG_LAPE_ETA 0x8u
 
 /* The parsed case, as the reference's initialize() stores it in the sw struct
  * (init.c:48-161). Angles are in degrees, as in the .sw file. */

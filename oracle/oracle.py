@@ -23,7 +23,7 @@ class Params(ctypes.Structure):
                 ("gE", ctypes.c_double), ("depth", ctypes.c_double),
                 ("Dt", ctypes.c_double), ("courant", ctypes.c_double),
                 ("tau", ctypes.c_double), ("tracer_dis", ctypes.c_double),
-                ("hypernu", ctypes.c_double * 3)]
+                ("hypernu", ctypes.c_double * 3), ("lape_eta", ctypes.c_int)]
 
 
 _lib = None
@@ -59,8 +59,9 @@ def lib():
     return _lib
 
 
-def params_from_case(p) -> Params:
+def params_from_case(p, lape_eta=False) -> Params:
     q = Params()
+    q.lape_eta = int(bool(lape_eta))
     q.nx, q.ny, q.sch = p.nx, p.ny, p.sch
     q.lon0, q.lon1, q.lat0, q.lat1 = p.lon0, p.lon1, p.lat0, p.lat1
     q.Omega, q.rE, q.rP, q.gE, q.depth = p.Omega, p.rE, p.rP, p.gE, p.depth
@@ -80,8 +81,8 @@ FIELDS = ("eta", "u", "v", "tracer", "windx", "windy", "hB")
 class Oracle:
     """One oracle run of a case; fields are (ny+4, nx+4) padded arrays."""
 
-    def __init__(self, params):
-        self._p = params_from_case(params)
+    def __init__(self, params, lape_eta=False):
+        self._p = params_from_case(params, lape_eta)
         self.nx, self.ny = params.nx, params.ny
         self.h = lib().sw2o_create(ctypes.byref(self._p))
         if not self.h:

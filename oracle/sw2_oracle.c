@@ -559,7 +559,7 @@ static void one_step(sw2o *s) {
   SCHEME_SWITCH(mass_sweep_s, s, dn);
   if (s->nu2 != 0 || s->nu4 != 0 || s->nu6 != 0) {
     for (int q = 0; q < 3; q++) memset(s->Le[q], 0, sizeof(double) * (size_t)s->S);
-    lap_eta(s, u, s->Le[0]); /* the reference applies it to u (calc.c:332) */
+    lap_eta(s, s->p.lape_eta ? eta : u, s->Le[0]); /* the reference applies it to u (calc.c:332) */
     if (s->nu4 != 0 || s->nu6 != 0) {
       lap_eta(s, s->Le[0], s->Le[1]);
       if (s->nu6 != 0) lap_eta(s, s->Le[1], s->Le[2]);

@@ -33,6 +33,8 @@ typedef struct {
   double tau;                    /* Tau: sigma = 0 when tau > 1e10 (init.c:110-114) */
   double tracer_dis;
   double hypernu[3];             /* as entered (nu4 is negated internally, init.c:117-122) */
+  int lape_eta;                  /* 1: laplacian_eta takes eta as its source; the reference
+                                    passes u (calc.c:332), which is 0 here */
 } sw2o_params;
 
 typedef struct sw2o sw2o;

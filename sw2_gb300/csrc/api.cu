@@ -154,6 +154,7 @@ struct sw2g_ctx {
   Timers timers;
   bool uploaded = false;
   bool tracer_active = false;
+  bool aux_zero[3] = {true, true, true};  // windx, windy, hB hold +0.0 in every padded cell
   int k = 0;  // Adams-Bashforth index n - nstart
   long long steps = 0;
   int err_step = -1;
@@ -199,7 +200,7 @@ bool case_ok(const sw2g_case* c) {
   if (!(c->lat0 > -pole) || !(c->lat1 < pole)) return false;
   // init.c:122: hyperviscosity coefficients are entered as non-negative
   if (c->hypernu[0] < 0 || c->hypernu[1] < 0 || c->hypernu[2] < 0) return false;
-  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA)) return false;
+  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | SW2G_FLAG_LAPE_ETA)) return false;
   if (c->polar != 0) {  // the square around the pole (init.c:66-79)
     if ((c->polar != 1 && c->polar != -1) || c->nx != c->ny) return false;
     if (!(c->lon1 > 0) || c->lon0 != -c->lon1 || c->lat0 != c->lon0 || c->lat1 != c->lon1) return false;
@@ -468,7 +469,8 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   *out = nullptr;
   if (!case_ok(c) || (precision != SW2G_FP64 && precision != SW2G_FP32)) return SW2G_ERR_BAD_ARG;
   // the FP32 form covers nabla^2 and nabla^4 hyperviscosity (the configurations' operators)
-  if (precision == SW2G_FP32 && (c->hypernu[2] != 0 || c->polar != 0)) return SW2G_ERR_BAD_ARG;
+  if (precision == SW2G_FP32 && (c->hypernu[2] != 0 || c->polar != 0 || (c->flags & SW2G_FLAG_LAPE_ETA)))
+    return SW2G_ERR_BAD_ARG;
   sw2g_ctx* x = new (std::nothrow) sw2g_ctx();
   if (!x) return SW2G_ERR_NOMEM;
   x->c = *c;
@@ -500,6 +502,10 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   s.nu2 = c->hypernu[0];
   s.nu4 = -c->hypernu[1];  // init.c:120
   s.nu6 = c->hypernu[2];
+  s.lape_eta = (c->flags & SW2G_FLAG_LAPE_ETA) ? 1 : 0;
+  s.nu2dt = s.nu2 * s.Dt;
+  s.nu4dt = s.nu4 * s.Dt;
+  s.nu6dt = s.nu6 * s.Dt;
   const size_t S = (size_t)s.W * s.H;
   if ((st = dalloc(x, &x->d_rows, x->rows.size())) != SW2G_OK) return fail(st);
   if ((st = cuda_fail(cudaMemcpyAsync(x->d_rows, x->rows.data(), x->rows.size() * sizeof(double),
@@ -583,6 +589,23 @@ sw2g_status sw2g_upload(sw2g_ctx* x, const double* eta, const double* u, const d
   }
   if (mode == SW2G_UPLOAD_FRAME)
     for (int q = 0; q < 4; q++) halo_wrap(x->b.f[q], s.nx, s.ny, x->stream);
+  // Winds and bottom that are +0.0 everywhere (the usual case) let the fast
+  // bodies drop the additions u+windx, v+windy and the subtraction -hB
+  // (fp64_step's plain form; do_channel keeps such fields +0.0).
+  for (int q = 4; q < 7; q++) {
+    if (src[q]) {
+      bool z = true;
+      for (size_t t = 0; t < S && z; t++) {
+        uint64_t bits;
+        std::memcpy(&bits, &src[q][t], sizeof(bits));
+        z = (bits == 0);
+      }
+      x->aux_zero[q - 4] = z;
+    } else if (!cont) {
+      x->aux_zero[q - 4] = true;
+    }
+  }
+  x->s.plain = x->aux_zero[0] && x->aux_zero[1] && x->aux_zero[2];
   if (cont) {
     // history, step count and the tracer decision carry over (unless a tracer is given)
     if (tracer) x->tracer_active = true;

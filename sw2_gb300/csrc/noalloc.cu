@@ -125,7 +125,8 @@ extern "C" sw2g_status sw2g_energy_noalloc(const sw2g_case* c, const double* eta
   if (!c || !eta || !u || !v || !out3) return SW2G_ERR_BAD_ARG;
   if (c->nx < 3 || c->ny < 3 || !(c->rE > 0) || !(c->rP > 0) || !(c->lon1 > c->lon0) || !(c->lat1 > c->lat0))
     return SW2G_ERR_BAD_ARG;
-  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA)) return SW2G_ERR_BAD_ARG;
+  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | SW2G_FLAG_LAPE_ETA))
+    return SW2G_ERR_BAD_ARG;
   if (c->polar != 0) return SW2G_ERR_BAD_ARG;  // its gravity is two-dimensional: sw2g_diag covers caps
   if (c->ny > SW2G_NOALLOC_MAX_ROWS) {
     fprintf(stderr,

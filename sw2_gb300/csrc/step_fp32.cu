@@ -130,7 +130,9 @@ __device__ __forceinline__ float face1(float qm, float q0, float q1, float q2, f
 template <int SCH>
 __device__ __forceinline__ float face2(float qm, float q0, float q1, float q2, float cP, float cM) {
   const float d = q1 - q0;
-  const float inv = (d != 0.f) ? __frcp_rn(d) : 0.f;
+  // approximate reciprocal (relative error below 2^-22); differences below the
+  // smallest normal count as zero, like a zero difference
+  const float inv = (fabsf(d) >= 1.17549435e-38f) ? __fdividef(1.f, d) : 0.f;
   const float rP = (q0 - qm) * inv, rM = (q2 - q1) * inv;
   const float bP = q0 + 0.5f * psi<SCH>(rP) * (1.f - cP) * d;
   const float bM = q1 - 0.5f * psi<SCH>(rM) * (1.f + cM) * d;
@@ -139,6 +141,31 @@ __device__ __forceinline__ float face2(float qm, float q0, float q1, float q2, f
 
 __device__ __forceinline__ float cpos2(float a, float b, float k) { return 0.5f * (fmaxf(a, 0.f) + fmaxf(b, 0.f)) * k; }
 __device__ __forceinline__ float cneg2(float a, float b, float k) { return 0.5f * (fminf(a, 0.f) + fminf(b, 0.f)) * k; }
+
+// y faces: the two cells of a face divide by their own row metric, so their
+// Courant numbers differ, while the limited slope is shared. For a mass face
+// (one Courant number, whose sign is that of v): g = +-psi(r)/2*(q1-q0) and the
+// upwind value; the cell's term is c*(base + g*(1-|c|)).
+template <int SCH>
+__device__ __forceinline__ float2 face1_shared(float qm, float q0, float q1, float q2, bool pos) {
+  const float d = q1 - q0;
+  const float n = pos ? (q0 - qm) : (q2 - q1);
+  const float r = (fabsf(d) >= 1.17549435e-38f) ? __fdividef(n, d) : 0.f;
+  return make_float2((pos ? 0.5f : -0.5f) * psi<SCH>(r) * d, pos ? q0 : q1);
+}
+__device__ __forceinline__ float face1_term(float2 gb, float c) { return c * (gb.y + gb.x * (1.f - fabsf(c))); }
+
+// A momentum y face: gP = psi(rP)/2*(q1-q0), gM = psi(rM)/2*(q1-q0); the
+// cell's term is cP*(q0 + gP*(1-cP)) + cM*(q1 - gM*(1+cM)).
+template <int SCH>
+__device__ __forceinline__ float2 face2_shared(float qm, float q0, float q1, float q2) {
+  const float d = q1 - q0;
+  const float inv = (fabsf(d) >= 1.17549435e-38f) ? __fdividef(1.f, d) : 0.f;
+  return make_float2(0.5f * psi<SCH>((q0 - qm) * inv) * d, 0.5f * psi<SCH>((q2 - q1) * inv) * d);
+}
+__device__ __forceinline__ float face2_term(float2 g, float q0, float q1, float cP, float cM) {
+  return cP * (q0 + g.x * (1.f - cP)) + cM * (q1 - g.y * (1.f + cM));
+}
 
 // ---------------------------------------------------------- halo images
 enum Img { IMG_ETA, IMG_U, IMG_V, IMG_LU, IMG_LV };
@@ -288,21 +315,56 @@ struct Main1Io {
   int* bad;
 };
 
+// Faces of the three TVD bodies in tile-local ring-2 coordinates (column A,
+// row B; global (i0-2+A, j0-2+B)). An x face lies west of column A and is
+// shared whole by its two cells (their Courant numbers use the same row
+// metric); a y face lies north of row B and shares its limited slopes.
+template <int SCH>
+__device__ __forceinline__ float mass_xface(const Tile& se, const Tile& su, float kx, int A, int B) {
+  return face1<SCH>(se[B][A - 2], se[B][A - 1], se[B][A], se[B][A + 1], su[B][A - 1] * kx);
+}
+template <int SCH>
+__device__ __forceinline__ float u_xface(const Tile& su, float kc, int A, int B) {
+  const float uw = su[B][A - 1], ue = su[B][A];
+  return face2<SCH>(su[B][A - 2], uw, ue, su[B][A + 1], cpos2(uw, ue, kc), cneg2(uw, ue, kc));
+}
+template <int SCH>
+__device__ __forceinline__ float v_xface(const Tile& sv, const Tile& su, float kxv, int A, int B) {
+  const float u1 = su[B + 1][A - 1], u0 = su[B][A - 1];
+  return face2<SCH>(sv[B][A - 2], sv[B][A - 1], sv[B][A], sv[B][A + 1], cpos2(u1, u0, kxv), cneg2(u1, u0, kxv));
+}
+// Heights relative to the reference of row B (global row j).
+template <int SCH>
+__device__ __forceinline__ float2 mass_yface(const Tile& se, const Tile& sv, const Rows& rc, int A, int B, int j) {
+  return face1_shared<SCH>(se[B - 1][A] + Q(rc, Q_DHBM1, j), se[B][A], se[B + 1][A] + Q(rc, Q_DHBP1, j),
+                           se[B + 2][A] + Q(rc, Q_DHBP2, j), sv[B][A] > 0.f);
+}
+template <int SCH>
+__device__ __forceinline__ float2 mom_yface(const Tile& t, int A, int B) {
+  return face2_shared<SCH>(t[B - 1][A], t[B][A], t[B + 1][A], t[B + 2][A]);
+}
+
 template <int SCH>
 __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1Io& o) {
   __shared__ __align__(16) Tile se, su, sv, sl, sm;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
+  // x faces [b][a]: west of tile column a (a = 0..TW); y faces [b][a]: south of
+  // tile row b (b = 0..TH)
+  __shared__ float xm[TH][TW + 1], xu[TH][TW + 1], xv[TH][TW + 1];
+  __shared__ float2 ym[TH + 1][TW], yu[TH + 1][TW], yv[TH + 1][TW];
   __shared__ float red[2][NT / 32];
   __shared__ RowCache sq;
   const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
   const int i0 = bx * TW + 1, j0 = by * TH + 1;
   // this thread's own cell: issue its global loads before the tile traffic
-  const int a = threadIdx.x % TW + 2, b = threadIdx.x / TW + 2;  // ring-2 local coordinates
-  const int i = i0 + a - 2, j = j0 + b - 2;
+  const int ta = threadIdx.x % TW, tb = threadIdx.x / TW;  // tile coordinates
+  const int a = ta + 2, b = tb + 2;                          // ring-2 local coordinates
+  const int i = i0 + ta, j = j0 + tb;
   const bool live = (i <= nx && j <= ny);
   const int q = IX(W, live ? i : 1, live ? j : 1), q32 = IX32(P, i, j);
   const double eta_old = o.eta[q];
   const float h1v = (p.k >= 1) ? o.h1[q32] : 0.f, h2v = (p.k >= 2) ? o.h2[q32] : 0.f;
+  const float e_raw = p.extra ? o.es[q32] : 0.f;  // eta without the bottom, for the damping
   fill_rows(p, j0, sq);
   const Rows rc{sq, j0};
   load_tile(o.es, P, i0, j0, se);
@@ -311,48 +373,55 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
   load_tile(o.Lu, P, i0, j0, sl);
   load_tile(o.Lv, P, i0, j0, sm);
   __syncthreads();
-  if (p.extra) {  // UWINDX, VWINDY (sw.h:216-217); the bottom enters H below
+  if (p.extra) {  // UWINDX, VWINDY (sw.h:216-217) and H = eta + depth - hB (sw.h:213)
     for (int t = threadIdx.x; t < (TH + 4) * (TW + 4); t += NT) {
-      const int a = t % (TW + 4), b = t / (TW + 4);
-      const int q = IX32(P, i0 - 2 + a, j0 - 2 + b);
-      su[b][a] += p.wx[q];
-      sv[b][a] += p.wy[q];
+      const int c = t % (TW + 4), r = t / (TW + 4);
+      const int qq = IX32(P, i0 - 2 + c, j0 - 2 + r);
+      su[r][c] += p.wx[qq];
+      sv[r][c] += p.wy[qq];
+      se[r][c] -= p.hb[qq];
     }
     __syncthreads();
   }
   zeta_div(p, rc, i0, j0, sl, sm, o.Lu, o.Lv, ze, di);
+  {  // faces: each thread the x faces west of its cell and the y faces north of it
+    xm[tb][ta] = mass_xface<SCH>(se, su, Q(rc, Q_KXE, j), a, b);
+    xu[tb][ta] = u_xface<SCH>(su, Q(rc, Q_KXC, j), a, b);
+    xv[tb][ta] = v_xface<SCH>(sv, su, Q(rc, Q_KXV, j), a, b);
+    ym[tb + 1][ta] = mass_yface<SCH>(se, sv, rc, a, b, j);
+    yu[tb + 1][ta] = mom_yface<SCH>(su, a, b);
+    yv[tb + 1][ta] = mom_yface<SCH>(sv, a, b);
+    // and the tile's south row and east column of faces, on the last warps
+    // (the first ones carry the extra items of zeta_div)
+    const int w = tb, l = ta;
+    if (w == TH - 4) ym[0][l] = mass_yface<SCH>(se, sv, rc, l + 2, 1, j0 - 1);
+    else if (w == TH - 3) yu[0][l] = mom_yface<SCH>(su, l + 2, 1);
+    else if (w == TH - 2) yv[0][l] = mom_yface<SCH>(sv, l + 2, 1);
+    else if (w == TH - 1 && l < 3 * TH) {
+      const int r = l % TH, B = r + 2, jr = j0 + r;
+      if (l < TH) xm[r][TW] = mass_xface<SCH>(se, su, Q(rc, Q_KXE, jr), TW + 2, B);
+      else if (l < 2 * TH) xu[r][TW] = u_xface<SCH>(su, Q(rc, Q_KXC, jr), TW + 2, B);
+      else xv[r][TW] = v_xface<SCH>(sv, su, Q(rc, Q_KXV, jr), TW + 2, B);
+    }
+  }
   __syncthreads();
 
   float mxu = 0.f, mxv = 0.f;
   if (live) {
     // ---- mass (BODYH, calc.c:70-113), H relative to the row reference Hb(j)
-    float qx[5], qy[5];
-#pragma unroll
-    for (int s = -2; s <= 2; s++) qx[s + 2] = se[b][a + s];
-    qy[0] = se[b - 2][a] + Q(rc, Q_DHBM2, j);
-    qy[1] = se[b - 1][a] + Q(rc, Q_DHBM1, j);
-    qy[2] = qx[2];
-    qy[3] = se[b + 1][a] + Q(rc, Q_DHBP1, j);
-    qy[4] = se[b + 2][a] + Q(rc, Q_DHBP2, j);
-    if (p.extra) {
-#pragma unroll
-      for (int s = -2; s <= 2; s++) {
-        qx[s + 2] -= p.hb[IX32(P, i + s, j)];
-        qy[s + 2] -= p.hb[IX32(P, i, j + s)];
-      }
-    }
     const float kx = Q(rc, Q_KXE, j), ky = Q(rc, Q_KYN, j);
     const float cw = su[b][a - 1] * kx, ce = su[b][a] * kx, cs = sv[b - 1][a] * ky, cn = sv[b][a] * ky;
-    float deta = face1<SCH>(qx[0], qx[1], qx[2], qx[3], cw) - face1<SCH>(qx[1], qx[2], qx[3], qx[4], ce) +
-                 face1<SCH>(qy[0], qy[1], qy[2], qy[3], cs) - face1<SCH>(qy[1], qy[2], qy[3], qy[4], cn);
+    float2 fs = ym[tb][ta];
+    fs.y += Q(rc, Q_DHBM1, j);  // the south face's upwind value relative to Hb(j)
+    float deta = xm[tb][ta] - xm[tb][ta + 1] + face1_term(fs, cs) - face1_term(ym[tb + 1][ta], cn);
     deta += Q(rc, Q_HB, j) * ((cw - ce) + (cs - cn));
-    deta -= p.sig2dt * (Q(rc, Q_EREF, j) + se[b][a]);
+    deta -= p.sig2dt * (Q(rc, Q_EREF, j) + (p.extra ? e_raw : se[b][a]));
     // Adams-Bashforth (calc.c:651-699) then the geofactor (calc.c:403-422)
     float ab;
     if (p.k == 0) ab = deta;
     else if (p.k == 1) ab = 1.5f * deta - 0.5f * h1v;
     else ab = (23.f / 12.f) * deta - (4.f / 3.f) * h1v + (5.f / 12.f) * h2v;
-    const float hcell = Q(rc, Q_HB, j) + qx[2];
+    const float hcell = Q(rc, Q_HB, j) + se[b][a];
     ab -= Q(rc, Q_GEO, j) * hcell * 0.5f * (sv[b][a] + sv[b - 1][a]);
     o.hist_eta[q32] = deta;
     const double en = eta_old + f2d(ab);
@@ -362,20 +431,16 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
 
     // ---- second Laplacian of (u, v) from L (laplacian.c:83-89)
     float llu, llv;
-    lap_out(rc, j, a - 2, b - 2, ze, di, llu, llv);
+    lap_out(rc, j, ta, tb, ze, di, llu, llv);
 
     // ---- BODYU (calc.c:168-200)
     {
-      float ux[5], uy[5];
-#pragma unroll
-      for (int s = -2; s <= 2; s++) { ux[s + 2] = su[b][a + s]; uy[s + 2] = su[b + s][a]; }
-      const float uwm = ux[1], u0 = ux[2], uep = ux[3];
+      const float uwm = su[b][a - 1], u0 = su[b][a], uep = su[b][a + 1];
       const float vs0 = sv[b - 1][a], vs1 = sv[b - 1][a + 1], vn0 = sv[b][a], vn1 = sv[b][a + 1];
-      const float kc = Q(rc, Q_KXC, j), kv = Q(rc, Q_KYV, j);
-      float p1 = face2<SCH>(ux[0], ux[1], ux[2], ux[3], cpos2(uwm, u0, kc), cneg2(uwm, u0, kc)) -
-                 face2<SCH>(ux[1], ux[2], ux[3], ux[4], cpos2(u0, uep, kc), cneg2(u0, uep, kc)) +
-                 face2<SCH>(uy[0], uy[1], uy[2], uy[3], cpos2(vs0, vs1, kv), cneg2(vs0, vs1, kv)) -
-                 face2<SCH>(uy[1], uy[2], uy[3], uy[4], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv));
+      const float kv = Q(rc, Q_KYV, j);
+      const float p1 = xu[tb][ta] - xu[tb][ta + 1] +
+                       face2_term(yu[tb][ta], su[b - 1][a], u0, cpos2(vs0, vs1, kv), cneg2(vs0, vs1, kv)) -
+                       face2_term(yu[tb + 1][ta], u0, su[b + 1][a], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv));
       const float p2 = u0 * (uep - uwm) * Q(rc, Q_K2XE, j) + u0 * (0.5f * (vn0 + vn1) - 0.5f * (vs0 + vs1)) * kv;
       const float ul = p.extra ? o.us[q32] : u0;  // dissipation acts on U without the wind
       float du = p1 + p2 - ul * p.sigdt;
@@ -385,16 +450,12 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
     }
     // ---- BODYV (calc.c:205-237)
     {
-      float vx[5], vy[5];
-#pragma unroll
-      for (int s = -2; s <= 2; s++) { vx[s + 2] = sv[b][a + s]; vy[s + 2] = sv[b + s][a]; }
-      const float vsm = vy[1], v0 = vy[2], vnp = vy[3];
+      const float vsm = sv[b - 1][a], v0 = sv[b][a], vnp = sv[b + 1][a];
       const float uw1 = su[b + 1][a - 1], uw0 = su[b][a - 1], ue1 = su[b + 1][a], ue0 = su[b][a];
       const float kxv = Q(rc, Q_KXV, j), kyc = Q(rc, Q_KYC, j);
-      float p1 = face2<SCH>(vx[0], vx[1], vx[2], vx[3], cpos2(uw1, uw0, kxv), cneg2(uw1, uw0, kxv)) -
-                 face2<SCH>(vx[1], vx[2], vx[3], vx[4], cpos2(ue1, ue0, kxv), cneg2(ue1, ue0, kxv)) +
-                 face2<SCH>(vy[0], vy[1], vy[2], vy[3], cpos2(vsm, v0, kyc), cneg2(vsm, v0, kyc)) -
-                 face2<SCH>(vy[1], vy[2], vy[3], vy[4], cpos2(v0, vnp, kyc), cneg2(v0, vnp, kyc));
+      const float p1 = xv[tb][ta] - xv[tb][ta + 1] +
+                       face2_term(yv[tb][ta], vsm, v0, cpos2(vsm, v0, kyc), cneg2(vsm, v0, kyc)) -
+                       face2_term(yv[tb + 1][ta], v0, vnp, cpos2(v0, vnp, kyc), cneg2(v0, vnp, kyc));
       const float p2 = v0 * (0.5f * (ue0 + ue1) - 0.5f * (uw0 + uw1)) * kxv + v0 * (vnp - vsm) * Q(rc, Q_KDYNS, j);
       const float vl = p.extra ? o.vs[q32] : v0;
       float dv = p1 + p2 - vl * p.sigdt;

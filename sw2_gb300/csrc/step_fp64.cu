@@ -367,28 +367,34 @@ __device__ __forceinline__ XN x_neighbours(double v, double aux, int lane) {
     const int ia = (lane == 0) ? base - 2 : (lane == 1) ? base - 1 : min(base + 32, nx + 2); \
     const bool own = (lane < FW) && (i <= nx);
 #define FAST_END }
+// Field values of the fast bodies. PL (plain form): windx, windy and hB are
+// +0.0 everywhere, so x - hB = x exactly, and u + windx = u except that -0
+// becomes +0, which the fast path cannot tell apart (see (3) above).
+#define UF(i, j) (PL ? f.u[IX(W, i, j)] : UW(i, j))
+#define VF(i, j) (PL ? f.v[IX(W, i, j)] : VW(i, j))
+#define HF(i, j) (PL ? (f.eta[IX(W, i, j)] + s.depth) : HH(i, j))
 
 // BODYH + damping, fast form.
-template <int SCH>
+template <int SCH, bool PL>
 __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   const double damp = 2.0 * Dt * (s.sigma);  // calc.c:112: (2.0*Dt*sigma)*ETA
   // H at this lane's column, rows j-1 .. j+1 (window), and the face south of j0
-  double h1 = HH(ic, j0 - 1), h2 = HH(ic, j0), h3 = HH(ic, j0 + 1);
+  double h1 = HF(ic, j0 - 1), h2 = HF(ic, j0), h3 = HF(ic, j0 + 1);
   double tsP, tsM;
   bool oks;
   {
-    const double b = VW(ic, j0 - 1);
-    const Face F = make_face<SCH>(HH(ic, j0 - 2), h1, h2, h3, up_p(b), up_m(b), fin(b));
+    const double b = VF(ic, j0 - 1);
+    const Face F = make_face<SCH>(HF(ic, j0 - 2), h1, h2, h3, up_p(b), up_m(b), fin(b));
     face_terms(F, Dt, ROW2(R_DYN, R_IDYN, j0), tsP, tsM);
     oks = F.ok;
   }
   for (int j = j0; j <= jn; j++) {
-    const double h4 = HH(ic, j + 2);
+    const double h4 = HF(ic, j + 2);
     // x face west of column i, row j
-    const XN xn = x_neighbours(h2, HH(ia, j), lane);
-    const double a = UW(iu, j);
+    const XN xn = x_neighbours(h2, HF(ia, j), lane);
+    const double a = UF(iu, j);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, h2, xn.p1, up_p(a), up_m(a), fin(a));
     double twP, twM;
     face_terms(FX, Dt, ROW2(R_DXE, R_IDXE, j), twP, twM);
@@ -396,7 +402,7 @@ __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, dou
     const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // y face north of row j: shared by this cell and the cell above
-    const double b = VW(ic, j);
+    const double b = VF(ic, j);
     const Face FY = make_face<SCH>(h1, h2, h3, h4, up_p(b), up_m(b), fin(b));
     double tnP, tnM, nsP, nsM;
     face_terms(FY, Dt, ROW2(R_DYN, R_IDYN, j), tnP, tnM);
@@ -427,25 +433,25 @@ __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, dou
 }
 
 // BODYU, fast form.
-template <int SCH>
+template <int SCH, bool PL>
 __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int ic1 = min(i + 1, nx + 2);
   // U at this lane's column, rows j-1 .. j+1, and V at columns i, i+1 of row j-1
-  double u1 = UW(ic, j0 - 1), u2 = UW(ic, j0), u3 = UW(ic, j0 + 1);
-  double vs0 = VW(ic, j0 - 1), vs1 = VW(ic1, j0 - 1);
+  double u1 = UF(ic, j0 - 1), u2 = UF(ic, j0), u3 = UF(ic, j0 + 1);
+  double vs0 = VF(ic, j0 - 1), vs1 = VF(ic1, j0 - 1);
   double tsP, tsM;
   bool oks;
   {
-    const Face F = make_face<SCH>(UW(ic, j0 - 2), u1, u2, u3, 0.5 * (up_p(vs0) + up_p(vs1)),
+    const Face F = make_face<SCH>(UF(ic, j0 - 2), u1, u2, u3, 0.5 * (up_p(vs0) + up_p(vs1)),
                                   0.5 * (up_m(vs0) + up_m(vs1)), fin(vs0) && fin(vs1));
     face_terms(F, Dt, ROW2(R_DYV, R_IDYV, j0), tsP, tsM);
     oks = F.ok;
   }
   for (int j = j0; j <= jn; j++) {
-    const double u4 = UW(ic, j + 2);
+    const double u4 = UF(ic, j + 2);
     // x face west of column i, row j: velocities u(i-1), u(i)
-    const XN xn = x_neighbours(u2, UW(ia, j), lane);
+    const XN xn = x_neighbours(u2, UF(ia, j), lane);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, u2, xn.p1, 0.5 * (up_p(xn.m1) + up_p(u2)),
                                    0.5 * (up_m(xn.m1) + up_m(u2)), true);
     double twP, twM;
@@ -454,7 +460,7 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, do
     const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // y face north of row j: velocities v(i, j), v(i+1, j)
-    const double vn0 = VW(ic, j), vn1 = VW(ic1, j);
+    const double vn0 = VF(ic, j), vn1 = VF(ic1, j);
     const Face FY = make_face<SCH>(u1, u2, u3, u4, 0.5 * (up_p(vn0) + up_p(vn1)), 0.5 * (up_m(vn0) + up_m(vn1)),
                                    fin(vn0) && fin(vn1));
     double tnP, tnM, nsP, nsM;
@@ -493,26 +499,26 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, do
 }
 
 // BODYV, fast form.
-template <int SCH>
+template <int SCH, bool PL>
 __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   // V at this lane's column, rows j-1 .. j+1; U at column i-1, row j
-  double v1 = VW(ic, j0 - 1), v2 = VW(ic, j0), v3 = VW(ic, j0 + 1);
-  double uw0 = UW(iu, j0);
+  double v1 = VF(ic, j0 - 1), v2 = VF(ic, j0), v3 = VF(ic, j0 + 1);
+  double uw0 = UF(iu, j0);
   double tsP, tsM;
   bool oks;
   {
-    const Face F = make_face<SCH>(VW(ic, j0 - 2), v1, v2, v3, 0.5 * (up_p(v1) + up_p(v2)),
+    const Face F = make_face<SCH>(VF(ic, j0 - 2), v1, v2, v3, 0.5 * (up_p(v1) + up_p(v2)),
                                   0.5 * (up_m(v1) + up_m(v2)), true);
     face_terms(F, Dt, ROW2(R_DYC, R_IDYC, j0), tsP, tsM);
     oks = F.ok;
   }
   for (int j = j0; j <= jn; j++) {
-    const double v4 = VW(ic, j + 2);
-    const double uw1 = UW(iu, j + 1);
+    const double v4 = VF(ic, j + 2);
+    const double uw1 = UF(iu, j + 1);
     // x face west of column i, row j: velocities u(i-1, j+1), u(i-1, j)
-    const XN xn = x_neighbours(v2, VW(ia, j), lane);
+    const XN xn = x_neighbours(v2, VF(ia, j), lane);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, v2, xn.p1, 0.5 * (up_p(uw1) + up_p(uw0)),
                                    0.5 * (up_m(uw1) + up_m(uw0)), fin(uw1) && fin(uw0));
     double twP, twM;
@@ -559,6 +565,9 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, do
 }
 #undef FAST_SETUP
 #undef FAST_END
+#undef UF
+#undef VF
+#undef HF
 #undef ROW2
 
 // Self-check of div_rcp: for each divisor b, `samples` numerators a drawn
@@ -645,14 +654,33 @@ __global__ void k_lape_fix(int nx, int ny, double* eo) {
   eo[IX(W, i, 0)] = eo[IX(W, i, 1)];
 }
 
-// Deta_n += nu*Dt*L (calc.c:346-350); Du/Dv the same (core.c:258-266)
+// Deta_n += nu*Dt*L (calc.c:346-350); Du/Dv the same (core.c:258-266), with
+// nu*Dt formed once on the host by the same multiplication. A term whose nu
+// is a zero adds the product nudt*L, a zero when L is finite, and adding a
+// zero to a finite nonzero x gives x; only a zero x (the sign of the sum) or a
+// non-finite operand needs that term's arithmetic.
+__device__ __forceinline__ bool zero_term_is_exact(double x, double L) {
+  const long long xb = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  return xb != 0 && xb < 0x7ff0000000000000LL && dexp(L) != 0x7ff;
+}
+// Out of line, so that the rare case is a branch and not predicated FP64 work.
+__device__ __noinline__ double add_product(double x, double nd, double v) { return x + nd * v; }
+
 __global__ void k_hyper_add(DevState s, double* d, const double* l2, const double* l4, const double* l6) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
   double x = d[q];
-  x += (s.nu2) * (s.Dt) * l2[q];
-  x += (s.nu4) * (s.Dt) * l4[q];
-  x += (s.nu6) * (s.Dt) * l6[q];
+  const double* L[3] = {l2, l4, l6};
+  const double nd[3] = {s.nu2dt, s.nu4dt, s.nu6dt};
+#pragma unroll
+  for (int t = 0; t < 3; t++) {
+    const double v = L[t][q];
+    if ((__double_as_longlong(nd[t]) & 0x7fffffffffffffffLL) != 0) {
+      x = x + nd[t] * v;
+    } else if (!zero_term_is_exact(x, v)) {
+      x = add_product(x, nd[t], v);
+    }
+  }
   d[q] = x;
 }
 
@@ -784,24 +812,53 @@ __global__ void k_channel(int nx, int ny, double* u, double* v, double* wx, doub
 }
 
 // compute_Dt maxima (calc.c:705-712): max |u+wx|/DXE and |v+wy|/DYN over the
-// interior; NaNs never win the comparison, as in the reference's loop.
-__global__ void k_cfl(DevState s, F7 f, unsigned long long* out) {
+// interior; NaNs never win the comparison, as in the reference's loop. A
+// correctly rounded division by a positive number is non-decreasing in the
+// numerator, so the largest quotient of a row is the quotient of its largest
+// magnitude: the magnitudes are compared as integers (NaNs set to 0) and each
+// warp divides once.
+__device__ __forceinline__ long long mag_bits(double x) {
+  const long long m = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  return (m > 0x7ff0000000000000LL) ? 0 : m;
+}
+// One block per row: the row's largest magnitudes, then its two quotients and
+// two atomics (atomics on the same address from every warp of the grid would
+// serialise in L2).
+constexpr int CFL_T = 256;
+__global__ void __launch_bounds__(CFL_T) k_cfl(DevState s, F7 f, unsigned long long* out) {
+  __shared__ long long red[2][CFL_T / 32];
   const int W = s.W;
-  const int i = blockIdx.x * TX + threadIdx.x + 1;
-  const int j = blockIdx.y + 1;
-  double mx = 0, my = 0;
-  if (i <= s.nx) {
-    const double ax = div_rcp(fabs(UW(i, j)), RW(s, R_DXE, j), RW(s, R_IDXE, j));
-    const double ay = div_rcp(fabs(VW(i, j)), RW(s, R_DYN, j), RW(s, R_IDYN, j));
-    mx = (ax > mx) ? ax : mx;
-    my = (ay > my) ? ay : my;
+  const int j = blockIdx.x + 1;
+  long long bx = 0, by = 0;
+  if (s.plain) {  // |u + (+0)| = |u|
+#pragma unroll 4
+    for (int i = threadIdx.x + 1; i <= s.nx; i += CFL_T) {
+      bx = max(bx, mag_bits(f.u[IX(W, i, j)]));
+      by = max(by, mag_bits(f.v[IX(W, i, j)]));
+    }
+  } else {
+#pragma unroll 4
+    for (int i = threadIdx.x + 1; i <= s.nx; i += CFL_T) {
+      bx = max(bx, mag_bits(UW(i, j)));
+      by = max(by, mag_bits(VW(i, j)));
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
-    const double ox = __shfl_xor_sync(0xffffffffu, mx, o), oy = __shfl_xor_sync(0xffffffffu, my, o);
-    mx = (ox > mx) ? ox : mx;
-    my = (oy > my) ? oy : my;
+    bx = max(bx, __shfl_xor_sync(0xffffffffu, bx, o));
+    by = max(by, __shfl_xor_sync(0xffffffffu, by, o));
   }
   if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = bx;
+    red[1][threadIdx.x >> 5] = by;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < CFL_T / 32; w++) {
+      bx = max(bx, red[0][w]);
+      by = max(by, red[1][w]);
+    }
+    const double mx = div_rcp(__longlong_as_double(bx), RW(s, R_DXE, j), RW(s, R_IDXE, j));
+    const double my = div_rcp(__longlong_as_double(by), RW(s, R_DYN, j), RW(s, R_IDYN, j));
     if (mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
     if (my > 0) atomicMax(out + 1, (unsigned long long)__double_as_longlong(my));
   }
@@ -810,11 +867,24 @@ __global__ void k_cfl(DevState s, F7 f, unsigned long long* out) {
 // check_stats_scaf (sppde_core.c:346-395) as the reference evaluates it: min and
 // max start from the first interior value and skip NaNs after it, so the step
 // aborts iff the first value is not finite or some value lies outside +-1e10.
-__global__ void k_range(DevState s, const double* x, int* bad) {
+// Tested on the bits (|x| > 1e10 and not NaN), for up to four fields at once.
+__device__ __forceinline__ bool range_bad(double x, bool first) {
+  const long long m = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  if (first) return m > 0x4202a05f20000000LL;  // beyond 1e10, inf or NaN
+  return m > 0x4202a05f20000000LL && m <= 0x7ff0000000000000LL;
+}
+struct RangeFields {
+  const double* f[4];
+  int n;
+};
+__global__ void k_range(DevState s, RangeFields r, int* bad) {
   INTERIOR_IJ
-  const double r = x[IX(W, i, j)];
-  bool b = (r < -1e10) || (r > 1e10);
-  if (i == 1 && j == 1) b = b || !isfinite(r);
+  const int q = IX(W, i, j);
+  const bool first = (i == 1 && j == 1);
+  bool b = false;
+#pragma unroll
+  for (int k = 0; k < 4; k++)
+    if (k < r.n) b = b || range_bad(r.f[k][q], first);
   if (b) atomicOr(bad, 1);
 }
 
@@ -839,9 +909,15 @@ int fast_grid(K kernel, const DevState& s) {
 template <int SCH>
 void launch_bodies(int which, dim3 g, cudaStream_t st, const DevState& s, const F7& f, double* out) {
   if constexpr (SCH != 3) {
-    if (which == 0) { k_mass_fast<SCH><<<fast_grid(k_mass_fast<SCH>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
-    if (which == 2) { k_adv_u_fast<SCH><<<fast_grid(k_adv_u_fast<SCH>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
-    if (which == 3) { k_adv_v_fast<SCH><<<fast_grid(k_adv_v_fast<SCH>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+    if (s.plain) {
+      if (which == 0) { k_mass_fast<SCH, true><<<fast_grid(k_mass_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 2) { k_adv_u_fast<SCH, true><<<fast_grid(k_adv_u_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 3) { k_adv_v_fast<SCH, true><<<fast_grid(k_adv_v_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+    } else {
+      if (which == 0) { k_mass_fast<SCH, false><<<fast_grid(k_mass_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 2) { k_adv_u_fast<SCH, false><<<fast_grid(k_adv_u_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 3) { k_adv_v_fast<SCH, false><<<fast_grid(k_adv_v_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+    }
   }
   if (which == 0) k_mass<SCH><<<g, TX, 0, st>>>(s, f, out);
   else if (which == 1) k_tracer<SCH><<<g, TX, 0, st>>>(s, f, out);
@@ -939,13 +1015,12 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
               cudaStream_t st, Timers* tm) {
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   const int gw = (s.nx + 127) / 128;
-  const size_t bytes = sizeof(double) * (size_t)s.W * s.H;
   int nl = 0;
   auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
   const bool hyper = (s.nu2 != 0 || s.nu4 != 0 || s.nu6 != 0);
 
   // compute_Dt (core.c:155-159): maxima at the start of the step
-  LAUNCH("cfl", k_cfl<<<g, TX, 0, st>>>(s, F(), chk.cfl + 2 * slot));
+  LAUNCH("cfl", k_cfl<<<s.ny, CFL_T, 0, st>>>(s, F(), chk.cfl + 2 * slot));
 
   // tracer (core.c:161-182); skipped while the tracer is identically +0, which
   // the step then provably leaves unchanged
@@ -960,12 +1035,14 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   // mass (core.c:184-210; calc.c:289-355)
   LAUNCH("mass", body(0, sch, g, st, s, F(), b.deta[0]));
   if (hyper) {
-    const double* src = b.f[1];  // the reference passes u, not eta (calc.c:332)
-    for (int q = 0; q < 3; q++) cudaMemsetAsync(b.Le[q], 0, bytes, st);
+    // The reference zeroes Le, psi and xi before the Laplacians (calc.c:325-327,
+    // laplacian.c:116-118). Here they are zeroed once at allocation: every
+    // level that runs rewrites all cells of its Le (interior, halo wrap, wall
+    // rows) and the interior of psi and xi, whose halos stay zero; levels that
+    // do not run leave their Le zero.
+    const double* src = s.lape_eta ? b.f[0] : b.f[1];  // the reference passes u, not eta (calc.c:332)
     const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
     for (int q = 0; q < nlap; q++) {
-      cudaMemsetAsync(b.psi, 0, bytes, st);
-      cudaMemsetAsync(b.xi, 0, bytes, st);
       LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
       LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
       LAUNCH("halo", halo_wrap(b.Le[q], s.nx, s.ny, st));
@@ -985,13 +1062,12 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   LAUNCH("adv_v", body(3, sch, g, st, s, F(), b.dvadv));
   LAUNCH("pres_sum", k_pres_sum<<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
   if (hyper) {
-    for (int q = 0; q < 6; q++) cudaMemsetAsync(b.L[q], 0, bytes, st);
+    // As above: each level rewrites every cell of ze, di and its two L fields
+    // (interior, halo wraps, wall fixes), and L of levels not run stay zero.
     const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
     for (int q = 0; q < nlap; q++) {
       const double* uu = q == 0 ? b.f[1] : b.L[2 * q - 2];
       const double* vv = q == 0 ? b.f[2] : b.L[2 * q - 1];
-      cudaMemsetAsync(b.ze, 0, bytes, st);
-      cudaMemsetAsync(b.di, 0, bytes, st);
       LAUNCH("lapv_pass1", k_lapv_pass1<<<g, TX, 0, st>>>(s, uu, vv, b.ze, b.di));
       LAUNCH("halo", halo_wrap(b.ze, s.nx, s.ny, st));
       LAUNCH("halo", halo_wrap(b.di, s.nx, s.ny, st));
@@ -1030,12 +1106,14 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
   int nl = 0;
   if (s.polar == 0) LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
 
-  // range checks of tracer, eta, u, v (core.c:309-312)
-  const int order[4] = {3, 0, 1, 2};
-  for (int q = 0; q < 4; q++) {
-    if (order[q] == 3 && !tracer) continue;  // an all-zero tracer passes trivially
-    LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, b.f[order[q]], chk.bad + slot));
-  }
+  // range checks of tracer, eta, u, v (core.c:309-312); an all-zero tracer
+  // passes trivially
+  RangeFields r{};
+  if (tracer) r.f[r.n++] = b.f[3];
+  r.f[r.n++] = b.f[0];
+  r.f[r.n++] = b.f[1];
+  r.f[r.n++] = b.f[2];
+  LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, r, chk.bad + slot));
   return nl;
 }
 #undef LAUNCH

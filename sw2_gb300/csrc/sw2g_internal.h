@@ -48,6 +48,9 @@ struct DevState {
   int nx, ny, W, H;  // W = nx+4 (row pitch), H = ny+4
   const double* rows;  // R_NUM * H
   double depth, Dt, sigma, sigma_tr, nu2, nu4, nu6;
+  double nu2dt, nu4dt, nu6dt;  // (nu)*(Dt) as the reference forms it (calc.c:346-348)
+  int plain;           // windx, windy and hB are +0.0 in every padded cell
+  int lape_eta;        // laplacian_eta of eta instead of u (SW2G_FLAG_LAPE_ETA)
   int polar;           // 0: band; +-1: polar cap, with the fields below
   const double* pf;    // P_NUM * W * H (polar only)
 };

@@ -22,6 +22,7 @@ FP64, FP32 = 0, 1
 FLAG_VANLEER_SAFE = 0x1
 FLAG_RADIANS = 0x2
 FLAG_SIGMA = 0x4
+FLAG_LAPE_ETA = 0x8
 UPLOAD_RAW, UPLOAD_FRAME, UPLOAD_CONTINUE = 0, 1, 2
 BATCH_MAX = 96
 

@@ -141,6 +141,37 @@ def test_gpu_cfl_abort_step_matches_oracle():
     assert s3.step(3) == lib.ERR_CFL and s3.error_step() == 0
 
 
+@pytest.mark.parametrize("plant", ["nan_u", "nan_v_first", "nan_eta_first", "inf_v", "big_eta", "negzero"])
+def test_gpu_nonfinite_values_follow_the_reference_checks(plant):
+    """The CFL maxima skip NaNs and keep infinities (calc.c:705-712); the range
+    check aborts on a non-finite first value or a value beyond 1e10 and is
+    blind to later NaNs (sppde_core.c:346-395). Planted values must give the
+    oracle's status, abort step and fields."""
+    case = cases.make_case(nx=40, ny=20, sch=2, seed=23)
+    f = list(case.fields())
+    names = ("eta", "u", "v")
+    where = {"nan_u": (1, 9, 5, np.nan), "nan_v_first": (2, 0, 0, np.nan), "nan_eta_first": (0, 0, 0, np.nan),
+             "inf_v": (2, 13, 4, np.inf), "big_eta": (0, 20, 10, 2e10), "negzero": (1, 7, 3, -0.0)}[plant]
+    k, i, j, val = where
+    arr = f[k].copy()
+    arr[j + 2, i + 2] = val
+    f[k] = arr
+    s = lib.Solver(case.params)
+    s.upload(*f, mode=lib.UPLOAD_FRAME)
+    o = orc.Oracle(case.params)
+    o.load(f)
+    rc_o, bad = o.step(6)
+    rc = s.step(6)
+    want = {0: lib.OK, 1: lib.ERR_CFL, 2: lib.ERR_NONFINITE}[rc_o]
+    assert rc == want, (names[k], rc, rc_o)
+    if rc != lib.OK:
+        assert s.error_step() == bad
+    else:
+        got = s.download()
+        for q in FIELDS:
+            assert same(got[q], o.field(q)), q
+
+
 def test_gpu_energy_matches_oracle():
     case = cases.make_case(nx=96, ny=48, sch=2, seed=3, bumps=3)
     s, o = run_both(case, 30)
@@ -206,3 +237,25 @@ def test_sw_struct_conventions():
     ga, gb = a.download(), b.download()
     for k in FIELDS:
         assert same(ga[k], gb[k]), k
+
+
+def test_gpu_eta_hyperviscosity_of_eta():
+    """SW2G_FLAG_LAPE_ETA: the eta hyperviscosity takes eta as its source
+    instead of u (the reference's calc.c:332). Bit-identical to the oracle run
+    the same way, and different from the default run."""
+    case = cases.make_case(nx=64, ny=32, sch=2, seed=5)
+    nu4 = case.params.hypernu[1]
+    case.params.hypernu = (1e-3 * nu4 ** 0.5, nu4, 1e-4 * nu4 ** 1.5)
+    s = lib.Solver(case.params, flags=lib.FLAG_LAPE_ETA)
+    s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    assert s.step(30) == lib.OK
+    got = s.download()
+    o = orc.Oracle(case.params, lape_eta=True)
+    o.load(case.fields())
+    assert o.step(30) == (0, -1)
+    for k in FIELDS:
+        assert same(got[k], o.field(k)), k
+    d = orc.Oracle(case.params)
+    d.load(case.fields())
+    d.step(30)
+    assert not np.array_equal(got["eta"], d.field("eta"))
