@@ -133,6 +133,22 @@ sw2g_status sw2g_diag(sw2g_ctx *ctx, double *ke, double *ape, double *mass);
 /* Restarts the Adams-Bashforth sequence with an Euler step (as after LoadFrom). */
 sw2g_status sw2g_reset_ab(sw2g_ctx *ctx);
 
+/* Exact restart of an FP64 context. The reference restarts from a frame
+ * (interior only, halos rewrapped) with the Adams-Bashforth index reset
+ * (core.c:115-134), so its restarted run departs from the uninterrupted one.
+ * A checkpoint holds everything the next step reads: every padded cell of
+ * eta, u, v, tracer, windx, windy and hB, the tendency histories D(n-1) and
+ * D(n-2) of eta, u, v and tracer, the Adams-Bashforth index and whether the
+ * tracer is advected. Loaded into a context created from the same case, the
+ * run continues bit for bit as if it had not stopped.
+ *   sw2g_checkpoint_doubles: length of the buffer (doubles); 0 for an FP32 context.
+ *   sw2g_checkpoint_save / _load: buffer of that length; the first values are
+ *   a header (format, nx, ny, Adams-Bashforth index, tracer flag). Loading a
+ *   buffer of another grid or format gives SW2G_ERR_BAD_ARG. */
+size_t sw2g_checkpoint_doubles(const sw2g_ctx *ctx);
+sw2g_status sw2g_checkpoint_save(sw2g_ctx *ctx, double *buf, size_t n);
+sw2g_status sw2g_checkpoint_load(sw2g_ctx *ctx, const double *buf, size_t n);
+
 /* Steps taken since the last upload. */
 long long sw2g_steps_done(const sw2g_ctx *ctx);
 

@@ -88,7 +88,8 @@ def build_host() -> None:
     _run([*HOST_C, "-shared", *inc, *srcs, "-o", HOSTLIB + ".tmp", "-lm"])
     os.replace(HOSTLIB + ".tmp", HOSTLIB)
     run_srcs = srcs + [os.path.join(HOSTDIR, "swrun.c"), os.path.join(HOSTDIR, "swmain.c")]
-    _run([*HOST_C, *inc, *run_srcs, "-o", RUNNER + ".tmp", "-L", OUT, "-lsw2g", "-Wl,-rpath,$ORIGIN", "-lm"])
+    _run([*HOST_C, *inc, *run_srcs, "-o", RUNNER + ".tmp", "-L", OUT, "-lsw2g", "-Wl,-rpath,$ORIGIN", "-lm",
+          "-lpthread"])
     os.replace(RUNNER + ".tmp", RUNNER)
 
 

@@ -833,6 +833,76 @@ sw2g_status sw2g_reset_ab(sw2g_ctx* x) {
 }
 
 namespace {
+constexpr size_t kCkpHeader = 8;  // format, nx, ny, k, tracer flag, 3 spare
+constexpr double kCkpFormat = 1.0;
+// The checkpoint's device arrays in buffer order: seven fields, then the
+// histories D(n-1), D(n-2) of eta, u, v, tracer (slots 1 and 2 after a step).
+void ckp_arrays(sw2g_ctx* x, double* a[15]) {
+  Fp64Buffers& b = x->b;
+  for (int q = 0; q < 7; q++) a[q] = b.f[q];
+  double** h[4] = {b.deta, b.du, b.dv, b.dtr};
+  for (int f = 0; f < 4; f++) {
+    a[7 + 2 * f] = h[f][1];
+    a[8 + 2 * f] = h[f][2];
+  }
+}
+}  // namespace
+
+size_t sw2g_checkpoint_doubles(const sw2g_ctx* x) {
+  if (!x || x->precision != SW2G_FP64) return 0;
+  return kCkpHeader + 15 * (size_t)x->s.W * x->s.H;
+}
+
+sw2g_status sw2g_checkpoint_save(sw2g_ctx* x, double* buf, size_t n) {
+  if (!x || !buf || x->precision != SW2G_FP64 || n != sw2g_checkpoint_doubles(x)) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded || x->open) return SW2G_ERR_STATE;
+  CK(cudaSetDevice(x->device));
+  const size_t S = (size_t)x->s.W * x->s.H;
+  double* a[15];
+  ckp_arrays(x, a);
+  for (int q = 0; q < 15; q++)
+    CK(cudaMemcpyAsync(buf + kCkpHeader + q * S, a[q], S * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  const double head[kCkpHeader] = {kCkpFormat, (double)x->s.nx, (double)x->s.ny, (double)x->k,
+                                   x->tracer_active ? 1.0 : 0.0, 0.0, 0.0, 0.0};
+  std::memcpy(buf, head, sizeof head);
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_checkpoint_load(sw2g_ctx* x, const double* buf, size_t n) {
+  if (!x || !buf || x->precision != SW2G_FP64 || n != sw2g_checkpoint_doubles(x)) return SW2G_ERR_BAD_ARG;
+  if (x->open) return SW2G_ERR_STATE;
+  if (buf[0] != kCkpFormat || buf[1] != (double)x->s.nx || buf[2] != (double)x->s.ny || !(buf[3] >= 0) ||
+      !(buf[3] <= 1e9) || (buf[4] != 0.0 && buf[4] != 1.0))
+    return SW2G_ERR_BAD_ARG;
+  CK(cudaSetDevice(x->device));
+  const size_t S = (size_t)x->s.W * x->s.H;
+  double* a[15];
+  ckp_arrays(x, a);
+  for (int q = 0; q < 15; q++)
+    CK(cudaMemcpyAsync(a[q], buf + kCkpHeader + q * S, S * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  // the plain form of the bodies depends on the winds and the bottom
+  for (int q = 4; q < 7; q++) {
+    bool z = true;
+    const double* f = buf + kCkpHeader + q * S;
+    for (size_t t = 0; t < S && z; t++) {
+      uint64_t bits;
+      std::memcpy(&bits, &f[t], sizeof(bits));
+      z = (bits == 0);
+    }
+    x->aux_zero[q - 4] = z;
+  }
+  x->s.plain = x->aux_zero[0] && x->aux_zero[1] && x->aux_zero[2];
+  x->k = (int)buf[3];
+  x->tracer_active = (buf[4] != 0.0);
+  x->steps = 0;
+  x->err_step = -1;
+  x->uploaded = true;
+  return SW2G_OK;
+}
+
+namespace {
 // Forcing calls are for uploaded FP64 contexts; the staging field is
 // allocated on first use.
 sw2g_status force_ready(sw2g_ctx* x, int which) {

@@ -28,11 +28,13 @@ __device__ __forceinline__ int dexp(double x) {
 // IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook of
 // Floating-Point Arithmetic, ch. "division with an FMA"): q1 is within one
 // ulp of a/b, so r1 = a - b*q1 is exact and RN(q1 + r1*y) = RN(a/b).
-// Numerators outside [2^-900, 2^776] (zeros, subnormals: remainders could
-// underflow) use the IEEE division. The row tables hold y = 1.0/b computed
-// by IEEE division on the host. fp64_check_division compares this with the
-// IEEE quotient on random and near-halfway numerators.
+// A zero numerator gives itself (+-0 / b = +-0 for b > 0); other numerators
+// outside [2^-900, 2^776] (subnormals: remainders could underflow; inf, NaN)
+// use the IEEE division. The row tables hold y = 1.0/b computed by IEEE
+// division on the host. fp64_check_division compares this with the IEEE
+// quotient on random and near-halfway numerators.
 __device__ __forceinline__ double div_rcp(double a, double b, double y) {
+  if ((__double_as_longlong(a) & 0x7fffffffffffffffLL) == 0) return a;
   if ((unsigned)(dexp(a) - 123) > 1799u - 123u) return a / b;
   const double q0 = __dmul_rn(a, y);
   const double r0 = __fma_rn(-b, q0, a);
@@ -270,9 +272,18 @@ __device__ __forceinline__ double limiter_fast(double r) {
 }
 
 
+// n/d for d nonzero, with a zero n answered on the integer pipe: the IEEE
+// quotient of +-0 by d is the zero whose sign is sign(n) xor sign(d).
+__device__ __forceinline__ double div_nz(double n, double d) {
+  const long long nb = __double_as_longlong(n);
+  if ((nb & 0x7fffffffffffffffLL) == 0)
+    return __longlong_as_double((nb ^ __double_as_longlong(d)) & (long long)0x8000000000000000ULL);
+  return n / d;
+}
+
 template <int SCH>
 __device__ __forceinline__ double half_psi(double n, double d) {
-  const double r = nz(d) ? (n / d) : 0.0;  // r2rP / r2rM (calc.c:42-43)
+  const double r = nz(d) ? div_nz(n, d) : 0.0;  // r2rP / r2rM (calc.c:42-43)
   return limiter_fast<SCH>(r) * 0.5;
 }
 
@@ -670,11 +681,11 @@ __global__ void k_hyper_add(DevState s, double* d, const double* l2, const doubl
   INTERIOR_IJ
   const int q = IX(W, i, j);
   double x = d[q];
-  const double* L[3] = {l2, l4, l6};
+  const double V[3] = {l2[q], l4[q], l6[q]};  // all loads issued before any branch
   const double nd[3] = {s.nu2dt, s.nu4dt, s.nu6dt};
 #pragma unroll
   for (int t = 0; t < 3; t++) {
-    const double v = L[t][q];
+    const double v = V[t];
     if ((__double_as_longlong(nd[t]) & 0x7fffffffffffffffLL) != 0) {
       x = x + nd[t] * v;
     } else if (!zero_term_is_exact(x, v)) {

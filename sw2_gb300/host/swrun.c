@@ -2,7 +2,13 @@
  * sw2g-run: runs an SW2 case file on the GPU step, as the reference's
  * executable runs it on one rank:
  *
- *     sw2g-run [--fp32] [--quiet] NPX NPY CASE OUTDIR      (NPX = NPY = 1)
+ *     sw2g-run [--fp32] [--quiet] [--checkpoint] [--resume F] NPX NPY CASE OUTDIR
+ *
+ * (NPX = NPY = 1). --checkpoint writes, next to each frame, an exact-restart
+ * checkpoint (full padded state, Adams-Bashforth histories and index);
+ * --resume F continues from the checkpoint of frame F bit for bit as the
+ * uninterrupted run would (the reference's LoadFrom restarts with an Euler
+ * step from a frame, and departs from it).
  *
  * reads CASE.sw (swcase.c), builds the initial fields of initialize() and
  * loop() (init.c:48-237, core.c:88-131: zero state, zonal wind from the
@@ -18,6 +24,7 @@
  * three phases injects nothing (the reference leaves the rate unset).
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -63,6 +70,88 @@ static int write_frame(const char *outdir, const char *bname, int frame, int nst
   return ok ? 0 : -1;
 }
 
+/* Frames are written by a background thread while the GPU steps on: two sets
+ * of host fields alternate, the step loop fills one while the writer drains
+ * the other, and waits only when the writer is still busy with the set it
+ * needs. */
+typedef struct {
+  pthread_t th;
+  pthread_mutex_t mu;
+  pthread_cond_t cv;
+  int started, pending, quit, failed;
+  const char *outdir, *bname;
+  int frame, nstep, nx, ny;
+  double t;
+  double *f[5];
+} frame_writer;
+
+static void *writer_main(void *arg) {
+  frame_writer *w = (frame_writer *)arg;
+  pthread_mutex_lock(&w->mu);
+  for (;;) {
+    while (!w->pending && !w->quit) pthread_cond_wait(&w->cv, &w->mu);
+    if (!w->pending && w->quit) break;
+    pthread_mutex_unlock(&w->mu);
+    const int rc = write_frame(w->outdir, w->bname, w->frame, w->nstep, w->t, w->nx, w->ny, w->f);
+    pthread_mutex_lock(&w->mu);
+    if (rc) w->failed = 1;
+    w->pending = 0;
+    pthread_cond_broadcast(&w->cv);
+  }
+  pthread_mutex_unlock(&w->mu);
+  return NULL;
+}
+
+static int writer_start(frame_writer *w) {
+  memset(w, 0, sizeof *w);
+  pthread_mutex_init(&w->mu, NULL);
+  pthread_cond_init(&w->cv, NULL);
+  if (pthread_create(&w->th, NULL, writer_main, w)) return -1;
+  w->started = 1;
+  return 0;
+}
+
+/* Waits until the writer is idle; returns -1 if a write failed. */
+static int writer_wait(frame_writer *w) {
+  pthread_mutex_lock(&w->mu);
+  while (w->pending) pthread_cond_wait(&w->cv, &w->mu);
+  const int failed = w->failed;
+  pthread_mutex_unlock(&w->mu);
+  return failed ? -1 : 0;
+}
+
+static int writer_submit(frame_writer *w, const char *outdir, const char *bname, int frame, int nstep, double t,
+                         int nx, int ny, double *const f[5]) {
+  if (writer_wait(w)) return -1;
+  pthread_mutex_lock(&w->mu);
+  w->outdir = outdir;
+  w->bname = bname;
+  w->frame = frame;
+  w->nstep = nstep;
+  w->t = t;
+  w->nx = nx;
+  w->ny = ny;
+  for (int k = 0; k < 5; k++) w->f[k] = f[k];
+  w->pending = 1;
+  pthread_cond_broadcast(&w->cv);
+  pthread_mutex_unlock(&w->mu);
+  return 0;
+}
+
+static int writer_stop(frame_writer *w) {
+  if (!w->started) return 0;
+  const int rc = writer_wait(w);
+  pthread_mutex_lock(&w->mu);
+  w->quit = 1;
+  pthread_cond_broadcast(&w->cv);
+  pthread_mutex_unlock(&w->mu);
+  pthread_join(w->th, NULL);
+  pthread_mutex_destroy(&w->mu);
+  pthread_cond_destroy(&w->cv);
+  w->started = 0;
+  return rc;
+}
+
 /* load_binary_sw (io.c:115-171): fields eta, u, v, tracer, perturbs (tracer
  * absent in MAGICSW1 frames); returns 1 if the file does not exist. */
 static int read_frame(const char *outdir, const char *bname, int frame, int nx, int ny, int *nstep, double *t,
@@ -91,6 +180,64 @@ static int read_frame(const char *outdir, const char *bname, int frame, int nx, 
   fclose(fi);
   if (!ok) fprintf(stderr, "sw2g-run: %s is truncated\n", path);
   return ok ? 0 : -1;
+}
+
+/* Exact-restart checkpoint next to a frame: "<case>.NNNN.ckp" holds the int
+ * 0x43325753 ("SW2C"), the step number, t, the length n of the library's
+ * checkpoint buffer (sw2g_checkpoint_save) as a 64-bit count, and the buffer. */
+#define MAGIC_CKP 0x43325753
+static int write_checkpoint(const char *outdir, const char *bname, int frame, int nstep, double t, sw2g_ctx *g) {
+  const size_t n = sw2g_checkpoint_doubles(g);
+  double *buf = (double *)malloc(n * sizeof(double));
+  if (!buf) {
+    fprintf(stderr, "sw2g-run: out of host memory for the checkpoint\n");
+    return -1;
+  }
+  const sw2g_status st = sw2g_checkpoint_save(g, buf, n);
+  if (st != SW2G_OK) {
+    fprintf(stderr, "sw2g-run: checkpoint: %s\n", sw2g_status_string(st));
+    free(buf);
+    return -1;
+  }
+  char path[4096];
+  snprintf(path, sizeof path, "%s/%s.%04d.ckp", outdir, base_name(bname), frame);
+  FILE *fo = fopen(path, "wb");
+  int ok = fo != NULL;
+  const int magic = MAGIC_CKP;
+  const unsigned long long nn = n;
+  ok = ok && fwrite(&magic, sizeof(int), 1, fo) == 1 && fwrite(&nstep, sizeof(int), 1, fo) == 1 &&
+       fwrite(&t, sizeof(double), 1, fo) == 1 && fwrite(&nn, sizeof nn, 1, fo) == 1 &&
+       fwrite(buf, sizeof(double), n, fo) == n;
+  if (fo) fclose(fo);
+  free(buf);
+  if (!ok) fprintf(stderr, "sw2g-run: cannot write %s\n", path);
+  return ok ? 0 : -1;
+}
+
+static int read_checkpoint(const char *outdir, const char *bname, int frame, int *nstep, double *t, sw2g_ctx *g) {
+  char path[4096];
+  snprintf(path, sizeof path, "%s/%s.%04d.ckp", outdir, base_name(bname), frame);
+  FILE *fi = fopen(path, "rb");
+  if (!fi) {
+    fprintf(stderr, "sw2g-run: checkpoint %s not found\n", path);
+    return -1;
+  }
+  const size_t n = sw2g_checkpoint_doubles(g);
+  double *buf = (double *)malloc(n * sizeof(double));
+  int magic = 0;
+  unsigned long long nn = 0;
+  int ok = buf && fread(&magic, sizeof(int), 1, fi) == 1 && magic == MAGIC_CKP &&
+           fread(nstep, sizeof(int), 1, fi) == 1 && fread(t, sizeof(double), 1, fi) == 1 &&
+           fread(&nn, sizeof nn, 1, fi) == 1 && nn == n && fread(buf, sizeof(double), n, fi) == n;
+  fclose(fi);
+  sw2g_status st = SW2G_OK;
+  if (ok) st = sw2g_checkpoint_load(g, buf, n);
+  free(buf);
+  if (!ok || st != SW2G_OK) {
+    fprintf(stderr, "sw2g-run: %s is not a checkpoint of this case\n", path);
+    return -1;
+  }
+  return 0;
 }
 
 static int ck(sw2g_status st, const char *what) {
@@ -143,7 +290,7 @@ static int print_energy(sw2g_ctx *g, double t) {
   return 0;
 }
 
-int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
+int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, int checkpoint, int resume) {
   char err[512] = {0}, path[4096];
   snprintf(path, sizeof path, "%s.sw", bname);
   swcase c;
@@ -155,6 +302,10 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
   sw2g_ctx *g = NULL;
   swforce w = {0};
   double *f[5] = {NULL, NULL, NULL, NULL, NULL}, *windx = NULL, *windy = NULL, *zero = NULL;
+  double *f2[5] = {NULL, NULL, NULL, NULL, NULL};
+  frame_writer wr;
+  memset(&wr, 0, sizeof wr);
+  int set = 0;  /* the host frame set the loop fills next */
   if (c.polar != 0 && (c.num_gaussians || c.num_vortices)) {
     fprintf(stderr, "sw2g-run: forcing on a polar cap is not supported\n");
     goto done;
@@ -164,10 +315,19 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
     fprintf(stderr, "sw2g-run: the FP32 form runs cases without forcing and without nu6\n");
     goto done;
   }
+  if (fp32 && (checkpoint || resume >= 0)) {
+    fprintf(stderr, "sw2g-run: checkpoints are written and read by the FP64 step only\n");
+    goto done;
+  }
   mkdir(outdir, 0775);
   const int nx = c.nx, ny = c.ny;
   const size_t S = (size_t)(nx + 4) * (ny + 4);
   for (int k = 0; k < 5; k++) f[k] = (double *)calloc(S, sizeof(double));
+  for (int k = 0; k < 5; k++) f2[k] = (double *)calloc(S, sizeof(double));
+  if (!f2[0] || !f2[1] || !f2[2] || !f2[3] || !f2[4] || writer_start(&wr)) {
+    fprintf(stderr, "sw2g-run: out of host memory\n");
+    goto done;
+  }
   windx = (double *)calloc(S, sizeof(double));
   zero = (double *)calloc(S, sizeof(double));
   if (!f[0] || !f[1] || !f[2] || !f[3] || !f[4] || !windx || !zero || swforce_init(&w, nx, ny)) {
@@ -210,7 +370,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
   const double Dt = c.Dt;
   double t = c.t0;
   /* forcing at t0 and the wall fixes (core.c:96-101) */
-  if (!fp32) {
+  if (!fp32 && resume < 0) {
     if (apply_forcing(&c, g, &w, Dt, t, err, sizeof err)) {
       if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
       goto done;
@@ -218,7 +378,10 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
     if (ck(sw2g_apply_channel(g), "channel")) goto done;
   }
   int frame = 0, nstart = 0;
-  if (c.loadFrom != 0) {  /* core.c:115-118 */
+  if (resume >= 0) {  /* exact restart from this runner's own checkpoint */
+    frame = resume;
+    if (read_checkpoint(outdir, bname, frame, &nstart, &t, g)) goto done;
+  } else if (c.loadFrom != 0) {  /* core.c:115-118 */
     frame = c.loadFrom;
     int ns = 0;
     const int lr = read_frame(outdir, bname, frame, nx, ny, &ns, &t, f);
@@ -278,9 +441,13 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
     const int m = n - 1;  /* the step just finished */
     if (!forced) memset(w.perturbs, 0, S * sizeof(double));  /* core.c:292 */
     if (m % c.saveEvery == 0) {  /* core.c:315-320 */
-      if (ck(sw2g_download(g, f[0], f[1], f[2], f[3]), "download")) goto done;
-      memcpy(f[4], w.perturbs, S * sizeof(double));
-      if (write_frame(outdir, bname, frame, m, t, nx, ny, f)) goto done;
+      /* the writer holds at most the other set: submitting it waited for this one */
+      double *const *fs = set ? f2 : f;
+      if (ck(sw2g_download(g, fs[0], fs[1], fs[2], fs[3]), "download")) goto done;
+      memcpy(fs[4], w.perturbs, S * sizeof(double));
+      if (writer_submit(&wr, outdir, bname, frame, m, t, nx, ny, fs)) goto done;
+      set ^= 1;
+      if (checkpoint && write_checkpoint(outdir, bname, frame, m, t, g)) goto done;
       frame++;
     }
     if (m == nstart || m % c.IteInfo == 0) {  /* core.c:136, 329-332 */
@@ -289,9 +456,11 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet) {
   }
   rc = 0;
 done:
+  if (writer_stop(&wr) && rc == 0) rc = 1;
   if (g) sw2g_destroy(g);
   swforce_free(&w);
   for (int k = 0; k < 5; k++) free(f[k]);
+  for (int k = 0; k < 5; k++) free(f2[k]);
   free(windx);
   free(windy);
   free(zero);

@@ -31,7 +31,8 @@ SYMBOLS = [
     "sw2g_diag", "sw2g_reset_ab", "sw2g_steps_done", "sw2g_device_field", "sw2g_stream", "sw2g_last_launches",
     "sw2g_destroy", "sw2g_last_step_ms", "sw2g_timers_enable", "sw2g_timers_reset", "sw2g_timers_count",
     "sw2g_timer_read", "sw2g_selfcheck_division", "sw2g_add_field", "sw2g_set_field_where",
-    "sw2g_apply_channel", "sw2g_step_open", "sw2g_step_close",
+    "sw2g_apply_channel", "sw2g_step_open", "sw2g_step_close", "sw2g_checkpoint_doubles",
+    "sw2g_checkpoint_save", "sw2g_checkpoint_load",
 ]
 
 
@@ -202,6 +203,26 @@ class Solver:
 
     def reset_ab(self):
         self._check(load().sw2g_reset_ab(self.h), "sw2g_reset_ab")
+
+    def checkpoint(self) -> np.ndarray:
+        """Exact-restart checkpoint (FP64 contexts): header, seven padded
+        fields, the Adams-Bashforth histories."""
+        L = load()
+        L.sw2g_checkpoint_doubles.restype = ctypes.c_size_t
+        L.sw2g_checkpoint_doubles.argtypes = [ctypes.c_void_p]
+        L.sw2g_checkpoint_save.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t]
+        n = L.sw2g_checkpoint_doubles(self.h)
+        if n == 0:
+            raise ValueError("checkpoints are for FP64 contexts")
+        buf = np.empty(n, dtype=np.float64)
+        self._check(L.sw2g_checkpoint_save(self.h, _ptr(buf), n), "sw2g_checkpoint_save")
+        return buf
+
+    def restore(self, buf):
+        L = load()
+        L.sw2g_checkpoint_load.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_size_t]
+        b = np.ascontiguousarray(buf, dtype=np.float64)
+        self._check(L.sw2g_checkpoint_load(self.h, _ptr(b), b.size), "sw2g_checkpoint_load")
 
     def last_step_ms(self) -> float:
         return load().sw2g_last_step_ms(self.h)

@@ -259,3 +259,40 @@ def test_gpu_eta_hyperviscosity_of_eta():
     d.load(case.fields())
     d.step(30)
     assert not np.array_equal(got["eta"], d.field("eta"))
+
+
+@pytest.mark.parametrize("winds", [False, True])
+def test_gpu_checkpoint_restart_is_exact(winds):
+    """A checkpoint taken mid-run and loaded into a fresh context continues bit
+    for bit as the uninterrupted run (every padded cell), unlike the
+    reference's frame restart, whose Euler step departs from it."""
+    wind = None
+    if winds:
+        lat = np.arange(-180.0, 181.0)
+        wind = np.stack([lat, 20 * np.cos(np.deg2rad(lat) * 3)], axis=1)
+    case = cases.make_case(nx=48, ny=24, sch=1, seed=13, tracer=winds, TracerDis=2e-6, wind=wind)
+    a = lib.Solver(case.params)
+    a.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    assert a.step(9) == lib.OK
+    buf = a.checkpoint()
+    assert a.step(11) == lib.OK
+    want = a.download()
+    b = lib.Solver(case.params)
+    b.restore(buf)
+    assert b.step(11) == lib.OK
+    got = b.download()
+    for k in FIELDS:
+        assert np.array_equal(got[k], want[k]), k
+    # a frame restart (interior, Euler step) differs
+    c = lib.Solver(case.params)
+    first = lib.Solver(case.params)
+    first.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    first.step(9)
+    mid = first.download()
+    c.upload(mid["eta"], mid["u"], mid["v"], mid["tracer"], *case.fields()[4:], mode=lib.UPLOAD_FRAME)
+    c.step(11)
+    assert not np.array_equal(c.download()["u"], want["u"])
+    # a checkpoint of another grid is refused
+    other = lib.Solver(cases.make_case(nx=40, ny=24, sch=1, seed=13).params)
+    with pytest.raises(lib.SW2GError):
+        other.restore(np.concatenate([buf[:8], np.zeros(15 * 44 * 28)]))

@@ -16,6 +16,7 @@ the reference executable on the same case files (tests/golden):
 """
 import hashlib
 import os
+import shutil
 import subprocess
 
 import numpy as np
@@ -27,20 +28,16 @@ from tests import golden_cases as gc
 pytestmark = pytest.mark.gpu
 
 
-def run(workdir, name, args=()):
-    r = subprocess.run([hostlib.RUNNER, "--quiet", *args, "1", "1", name, "out"], cwd=workdir, capture_output=True,
-                       text=True, timeout=900)
+def run(workdir, name, args=(), flags=()):
+    r = subprocess.run([hostlib.RUNNER, "--quiet", *flags, *args, "1", "1", name, "out"], cwd=workdir,
+                       capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     energy = [ln.split(None, 1)[1].strip() for ln in r.stdout.splitlines() if ln.startswith("ENERGY")]
     frames = {}
-    k = 0
-    while True:
-        path = os.path.join(workdir, "out", f"{name}.{k:04d}.bin")
-        if os.path.exists(path):
-            frames[k] = formats.read_frame(path)
-        elif k > 1:
-            break
-        k += 1
+    pre, post = f"{name}.", ".bin"
+    for fn in os.listdir(os.path.join(workdir, "out")):
+        if fn.startswith(pre) and fn.endswith(post) and fn[len(pre):-len(post)].isdigit():
+            frames[int(fn[len(pre):-len(post)])] = formats.read_frame(os.path.join(workdir, "out", fn))
     return energy, frames
 
 
@@ -109,6 +106,29 @@ def test_restart_cases_match_the_reference(tmp_path, name):
     assert len(energy) == len(printed)
     for a, b in zip(energy, printed):
         assert same_energy(a, "%e %e %e %e" % tuple(b)), (a, b)
+
+
+def test_checkpoint_resume_continues_exactly(tmp_path):
+    """--checkpoint writes an exact-restart file beside each frame; --resume F
+    continues from it and writes the uninterrupted run's later frames bit for
+    bit (with its Gaussian injections and vortices on the way)."""
+    name = FULL[-1]
+    p = gc.forcing_params(name)
+    a, b = tmp_path / "a", tmp_path / "b"
+    for d in (a, b):
+        os.makedirs(d / "out")
+        formats.write_sw(str(d / f"{name}.sw"), p)
+    _, full = run(a, name, flags=("--checkpoint",))
+    last = max(full)
+    assert last >= 3
+    k = last // 2
+    shutil.copy(a / "out" / f"{name}.{k:04d}.ckp", b / "out")
+    _, tail = run(b, name, flags=("--resume", str(k)))
+    assert sorted(tail) == list(range(k + 1, last + 1))
+    for q in tail:
+        assert tail[q][:2] == full[q][:2]
+        for f in ("eta", "u", "v", "tracer", "perturbs"):
+            assert np.array_equal(tail[q][4][f], full[q][4][f]), (q, f)
 
 
 def test_known_answer_file(tmp_path):
