@@ -61,13 +61,21 @@ __device__ __forceinline__ void fill_rows(const KP& p, int j0, RowCache& sq) {
   }
 }
 
+// The bit pattern of a double through an opaque move, so that tests on it
+// stay integer operations instead of being turned back into FP64 compares.
+__device__ __forceinline__ long long dbits(double x) {
+  long long r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
+}
+
 // FP64 <-> FP32 conversions on the integer pipe. On GB300 the hardware
 // conversions issue on the FP64 unit, whose throughput (~1/64 of FP32) would
 // otherwise bound these kernels; here only the state additions use it.
 // d2f: round to nearest (ties away), magnitudes below 2^-126 flush to zero,
 // overflow gives inf, NaN stays NaN.
 __device__ __forceinline__ float d2f(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long b = (unsigned long long)dbits(x);
   const unsigned long long mag = b & 0x7fffffffffffffffULL;
   const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
   unsigned r;
@@ -93,7 +101,7 @@ __device__ __forceinline__ double f2d(float f) {
 // |x| <= 1e10 and not NaN, tested on the bits (the reference's range check,
 // sppde_core.c:386-395, without an FP64 compare).
 __device__ __forceinline__ bool in_range(double x) {
-  const unsigned long long mag = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  const unsigned long long mag = (unsigned long long)dbits(x) & 0x7fffffffffffffffULL;
   return mag <= 0x4202a05f20000000ULL;  // bits of 1e10
 }
 

@@ -19,8 +19,18 @@ __device__ __forceinline__ double RW(const DevState& s, int t, int j) { return s
 // A field of a polar cap at padded index q.
 __device__ __forceinline__ double PF(const DevState& s, int t, int q) { return s.pf[(size_t)t * s.W * s.H + q]; }
 
+// The bit pattern of a double, through an opaque move: tests written on the
+// integer image (sign, exponent, zero) then stay integer operations; given
+// the plain reinterpretation, the compiler may turn them back into FP64
+// comparisons, which issue on GB300's narrow FP64 unit.
+__device__ __forceinline__ long long dbits(double x) {
+  long long r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
+}
+
 __device__ __forceinline__ int dexp(double x) {
-  return (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffULL);
+  return (int)(((unsigned long long)dbits(x) >> 52) & 0x7ffULL);
 }
 
 // Correctly rounded a/b given y = RN(1/b), b a positive normal number, with
@@ -34,7 +44,7 @@ __device__ __forceinline__ int dexp(double x) {
 // division on the host. fp64_check_division compares this with the IEEE
 // quotient on random and near-halfway numerators.
 __device__ __forceinline__ double div_rcp(double a, double b, double y) {
-  if ((__double_as_longlong(a) & 0x7fffffffffffffffLL) == 0) return a;
+  if ((dbits(a) & 0x7fffffffffffffffLL) == 0) return a;
   if ((unsigned)(dexp(a) - 123) > 1799u - 123u) return a / b;
   const double q0 = __dmul_rn(a, y);
   const double r0 = __fma_rn(-b, q0, a);
@@ -249,11 +259,11 @@ constexpr unsigned FULL = 0xffffffffu;
 // a zero, which cannot reach a nonzero sum (see above), and non-finite inputs
 // are recomputed literally.
 __device__ __forceinline__ long long key(double x) {  // order-preserving integer image
-  const long long b = __double_as_longlong(x);
+  const long long b = dbits(x);
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
 }
-__device__ __forceinline__ bool nz(double x) { return (__double_as_longlong(x) & 0x7fffffffffffffffLL) != 0; }
-__device__ __forceinline__ bool gt0(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool nz(double x) { return (dbits(x) & 0x7fffffffffffffffLL) != 0; }
+__device__ __forceinline__ bool gt0(double x) { return dbits(x) > 0; }
 __device__ __forceinline__ bool lt0(double x) { return key(x) < -1; }
 __device__ __forceinline__ double mn(double a, double b) { return key(a) < key(b) ? a : b; }  // sw.h MIN
 __device__ __forceinline__ double mx(double a, double b) { return key(a) > key(b) ? a : b; }  // sw.h MAX
@@ -267,7 +277,7 @@ __device__ __forceinline__ double limiter_fast(double r) {
   else if constexpr (SCH == 4) return mx(0.0, mn(2.0 * r, mn((1 + 2.0 * r) / 3.0, 2.0)));
   else if constexpr (SCH == 7) return mx(0.0, mn(mn(2.0, 2.0 * r), mn(0.25 + 0.75 * r, 0.75 + 0.25 * r)));
   else if constexpr (SCH == kVanLeerSafe)
-    return (__double_as_longlong(r) == __double_as_longlong(-1.0)) ? 0.0 : (r + fabs(r)) / (1.0 + r);
+    return (dbits(r) == dbits(-1.0)) ? 0.0 : (r + fabs(r)) / (1.0 + r);
   else return limiter<SCH>(r);
 }
 
@@ -275,9 +285,9 @@ __device__ __forceinline__ double limiter_fast(double r) {
 // n/d for d nonzero, with a zero n answered on the integer pipe: the IEEE
 // quotient of +-0 by d is the zero whose sign is sign(n) xor sign(d).
 __device__ __forceinline__ double div_nz(double n, double d) {
-  const long long nb = __double_as_longlong(n);
+  const long long nb = dbits(n);
   if ((nb & 0x7fffffffffffffffLL) == 0)
-    return __longlong_as_double((nb ^ __double_as_longlong(d)) & (long long)0x8000000000000000ULL);
+    return __longlong_as_double((nb ^ dbits(d)) & (long long)0x8000000000000000ULL);
   return n / d;
 }
 
@@ -613,7 +623,7 @@ __global__ void k_check_division(const double* div, int n, long long samples, un
       a = __dmul_rn(b, q + h);
     }
     const double want = a / b, got = div_rcp(a, b, y);
-    if (__double_as_longlong(want) != __double_as_longlong(got)) miss++;
+    if (dbits(want) != dbits(got)) miss++;
   }
   if (miss) atomicAdd(bad, miss);
 }
@@ -671,7 +681,7 @@ __global__ void k_lape_fix(int nx, int ny, double* eo) {
 // zero to a finite nonzero x gives x; only a zero x (the sign of the sum) or a
 // non-finite operand needs that term's arithmetic.
 __device__ __forceinline__ bool zero_term_is_exact(double x, double L) {
-  const long long xb = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  const long long xb = dbits(x) & 0x7fffffffffffffffLL;
   return xb != 0 && xb < 0x7ff0000000000000LL && dexp(L) != 0x7ff;
 }
 // Out of line, so that the rare case is a branch and not predicated FP64 work.
@@ -686,7 +696,7 @@ __global__ void k_hyper_add(DevState s, double* d, const double* l2, const doubl
 #pragma unroll
   for (int t = 0; t < 3; t++) {
     const double v = V[t];
-    if ((__double_as_longlong(nd[t]) & 0x7fffffffffffffffLL) != 0) {
+    if ((dbits(nd[t]) & 0x7fffffffffffffffLL) != 0) {
       x = x + nd[t] * v;
     } else if (!zero_term_is_exact(x, v)) {
       x = add_product(x, nd[t], v);
@@ -829,7 +839,7 @@ __global__ void k_channel(int nx, int ny, double* u, double* v, double* wx, doub
 // magnitude: the magnitudes are compared as integers (NaNs set to 0) and each
 // warp divides once.
 __device__ __forceinline__ long long mag_bits(double x) {
-  const long long m = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  const long long m = dbits(x) & 0x7fffffffffffffffLL;
   return (m > 0x7ff0000000000000LL) ? 0 : m;
 }
 // One block per row: the row's largest magnitudes, then its two quotients and
@@ -870,8 +880,8 @@ __global__ void __launch_bounds__(CFL_T) k_cfl(DevState s, F7 f, unsigned long l
     }
     const double mx = div_rcp(__longlong_as_double(bx), RW(s, R_DXE, j), RW(s, R_IDXE, j));
     const double my = div_rcp(__longlong_as_double(by), RW(s, R_DYN, j), RW(s, R_IDYN, j));
-    if (mx > 0) atomicMax(out, (unsigned long long)__double_as_longlong(mx));
-    if (my > 0) atomicMax(out + 1, (unsigned long long)__double_as_longlong(my));
+    if (mx > 0) atomicMax(out, (unsigned long long)dbits(mx));
+    if (my > 0) atomicMax(out + 1, (unsigned long long)dbits(my));
   }
 }
 
@@ -880,7 +890,7 @@ __global__ void __launch_bounds__(CFL_T) k_cfl(DevState s, F7 f, unsigned long l
 // aborts iff the first value is not finite or some value lies outside +-1e10.
 // Tested on the bits (|x| > 1e10 and not NaN), for up to four fields at once.
 __device__ __forceinline__ bool range_bad(double x, bool first) {
-  const long long m = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  const long long m = dbits(x) & 0x7fffffffffffffffLL;
   if (first) return m > 0x4202a05f20000000LL;  // beyond 1e10, inf or NaN
   return m > 0x4202a05f20000000LL && m <= 0x7ff0000000000000LL;
 }
