@@ -51,8 +51,9 @@ KERNEL_BYTES = {
     "adv_v": 8 * (2 + 1),       # u v -> Dv_adv
     "pres_sum": 8 * (5 + 2),    # eta u v Du_adv Dv_adv -> Du_n Dv_n
     "ab": 8 * (3 + 1),
-    "coriolis_u": 8 * (3 + 1),
-    "coriolis_v": 8 * (3 + 1),
+    "coriolis_u": 8 * (6 + 2),  # from the third step: u v, D_n D_n-1 D_n-2, nu4 L -> D_n u (AB3 fused)
+    "coriolis_v": 8 * (6 + 2),
+    "eta_ab3": 8 * (6 + 2),     # eta v, D_n D_n-1 D_n-2, nu4 L -> D_n eta (hyper, AB3, geofactor, update)
     "lape_pass1": 8 * (1 + 2),
     "lape_pass2": 8 * (2 + 1),
     "lapv_pass1": 8 * (2 + 2),

@@ -348,6 +348,50 @@ __device__ __forceinline__ void face_terms(const Face& F, double Dt, double dx, 
 }
 #define ROW2(t, it, j) RW(s, t, j), RW(s, it, j)
 
+// calc.c:100 over the four faces: +wP +wM -eP -eM +sP +sM -nP -nM. The term
+// of an unused side is a +0 placeholder; leaving it out changes only the sign
+// of a zero sum, which the literal path recomputes. Unless a face of the
+// warp's cells uses both sides, each face has one term (the side in use) and
+// the sum takes three additions; otherwise all eight terms are summed, out of
+// line so that the common case does not carry the extra FP64 operations.
+__device__ __noinline__ double sum_faces8(double wP, double wM, double eP, double eM, double sP, double sM,
+                                          double nP, double nM) {
+  double S = wP + wM;
+  S = S - eP;
+  S = S - eM;
+  S = S + sP;
+  S = S + sM;
+  S = S - nP;
+  S = S - nM;
+  return S;
+}
+struct Side {  // a face's terms as seen by one cell, and which side is in use
+  double P, M;
+  bool pos, both;
+};
+__device__ __forceinline__ double sum_faces(const Side& w, const Side& e, const Side& so, const Side& n) {
+  if (__any_sync(FULL, w.both || e.both || so.both || n.both))
+    return sum_faces8(w.P, w.M, e.P, e.M, so.P, so.M, n.P, n.M);
+  const double tw = w.pos ? w.P : w.M, te = e.pos ? e.P : e.M;
+  const double ts = so.pos ? so.P : so.M, tn = n.pos ? n.P : n.M;
+  return ((tw - te) + ts) - tn;
+}
+__device__ __forceinline__ Side east_of(const Side& w, int lane) {
+  Side e;
+  e.P = __shfl_sync(FULL, w.P, (lane + 1) & 31);
+  e.M = __shfl_sync(FULL, w.M, (lane + 1) & 31);
+  e.pos = __shfl_sync(FULL, (int)w.pos, (lane + 1) & 31) != 0;
+  e.both = __shfl_sync(FULL, (int)w.both, (lane + 1) & 31) != 0;
+  return e;
+}
+__device__ __forceinline__ Side side_of(const Face& F, double Dt, double dx, double idx) {
+  Side t;
+  face_terms(F, Dt, dx, idx, t.P, t.M);
+  t.pos = F.pos1;
+  t.both = F.both;
+  return t;
+}
+
 // Upwind halves of one velocity: 0.5(a+|a|) and 0.5(a-|a|) up to the sign of a zero.
 __device__ __forceinline__ double up_p(double a) { return gt0(a) ? a : 0.0; }
 __device__ __forceinline__ double up_m(double a) { return lt0(a) ? a : 0.0; }
@@ -396,19 +440,21 @@ __device__ __forceinline__ XN x_neighbours(double v, double aux, int lane) {
 #define HF(i, j) (PL ? (f.eta[IX(W, i, j)] + s.depth) : HH(i, j))
 
 // BODYH + damping, fast form.
-template <int SCH, bool PL>
+template <int SCH, bool PL, bool UD>
 __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   const double damp = 2.0 * Dt * (s.sigma);  // calc.c:112: (2.0*Dt*sigma)*ETA
   // H at this lane's column, rows j-1 .. j+1 (window), and the face south of j0
   double h1 = HF(ic, j0 - 1), h2 = HF(ic, j0), h3 = HF(ic, j0 + 1);
-  double tsP, tsM;
+  // UD (no damping: sigma = 0, a band): the product damp*eta is a zero (eta is
+  // finite on the fast path), and a nonzero S minus a zero is S
+  Side ts;
   bool oks;
   {
     const double b = VF(ic, j0 - 1);
     const Face F = make_face<SCH>(HF(ic, j0 - 2), h1, h2, h3, up_p(b), up_m(b), fin(b));
-    face_terms(F, Dt, ROW2(R_DYN, R_IDYN, j0), tsP, tsM);
+    ts = side_of(F, Dt, ROW2(R_DYN, R_IDYN, j0));
     oks = F.ok;
   }
   for (int j = j0; j <= jn; j++) {
@@ -417,34 +463,24 @@ __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, dou
     const XN xn = x_neighbours(h2, HF(ia, j), lane);
     const double a = UF(iu, j);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, h2, xn.p1, up_p(a), up_m(a), fin(a));
-    double twP, twM;
-    face_terms(FX, Dt, ROW2(R_DXE, R_IDXE, j), twP, twM);
-    const double teP = __shfl_sync(FULL, twP, (lane + 1) & 31);
-    const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
+    const Side tw = side_of(FX, Dt, ROW2(R_DXE, R_IDXE, j));
+    const Side te = east_of(tw, lane);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // y face north of row j: shared by this cell and the cell above
     const double b = VF(ic, j);
     const Face FY = make_face<SCH>(h1, h2, h3, h4, up_p(b), up_m(b), fin(b));
-    double tnP, tnM, nsP, nsM;
-    face_terms(FY, Dt, ROW2(R_DYN, R_IDYN, j), tnP, tnM);
-    face_terms(FY, Dt, ROW2(R_DYN, R_IDYN, j + 1), nsP, nsM);
-    // calc.c:100 in its order: +w -e +s -n
-    double S = twP + twM;
-    S = S - teP;
-    S = S - teM;
-    S = S + tsP;
-    S = S + tsM;
-    S = S - tnP;
-    S = S - tnM;
+    const Side tn = side_of(FY, Dt, ROW2(R_DYN, R_IDYN, j));
+    const Side ns = side_of(FY, Dt, ROW2(R_DYN, R_IDYN, j + 1));
+    const double S = sum_faces(tw, te, ts, tn);  // calc.c:100 in its order: +w -e +s -n
     const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
     if (own) {
       double r;
       if (slow) r = mass_cell_ool<SCH>(s, f, i, j);
+      else if (UD) r = S;
       else r = S - (s.polar ? 2.0 * Dt * PF(s, P_SH, IX(W, i, j)) : damp) * f.eta[IX(W, i, j)];
       out[IX(W, i, j)] = r;
     }
-    tsP = nsP;
-    tsM = nsM;
+    ts = ns;
     oks = FY.ok;
     h1 = h2;
     h2 = h3;
@@ -461,40 +497,33 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, do
   // U at this lane's column, rows j-1 .. j+1, and V at columns i, i+1 of row j-1
   double u1 = UF(ic, j0 - 1), u2 = UF(ic, j0), u3 = UF(ic, j0 + 1);
   double vs0 = VF(ic, j0 - 1), vs1 = VF(ic1, j0 - 1);
-  double tsP, tsM;
+  Side ts;
   bool oks;
   {
     const Face F = make_face<SCH>(UF(ic, j0 - 2), u1, u2, u3, 0.5 * (up_p(vs0) + up_p(vs1)),
                                   0.5 * (up_m(vs0) + up_m(vs1)), fin(vs0) && fin(vs1));
-    face_terms(F, Dt, ROW2(R_DYV, R_IDYV, j0), tsP, tsM);
+    ts = side_of(F, Dt, ROW2(R_DYV, R_IDYV, j0));
     oks = F.ok;
   }
+  double vsh = (vs0 + vs1) / 2.;  // calc.c:198, carried from the row below
   for (int j = j0; j <= jn; j++) {
     const double u4 = UF(ic, j + 2);
     // x face west of column i, row j: velocities u(i-1), u(i)
     const XN xn = x_neighbours(u2, UF(ia, j), lane);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, u2, xn.p1, 0.5 * (up_p(xn.m1) + up_p(u2)),
                                    0.5 * (up_m(xn.m1) + up_m(u2)), true);
-    double twP, twM;
-    face_terms(FX, Dt, ROW2(R_DXC, R_IDXC, j), twP, twM);
-    const double teP = __shfl_sync(FULL, twP, (lane + 1) & 31);
-    const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
+    const Side tw = side_of(FX, Dt, ROW2(R_DXC, R_IDXC, j));
+    const Side te = east_of(tw, lane);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // y face north of row j: velocities v(i, j), v(i+1, j)
     const double vn0 = VF(ic, j), vn1 = VF(ic1, j);
     const Face FY = make_face<SCH>(u1, u2, u3, u4, 0.5 * (up_p(vn0) + up_p(vn1)), 0.5 * (up_m(vn0) + up_m(vn1)),
                                    fin(vn0) && fin(vn1));
-    double tnP, tnM, nsP, nsM;
-    face_terms(FY, Dt, ROW2(R_DYV, R_IDYV, j), tnP, tnM);
-    face_terms(FY, Dt, ROW2(R_DYV, R_IDYV, j + 1), nsP, nsM);
-    double S = twP + twM;
-    S = S - teP;
-    S = S - teM;
-    S = S + tsP;
-    S = S + tsM;
-    S = S - tnP;
-    S = S - tnM;
+    const Side tn = side_of(FY, Dt, ROW2(R_DYV, R_IDYV, j));
+    const Side ns = side_of(FY, Dt, ROW2(R_DYV, R_IDYV, j + 1));
+    const double S = sum_faces(tw, te, ts, tn);
     const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
+    const double vnh = (vn0 + vn1) / 2.;
     if (own) {
       double r;
       if (slow) {
@@ -502,16 +531,14 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, do
       } else {
         const double uwm = xn.m1, u0 = u2, uep = xn.p1;  // calc.c:198
         const double p2 = Dt * (div_rcp(u0 * (uep - uwm), ROW2(R_DXE2, R_IDXE2, j)) +
-                                div_rcp(u0 * ((vn0 + vn1) / 2. - (vs0 + vs1) / 2.), ROW2(R_DYV, R_IDYV, j)));
+                                div_rcp(u0 * (vnh - vsh), ROW2(R_DYV, R_IDYV, j)));
         r = S + p2;
       }
       out[IX(W, i, j)] = r;
     }
-    tsP = nsP;
-    tsM = nsM;
+    ts = ns;
     oks = FY.ok;
-    vs0 = vn0;
-    vs1 = vn1;
+    vsh = vnh;
     u1 = u2;
     u2 = u3;
     u3 = u4;
@@ -527,12 +554,12 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, do
   // V at this lane's column, rows j-1 .. j+1; U at column i-1, row j
   double v1 = VF(ic, j0 - 1), v2 = VF(ic, j0), v3 = VF(ic, j0 + 1);
   double uw0 = UF(iu, j0);
-  double tsP, tsM;
+  Side ts;
   bool oks;
   {
     const Face F = make_face<SCH>(VF(ic, j0 - 2), v1, v2, v3, 0.5 * (up_p(v1) + up_p(v2)),
                                   0.5 * (up_m(v1) + up_m(v2)), true);
-    face_terms(F, Dt, ROW2(R_DYC, R_IDYC, j0), tsP, tsM);
+    ts = side_of(F, Dt, ROW2(R_DYC, R_IDYC, j0));
     oks = F.ok;
   }
   for (int j = j0; j <= jn; j++) {
@@ -542,25 +569,17 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, do
     const XN xn = x_neighbours(v2, VF(ia, j), lane);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, v2, xn.p1, 0.5 * (up_p(uw1) + up_p(uw0)),
                                    0.5 * (up_m(uw1) + up_m(uw0)), fin(uw1) && fin(uw0));
-    double twP, twM;
-    face_terms(FX, Dt, ROW2(R_DXV, R_IDXV, j), twP, twM);
-    const double teP = __shfl_sync(FULL, twP, (lane + 1) & 31);
-    const double teM = __shfl_sync(FULL, twM, (lane + 1) & 31);
+    const Side tw = side_of(FX, Dt, ROW2(R_DXV, R_IDXV, j));
+    const Side te = east_of(tw, lane);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
-    const double ue0 = __shfl_sync(FULL, uw0, (lane + 1) & 31);  // u(i, j), u(i, j+1)
-    const double ue1 = __shfl_sync(FULL, uw1, (lane + 1) & 31);
+    // (u(i-1, j) + u(i-1, j+1))/2 and, from the next lane, (u(i, j) + u(i, j+1))/2 (calc.c:235)
+    const double uwh = (uw0 + uw1) / 2.;
+    const double ueh = __shfl_sync(FULL, uwh, (lane + 1) & 31);
     // y face north of row j: velocities v(i, j), v(i, j+1)
     const Face FY = make_face<SCH>(v1, v2, v3, v4, 0.5 * (up_p(v2) + up_p(v3)), 0.5 * (up_m(v2) + up_m(v3)), true);
-    double tnP, tnM, nsP, nsM;
-    face_terms(FY, Dt, ROW2(R_DYC, R_IDYC, j), tnP, tnM);
-    face_terms(FY, Dt, ROW2(R_DYC, R_IDYC, j + 1), nsP, nsM);
-    double S = twP + twM;
-    S = S - teP;
-    S = S - teM;
-    S = S + tsP;
-    S = S + tsM;
-    S = S - tnP;
-    S = S - tnM;
+    const Side tn = side_of(FY, Dt, ROW2(R_DYC, R_IDYC, j));
+    const Side ns = side_of(FY, Dt, ROW2(R_DYC, R_IDYC, j + 1));
+    const double S = sum_faces(tw, te, ts, tn);
     const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
     if (own) {
       double r;
@@ -568,14 +587,13 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, do
         r = advv_cell_ool<SCH>(s, f, i, j);
       } else {
         const double vsm = v1, v0 = v2, vnp = v3;  // calc.c:235
-        const double p2 = Dt * (div_rcp(v0 * ((ue0 + ue1) / 2. - (uw0 + uw1) / 2.), ROW2(R_DXV, R_IDXV, j)) +
+        const double p2 = Dt * (div_rcp(v0 * (ueh - uwh), ROW2(R_DXV, R_IDXV, j)) +
                                 div_rcp(v0 * (vnp - vsm), ROW2(R_DYNS, R_IDYNS, j)));
         r = S + p2;
       }
       out[IX(W, i, j)] = r;
     }
-    tsP = nsP;
-    tsM = nsM;
+    ts = ns;
     oks = FY.ok;
     uw0 = uw1;
     v1 = v2;
@@ -687,22 +705,54 @@ __device__ __forceinline__ bool zero_term_is_exact(double x, double L) {
 // Out of line, so that the rare case is a branch and not predicated FP64 work.
 __device__ __noinline__ double add_product(double x, double nd, double v) { return x + nd * v; }
 
+// NZ: bit t set when the order-t coefficient is nonzero (chosen at compile
+// time: a skipped FP64 operation under a predicate still occupies the FP64 unit).
+// NZ = 8: no hyperviscosity block at all (every nu zero: the reference skips it).
+constexpr int kNoHyper = 8;
+template <int NZ>
+__device__ __forceinline__ double hyper_terms(const DevState& s, double x, const double* l2, const double* l4,
+                                              const double* l6, int q) {
+  if constexpr (NZ == kNoHyper) {
+    return x;
+  } else {
+    const double V[3] = {l2[q], l4[q], l6[q]};  // all loads issued before any branch
+    const double nd[3] = {s.nu2dt, s.nu4dt, s.nu6dt};
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+      const double v = V[t];
+      if ((NZ >> t) & 1) x = x + nd[t] * v;
+      else if (!zero_term_is_exact(x, v)) x = add_product(x, nd[t], v);
+    }
+    return x;
+  }
+}
+
+template <int NZ>
 __global__ void k_hyper_add(DevState s, double* d, const double* l2, const double* l4, const double* l6) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
-  double x = d[q];
-  const double V[3] = {l2[q], l4[q], l6[q]};  // all loads issued before any branch
-  const double nd[3] = {s.nu2dt, s.nu4dt, s.nu6dt};
-#pragma unroll
-  for (int t = 0; t < 3; t++) {
-    const double v = V[t];
-    if ((dbits(nd[t]) & 0x7fffffffffffffffLL) != 0) {
-      x = x + nd[t] * v;
-    } else if (!zero_term_is_exact(x, v)) {
-      x = add_product(x, nd[t], v);
-    }
+  d[q] = hyper_terms<NZ>(s, d[q], l2, l4, l6, q);
+}
+
+// The coefficient mask of the hyperviscosity terms (kNoHyper when every nu is zero).
+int hyper_mask(const DevState& s) {
+  if (s.nu2 == 0 && s.nu4 == 0 && s.nu6 == 0) return kNoHyper;
+  return (s.nu2dt != 0.0 ? 1 : 0) | (s.nu4dt != 0.0 ? 2 : 0) | (s.nu6dt != 0.0 ? 4 : 0);
+}
+
+void hyper_add(const DevState& s, dim3 g, cudaStream_t st, double* d, const double* l2, const double* l4,
+               const double* l6) {
+  const int m = (s.nu2dt != 0.0 ? 1 : 0) | (s.nu4dt != 0.0 ? 2 : 0) | (s.nu6dt != 0.0 ? 4 : 0);
+  switch (m) {
+    case 0: k_hyper_add<0><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 1: k_hyper_add<1><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 2: k_hyper_add<2><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 3: k_hyper_add<3><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 4: k_hyper_add<4><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 5: k_hyper_add<5><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 6: k_hyper_add<6><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    default: k_hyper_add<7><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
   }
-  d[q] = x;
 }
 
 // do_eta_geofactor (calc.c:403-422)
@@ -794,13 +844,106 @@ __global__ void k_coriolis_v(DevState s, const double* u, double* v, const doubl
   v[q] = (v[q] + dvab[q] - be * v[q] - al * semi) / (1.0 + be);
 }
 
+// From the third step on (AB3), the tail of each tendency is fused into one
+// kernel per field, with the operations of the separate kernels in their
+// order: the hyperviscosity terms (into the stored tendency), the
+// Adams-Bashforth combination (calc.c:651-699, linop_scaf's two passes) and
+//   eta: the geofactor (calc.c:403-422) and eta += D (core.c:203-205);
+//   u, v: the Coriolis update (calc.c:542-598).
+__device__ __forceinline__ double ab3(double dn, double dm1, double dm2) {
+  const double t = -(4.0 / 3.0) * dm1 + +(5.0 / 12.0) * dm2;
+  return (23.0 / 12.0) * dn + 1.0 * t;
+}
+// v + (+0): v, except that -0 becomes +0 (the plain form's zero winds).
+__device__ __forceinline__ double plus_pos_zero(double v) {
+  return (dbits(v) == (long long)0x8000000000000000ULL) ? 0.0 : v;
+}
+
+template <int NZ, bool PL>
+__global__ void k_eta_ab3(DevState s, F7 f, double* eta, double* dn, const double* dm1, const double* dm2,
+                          const double* l2, const double* l4, const double* l6) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
+  if constexpr (NZ != kNoHyper) dn[q] = x;
+  double ab = ab3(x, dm1[q], dm2[q]);
+  const double e = f.eta[q];
+  if constexpr (PL) {
+    const double h = e + s.depth;  // - hB with hB = +0 is exact
+    ab -= (RW(s, R_GEO, j) * h * 0.5 * (plus_pos_zero(f.v[q]) + plus_pos_zero(f.v[IX(W, i, j - 1)])));
+  } else {
+    ab -= (RW(s, R_GEO, j) * HH(i, j) * 0.5 * (VW(i, j) + VW(i, j - 1)));
+  }
+  eta[q] = e + ab;
+}
+
+template <int NZ>
+__global__ void k_coriolis_u_ab3(DevState s, double* u, const double* v, double* dn, const double* dm1,
+                                 const double* dm2, const double* l2, const double* l4, const double* l6) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
+  if constexpr (NZ != kNoHyper) dn[q] = x;
+  const double duab = ab3(x, dm1[q], dm2[q]);
+  const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
+  const double dtf = s.polar ? s.Dt * PF(s, P_FE, q) : RW(s, R_DTFE, j);
+  const double al = dtf + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
+  const double be = 0.25 * al * al;
+  u[q] = (u[q] + duab - be * u[q] + al * semi) / (1.0 + be);
+}
+
+template <int NZ>
+__global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double* dn, const double* dm1,
+                                 const double* dm2, const double* l2, const double* l4, const double* l6) {
+  INTERIOR_IJ
+  const int q = IX(W, i, j);
+  const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
+  if constexpr (NZ != kNoHyper) dn[q] = x;
+  const double dvab = ab3(x, dm1[q], dm2[q]);
+  const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
+  const double dtf = s.polar ? s.Dt * PF(s, P_FN, q) : RW(s, R_DTFN, j);
+  const double al = dtf + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
+  const double be = 0.25 * al * al;
+  v[q] = (v[q] + dvab - be * v[q] - al * semi) / (1.0 + be);
+}
+
+template <int NZ>
+void fused_tails(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which) {
+  if (which == 0) {
+    if (s.plain)
+      k_eta_ab3<NZ, true><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2]);
+    else
+      k_eta_ab3<NZ, false><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2]);
+  } else if (which == 1) {
+    k_coriolis_u_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.du[0], b.du[1], b.du[2], b.L[0], b.L[2], b.L[4]);
+  } else {
+    k_coriolis_v_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dv[0], b.dv[1], b.dv[2], b.L[1], b.L[3], b.L[5]);
+  }
+}
+// which: 0 eta (hyper + AB3 + geofactor + update), 1 u, 2 v (hyper + AB3 + Coriolis)
+void fused_tail(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which) {
+  switch (hyper_mask(s)) {
+    case 0: fused_tails<0>(s, g, st, f, b, which); break;
+    case 1: fused_tails<1>(s, g, st, f, b, which); break;
+    case 2: fused_tails<2>(s, g, st, f, b, which); break;
+    case 3: fused_tails<3>(s, g, st, f, b, which); break;
+    case 4: fused_tails<4>(s, g, st, f, b, which); break;
+    case 5: fused_tails<5>(s, g, st, f, b, which); break;
+    case 6: fused_tails<6>(s, g, st, f, b, which); break;
+    case 7: fused_tails<7>(s, g, st, f, b, which); break;
+    default: fused_tails<kNoHyper>(s, g, st, f, b, which); break;
+  }
+}
+
 // Single-rank halo update (sppde_hupdate.c:274-342). The y pass then the x pass
 // compose to: every halo cell copies the interior cell (wrapx(i), wrapy(j)).
-__global__ void k_halo(double* x, int nx, int ny) {
+// blockIdx.y selects the field: one launch wraps x and, when given, y.
+__global__ void k_halo(double* x, double* y, int nx, int ny) {
   const int W = nx + 4;
   const int nh = 4 * W + 4 * ny;  // 4 full halo rows + 4 halo columns over interior rows
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nh) return;
+  if (blockIdx.y == 1) x = y;
   int i, j;
   if (t < 4 * W) {
     const int r = t / W;
@@ -930,12 +1073,16 @@ int fast_grid(K kernel, const DevState& s) {
 template <int SCH>
 void launch_bodies(int which, dim3 g, cudaStream_t st, const DevState& s, const F7& f, double* out) {
   if constexpr (SCH != 3) {
+    const bool ud = !s.polar && s.sigma == 0.0;
+    if (s.plain && ud) {
+      if (which == 0) { k_mass_fast<SCH, true, true><<<fast_grid(k_mass_fast<SCH, true, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+    }
     if (s.plain) {
-      if (which == 0) { k_mass_fast<SCH, true><<<fast_grid(k_mass_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 0) { k_mass_fast<SCH, true, false><<<fast_grid(k_mass_fast<SCH, true, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
       if (which == 2) { k_adv_u_fast<SCH, true><<<fast_grid(k_adv_u_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
       if (which == 3) { k_adv_v_fast<SCH, true><<<fast_grid(k_adv_v_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
     } else {
-      if (which == 0) { k_mass_fast<SCH, false><<<fast_grid(k_mass_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 0) { k_mass_fast<SCH, false, false><<<fast_grid(k_mass_fast<SCH, false, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
       if (which == 2) { k_adv_u_fast<SCH, false><<<fast_grid(k_adv_u_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
       if (which == 3) { k_adv_v_fast<SCH, false><<<fast_grid(k_adv_v_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
     }
@@ -1015,7 +1162,12 @@ void fp64_check_division(const double* d_div, int n, long long samples, unsigned
 
 void halo_wrap(double* x, int nx, int ny, cudaStream_t st) {
   const int nh = 4 * (nx + 4) + 4 * ny;
-  k_halo<<<(nh + 255) / 256, 256, 0, st>>>(x, nx, ny);
+  k_halo<<<(nh + 255) / 256, 256, 0, st>>>(x, x, nx, ny);
+}
+// Two fields in one launch.
+void halo_wrap2(double* x, double* y, int nx, int ny, cudaStream_t st) {
+  const int nh = 4 * (nx + 4) + 4 * ny;
+  k_halo<<<dim3((nh + 255) / 256, 2), 256, 0, st>>>(x, y, nx, ny);
 }
 
 // One reference time step; returns the number of kernels launched.
@@ -1070,12 +1222,17 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
       // the wall rows of a band (laplacian.c:131-146); a polar cap is periodic in y and has none
       if (s.polar == 0) LAUNCH("lape_fix", k_lape_fix<<<gw, 128, 0, st>>>(s.nx, s.ny, b.Le[q]));
     }
-    LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
+    if (k < 2) LAUNCH("hyper_add", hyper_add(s, g, st, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
   }
-  LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
-  LAUNCH("geofactor", k_geofactor<<<g, TX, 0, st>>>(s, F(), b.detaAB));
-  rotate3(b.deta);
-  LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[0], b.detaAB));
+  if (k >= 2) {
+    LAUNCH("eta_ab3", fused_tail(s, g, st, F(), b, 0));
+    rotate3(b.deta);
+  } else {
+    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
+    LAUNCH("geofactor", k_geofactor<<<g, TX, 0, st>>>(s, F(), b.detaAB));
+    rotate3(b.deta);
+    LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[0], b.detaAB));
+  }
   LAUNCH("halo", halo_wrap(b.f[0], s.nx, s.ny, st));
 
   // momentum (core.c:212-280)
@@ -1090,29 +1247,36 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
       const double* uu = q == 0 ? b.f[1] : b.L[2 * q - 2];
       const double* vv = q == 0 ? b.f[2] : b.L[2 * q - 1];
       LAUNCH("lapv_pass1", k_lapv_pass1<<<g, TX, 0, st>>>(s, uu, vv, b.ze, b.di));
-      LAUNCH("halo", halo_wrap(b.ze, s.nx, s.ny, st));
-      LAUNCH("halo", halo_wrap(b.di, s.nx, s.ny, st));
+      LAUNCH("halo", halo_wrap2(b.ze, b.di, s.nx, s.ny, st));
       if (s.polar == 0) LAUNCH("lapv_fix1", k_lapv_fix1<<<gw, 128, 0, st>>>(s, uu, b.ze, b.di));
       LAUNCH("lapv_pass2", k_lapv_pass2<<<g, TX, 0, st>>>(s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
-      LAUNCH("halo", halo_wrap(b.L[2 * q], s.nx, s.ny, st));
-      LAUNCH("halo", halo_wrap(b.L[2 * q + 1], s.nx, s.ny, st));
+      LAUNCH("halo", halo_wrap2(b.L[2 * q], b.L[2 * q + 1], s.nx, s.ny, st));
       if (s.polar == 0) LAUNCH("lapv_fix2", k_lapv_fix2<<<gw, 128, 0, st>>>(s.nx, s.ny, b.L[2 * q], b.L[2 * q + 1]));
     }
-    LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.du[0], b.L[0], b.L[2], b.L[4]));
-    LAUNCH("hyper_add", k_hyper_add<<<g, TX, 0, st>>>(s, b.dv[0], b.L[1], b.L[3], b.L[5]));
+    if (k < 2) {
+      LAUNCH("hyper_add", hyper_add(s, g, st, b.du[0], b.L[0], b.L[2], b.L[4]));
+      LAUNCH("hyper_add", hyper_add(s, g, st, b.dv[0], b.L[1], b.L[3], b.L[5]));
+    }
   }
-  LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.duAB, b.du[0], b.du[1], b.du[2]));
-  LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.dvAB, b.dv[0], b.dv[1], b.dv[2]));
-  rotate3(b.du);
-  rotate3(b.dv);
-
-  // Coriolis (core.c:282-285)
-  LAUNCH("coriolis_u", k_coriolis_u<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.duAB));
-  LAUNCH("coriolis_v", k_coriolis_v<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dvAB));
+  if (k >= 2) {
+    // AB3 of u and v folded into the Coriolis updates (core.c:271-285); the v
+    // tendency does not depend on the new u
+    LAUNCH("coriolis_u", fused_tail(s, g, st, F(), b, 1));
+    LAUNCH("coriolis_v", fused_tail(s, g, st, F(), b, 2));
+    rotate3(b.du);
+    rotate3(b.dv);
+  } else {
+    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.duAB, b.du[0], b.du[1], b.du[2]));
+    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.dvAB, b.dv[0], b.dv[1], b.dv[2]));
+    rotate3(b.du);
+    rotate3(b.dv);
+    // Coriolis (core.c:282-285)
+    LAUNCH("coriolis_u", k_coriolis_u<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.duAB));
+    LAUNCH("coriolis_v", k_coriolis_v<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dvAB));
+  }
 
   // halos (core.c:287-290)
-  LAUNCH("halo", halo_wrap(b.f[1], s.nx, s.ny, st));
-  LAUNCH("halo", halo_wrap(b.f[2], s.nx, s.ny, st));
+  LAUNCH("halo", halo_wrap2(b.f[1], b.f[2], s.nx, s.ny, st));
   return nl;
 }
 
