@@ -33,6 +33,22 @@ __device__ __forceinline__ int dexp(double x) {
   return (int)(((unsigned long long)dbits(x) >> 52) & 0x7ffULL);
 }
 
+// x * 2^k for k in -2..1 (p = 2^k), the same value as the FP64 product: when
+// x and the product are normal numbers, the product only changes the exponent
+// field, done here on the integer pipe; zeros are their own product; other
+// cases (subnormal operand or result, inf, NaN) multiply, out of line.
+__device__ __noinline__ double mul_pow2_fp64(double x, double p) { return x * p; }
+__device__ __forceinline__ double mul_pow2(double x, int k, double p) {
+  const long long b = dbits(x);
+  if ((b & 0x7fffffffffffffffLL) == 0) return x;
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e >= 1 && e <= 2046 && e + k >= 1 && e + k <= 2046) return __longlong_as_double(b + ((long long)k << 52));
+  return mul_pow2_fp64(x, p);
+}
+#define HALF(x) mul_pow2((x), -1, 0.5)
+#define QUARTER(x) mul_pow2((x), -2, 0.25)
+#define TWICE(x) mul_pow2((x), 1, 2.0)
+
 // Correctly rounded a/b given y = RN(1/b), b a positive normal number, with
 // multiplications and fused multiply-adds (Markstein's method: P. Markstein,
 // IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook of
@@ -271,11 +287,11 @@ __device__ __forceinline__ double mx(double a, double b) { return key(a) > key(b
 // The limiters of calc.c:54-63 with the comparisons above.
 template <int SCH>
 __device__ __forceinline__ double limiter_fast(double r) {
-  if constexpr (SCH == 0) return mx(0.0, mn(mn((1 + r) / 2.0, 2.0 * r), 2.0));
-  else if constexpr (SCH == 1) return mx(mx(0.0, mn(2.0 * r, 1.0)), mx(0.0, mn(r, 2.0)));
+  if constexpr (SCH == 0) return mx(0.0, mn(mn(HALF(1 + r), TWICE(r)), 2.0));
+  else if constexpr (SCH == 1) return mx(mx(0.0, mn(TWICE(r), 1.0)), mx(0.0, mn(r, 2.0)));
   else if constexpr (SCH == 2) return mn(r, 1.0);
-  else if constexpr (SCH == 4) return mx(0.0, mn(2.0 * r, mn((1 + 2.0 * r) / 3.0, 2.0)));
-  else if constexpr (SCH == 7) return mx(0.0, mn(mn(2.0, 2.0 * r), mn(0.25 + 0.75 * r, 0.75 + 0.25 * r)));
+  else if constexpr (SCH == 4) { const double r2 = TWICE(r); return mx(0.0, mn(r2, mn((1 + r2) / 3.0, 2.0))); }
+  else if constexpr (SCH == 7) return mx(0.0, mn(mn(2.0, TWICE(r)), mn(0.25 + 0.75 * r, 0.75 + QUARTER(r))));
   else if constexpr (SCH == kVanLeerSafe)
     return (dbits(r) == dbits(-1.0)) ? 0.0 : (r + fabs(r)) / (1.0 + r);
   else return limiter<SCH>(r);
@@ -294,7 +310,7 @@ __device__ __forceinline__ double div_nz(double n, double d) {
 template <int SCH>
 __device__ __forceinline__ double half_psi(double n, double d) {
   const double r = nz(d) ? div_nz(n, d) : 0.0;  // r2rP / r2rM (calc.c:42-43)
-  return limiter_fast<SCH>(r) * 0.5;
+  return HALF(limiter_fast<SCH>(r));
 }
 
 // c*B of one side: B2BP (pos) = q0 + psi*0.5*(1-c)*(q1-q0), or B2BM =
@@ -500,30 +516,30 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, do
   Side ts;
   bool oks;
   {
-    const Face F = make_face<SCH>(UF(ic, j0 - 2), u1, u2, u3, 0.5 * (up_p(vs0) + up_p(vs1)),
-                                  0.5 * (up_m(vs0) + up_m(vs1)), fin(vs0) && fin(vs1));
+    const Face F = make_face<SCH>(UF(ic, j0 - 2), u1, u2, u3, HALF(up_p(vs0) + up_p(vs1)),
+                                  HALF(up_m(vs0) + up_m(vs1)), fin(vs0) && fin(vs1));
     ts = side_of(F, Dt, ROW2(R_DYV, R_IDYV, j0));
     oks = F.ok;
   }
-  double vsh = (vs0 + vs1) / 2.;  // calc.c:198, carried from the row below
+  double vsh = HALF(vs0 + vs1);  // (vs0 + vs1) / 2., calc.c:198, carried from the row below
   for (int j = j0; j <= jn; j++) {
     const double u4 = UF(ic, j + 2);
     // x face west of column i, row j: velocities u(i-1), u(i)
     const XN xn = x_neighbours(u2, UF(ia, j), lane);
-    const Face FX = make_face<SCH>(xn.m2, xn.m1, u2, xn.p1, 0.5 * (up_p(xn.m1) + up_p(u2)),
-                                   0.5 * (up_m(xn.m1) + up_m(u2)), true);
+    const Face FX = make_face<SCH>(xn.m2, xn.m1, u2, xn.p1, HALF(up_p(xn.m1) + up_p(u2)),
+                                   HALF(up_m(xn.m1) + up_m(u2)), true);
     const Side tw = side_of(FX, Dt, ROW2(R_DXC, R_IDXC, j));
     const Side te = east_of(tw, lane);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // y face north of row j: velocities v(i, j), v(i+1, j)
     const double vn0 = VF(ic, j), vn1 = VF(ic1, j);
-    const Face FY = make_face<SCH>(u1, u2, u3, u4, 0.5 * (up_p(vn0) + up_p(vn1)), 0.5 * (up_m(vn0) + up_m(vn1)),
+    const Face FY = make_face<SCH>(u1, u2, u3, u4, HALF(up_p(vn0) + up_p(vn1)), HALF(up_m(vn0) + up_m(vn1)),
                                    fin(vn0) && fin(vn1));
     const Side tn = side_of(FY, Dt, ROW2(R_DYV, R_IDYV, j));
     const Side ns = side_of(FY, Dt, ROW2(R_DYV, R_IDYV, j + 1));
     const double S = sum_faces(tw, te, ts, tn);
     const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
-    const double vnh = (vn0 + vn1) / 2.;
+    const double vnh = HALF(vn0 + vn1);
     if (own) {
       double r;
       if (slow) {
@@ -557,8 +573,8 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, do
   Side ts;
   bool oks;
   {
-    const Face F = make_face<SCH>(VF(ic, j0 - 2), v1, v2, v3, 0.5 * (up_p(v1) + up_p(v2)),
-                                  0.5 * (up_m(v1) + up_m(v2)), true);
+    const Face F = make_face<SCH>(VF(ic, j0 - 2), v1, v2, v3, HALF(up_p(v1) + up_p(v2)),
+                                  HALF(up_m(v1) + up_m(v2)), true);
     ts = side_of(F, Dt, ROW2(R_DYC, R_IDYC, j0));
     oks = F.ok;
   }
@@ -567,16 +583,16 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, do
     const double uw1 = UF(iu, j + 1);
     // x face west of column i, row j: velocities u(i-1, j+1), u(i-1, j)
     const XN xn = x_neighbours(v2, VF(ia, j), lane);
-    const Face FX = make_face<SCH>(xn.m2, xn.m1, v2, xn.p1, 0.5 * (up_p(uw1) + up_p(uw0)),
-                                   0.5 * (up_m(uw1) + up_m(uw0)), fin(uw1) && fin(uw0));
+    const Face FX = make_face<SCH>(xn.m2, xn.m1, v2, xn.p1, HALF(up_p(uw1) + up_p(uw0)),
+                                   HALF(up_m(uw1) + up_m(uw0)), fin(uw1) && fin(uw0));
     const Side tw = side_of(FX, Dt, ROW2(R_DXV, R_IDXV, j));
     const Side te = east_of(tw, lane);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // (u(i-1, j) + u(i-1, j+1))/2 and, from the next lane, (u(i, j) + u(i, j+1))/2 (calc.c:235)
-    const double uwh = (uw0 + uw1) / 2.;
+    const double uwh = HALF(uw0 + uw1);
     const double ueh = __shfl_sync(FULL, uwh, (lane + 1) & 31);
     // y face north of row j: velocities v(i, j), v(i, j+1)
-    const Face FY = make_face<SCH>(v1, v2, v3, v4, 0.5 * (up_p(v2) + up_p(v3)), 0.5 * (up_m(v2) + up_m(v3)), true);
+    const Face FY = make_face<SCH>(v1, v2, v3, v4, HALF(up_p(v2) + up_p(v3)), HALF(up_m(v2) + up_m(v3)), true);
     const Side tn = side_of(FY, Dt, ROW2(R_DYC, R_IDYC, j));
     const Side ns = side_of(FY, Dt, ROW2(R_DYC, R_IDYC, j + 1));
     const double S = sum_faces(tw, te, ts, tn);
@@ -763,6 +779,12 @@ __global__ void k_geofactor(DevState s, F7 f, double* ab) {
 }
 
 // solve_pres_u/v + new_vels + dissipation_effect (core.c:217-231; calc.c:500-540, 357-400)
+// x - (U*0)*Dt with U finite is x - (+-0): x itself unless x is a zero.
+__device__ __noinline__ double minus_damping(double x, double U, double sigma, double Dt) { return x - U * sigma * Dt; }
+
+// UD (a band with sigma = 0): the dissipation terms are zeros, subtracted
+// only where the sum is zero or an operand is not finite.
+template <bool UD>
 __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* dvadv, double* dun, double* dvn) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
@@ -773,9 +795,15 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
   const double dvp = div_rcp(mgn * (e[IX(W, i, j + 1)] - e[q]), RW(s, R_DYC, j + 1), RW(s, R_IDYC, j + 1));
   double a = duadv[q] + dup;
   double b = dvadv[q] + dvp;
-  const double su = s.polar ? PF(s, P_SU, q) : s.sigma, sv = s.polar ? PF(s, P_SV, q) : s.sigma;  // calc.c:374-394
-  a -= f.u[q] * su * s.Dt;
-  b -= f.v[q] * sv * s.Dt;
+  if constexpr (UD) {
+    const double U = f.u[q], V = f.v[q];
+    if (!zero_term_is_exact(a, U)) a = minus_damping(a, U, s.sigma, s.Dt);
+    if (!zero_term_is_exact(b, V)) b = minus_damping(b, V, s.sigma, s.Dt);
+  } else {
+    const double su = s.polar ? PF(s, P_SU, q) : s.sigma, sv = s.polar ? PF(s, P_SV, q) : s.sigma;  // calc.c:374-394
+    a -= f.u[q] * su * s.Dt;
+    b -= f.v[q] * sv * s.Dt;
+  }
   dun[q] = a;
   dvn[q] = b;
 }
@@ -870,9 +898,9 @@ __global__ void k_eta_ab3(DevState s, F7 f, double* eta, double* dn, const doubl
   const double e = f.eta[q];
   if constexpr (PL) {
     const double h = e + s.depth;  // - hB with hB = +0 is exact
-    ab -= (RW(s, R_GEO, j) * h * 0.5 * (plus_pos_zero(f.v[q]) + plus_pos_zero(f.v[IX(W, i, j - 1)])));
+    ab -= (HALF(RW(s, R_GEO, j) * h) * (plus_pos_zero(f.v[q]) + plus_pos_zero(f.v[IX(W, i, j - 1)])));
   } else {
-    ab -= (RW(s, R_GEO, j) * HH(i, j) * 0.5 * (VW(i, j) + VW(i, j - 1)));
+    ab -= (HALF(RW(s, R_GEO, j) * HH(i, j)) * (VW(i, j) + VW(i, j - 1)));
   }
   eta[q] = e + ab;
 }
@@ -885,10 +913,10 @@ __global__ void k_coriolis_u_ab3(DevState s, double* u, const double* v, double*
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
   if constexpr (NZ != kNoHyper) dn[q] = x;
   const double duab = ab3(x, dm1[q], dm2[q]);
-  const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
+  const double semi = QUARTER(v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
   const double dtf = s.polar ? s.Dt * PF(s, P_FE, q) : RW(s, R_DTFE, j);
   const double al = dtf + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
-  const double be = 0.25 * al * al;
+  const double be = QUARTER(al) * al;
   u[q] = (u[q] + duab - be * u[q] + al * semi) / (1.0 + be);
 }
 
@@ -900,10 +928,10 @@ __global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double*
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
   if constexpr (NZ != kNoHyper) dn[q] = x;
   const double dvab = ab3(x, dm1[q], dm2[q]);
-  const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
+  const double semi = QUARTER(u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
   const double dtf = s.polar ? s.Dt * PF(s, P_FN, q) : RW(s, R_DTFN, j);
   const double al = dtf + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
-  const double be = 0.25 * al * al;
+  const double be = QUARTER(al) * al;
   v[q] = (v[q] + dvab - be * v[q] - al * semi) / (1.0 + be);
 }
 
@@ -1238,7 +1266,10 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   // momentum (core.c:212-280)
   LAUNCH("adv_u", body(2, sch, g, st, s, F(), b.duadv));
   LAUNCH("adv_v", body(3, sch, g, st, s, F(), b.dvadv));
-  LAUNCH("pres_sum", k_pres_sum<<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
+  if (s.polar == 0 && s.sigma == 0.0)
+    LAUNCH("pres_sum", k_pres_sum<true><<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
+  else
+    LAUNCH("pres_sum", k_pres_sum<false><<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
   if (hyper) {
     // As above: each level rewrites every cell of ze, di and its two L fields
     // (interior, halo wraps, wall fixes), and L of levels not run stay zero.
