@@ -266,6 +266,9 @@ __device__ __noinline__ double advv_cell_ool(const DevState& s, const F7& f, int
 constexpr int FW = 31;      // cells per strip along x (32 faces)
 constexpr int FK = 8;       // rows per strip
 constexpr int FWARPS = 4;   // warps per block; each warp takes strips in turn
+// Resident blocks per SM the register allocation must allow: 5 blocks (20
+// warps) at 96 registers hide the FP64 unit's latency better than 4 at ~120.
+#define FAST_MIN_BLOCKS 5
 constexpr unsigned FULL = 0xffffffffu;
 
 
@@ -457,7 +460,7 @@ __device__ __forceinline__ XN x_neighbours(double v, double aux, int lane) {
 
 // BODYH + damping, fast form.
 template <int SCH, bool PL, bool UD>
-__global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, double* out) {
+__global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_mass_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   const double damp = 2.0 * Dt * (s.sigma);  // calc.c:112: (2.0*Dt*sigma)*ETA
@@ -507,7 +510,7 @@ __global__ void __launch_bounds__(32 * FWARPS) k_mass_fast(DevState s, F7 f, dou
 
 // BODYU, fast form.
 template <int SCH, bool PL>
-__global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, double* out) {
+__global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_adv_u_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int ic1 = min(i + 1, nx + 2);
   // U at this lane's column, rows j-1 .. j+1, and V at columns i, i+1 of row j-1
@@ -564,7 +567,7 @@ __global__ void __launch_bounds__(32 * FWARPS) k_adv_u_fast(DevState s, F7 f, do
 
 // BODYV, fast form.
 template <int SCH, bool PL>
-__global__ void __launch_bounds__(32 * FWARPS) k_adv_v_fast(DevState s, F7 f, double* out) {
+__global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_adv_v_fast(DevState s, F7 f, double* out) {
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   // V at this lane's column, rows j-1 .. j+1; U at column i-1, row j
