@@ -296,3 +296,20 @@ def test_gpu_checkpoint_restart_is_exact(winds):
     other = lib.Solver(cases.make_case(nx=40, ny=24, sch=1, seed=13).params)
     with pytest.raises(lib.SW2GError):
         other.restore(np.concatenate([buf[:8], np.zeros(15 * 44 * 28)]))
+
+
+@pytest.mark.parametrize("orders", [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 0), (0, 1, 1)])
+def test_gpu_hyperviscosity_orders_match_oracle(orders):
+    """The step's kernels are specialised on which hyperviscosity orders are
+    in use (and the Adams-Bashforth tails fuse them from the third step):
+    every combination, with and without Tau damping, matches the oracle in
+    every padded cell."""
+    case = cases.make_case(nx=45, ny=22, sch=1, seed=60 + sum(k << i for i, k in enumerate(orders)),
+                           Tau=3e5 if orders[0] else 1e20)
+    nu4 = case.params.hypernu[1]
+    scale = (1e-3 * nu4 ** 0.5, nu4, 1e-4 * nu4 ** 1.5)
+    case.params.hypernu = tuple(s * k for s, k in zip(scale, orders))
+    s, o = run_both(case, 14, chunk=5)
+    got = s.download()
+    for k in FIELDS:
+        assert same(got[k], o.field(k)), k
