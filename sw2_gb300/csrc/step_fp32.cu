@@ -184,6 +184,11 @@ enum Img { IMG_ETA, IMG_U, IMG_V, IMG_LU, IMG_LV };
 // u and v (calc.c:600-649) or the wall fixes of laplacian_vels (laplacian.c:94-107).
 template <Img M, typename T>
 __device__ __forceinline__ void put(T* f, int W, int nx, int ny, int i, int j, T val) {
+  // cells at least three columns and rows from every edge have no images
+  if (i > 2 && i < nx - 1 && j > 2 && j < ny - 1) {
+    f[IX(W, i, j)] = val;
+    return;
+  }
   const T zero = T(0);
   f[IX(W, i, j)] = (M == IMG_V && j == ny) ? zero : val;
   const int xa = (i <= 2) ? i + nx : NONE, xb = (i >= nx - 1) ? i - nx : NONE;
