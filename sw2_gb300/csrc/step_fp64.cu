@@ -686,6 +686,74 @@ __global__ void k_add(DevState s, double* x, const double* dx) {
   x[q] = x[q] + dx[q];
 }
 
+// Writer-side halos. The reference refreshes a Laplacian field's halo with the
+// single-rank update (every halo cell copies interior cell (wrap(i), wrap(j)))
+// and then fixes the wall rows of the interior columns. Each halo cell's
+// final value therefore comes from one interior cell (or is a constant), and
+// the thread that computes that interior cell writes it:
+//   x-halo columns and corners: the wrap;
+//   halo rows of the interior columns, per field (band; a polar cap keeps the
+//   wrap, it has no walls):
+//     LE (laplacian_eta, laplacian.c:131-146): rows ny+1, ny+2 <- row ny,
+//        row 0 <- row 1, row -1 <- row ny-1;
+//     ZE (laplacian.c:79): row 0 = 0, the other rows wrap;
+//     DI (laplacian.c:73): row ny+1 = the wall difference of u (written by
+//        the kernel), the other rows wrap;
+//     LU (laplacian.c:94-107): row ny+1 <- row ny, row 0 <- row 1, others wrap;
+//     LV: rows ny+1 and 0 = 0, others wrap.
+enum HaloKind { HK_WRAP, HK_LE, HK_ZE, HK_DI, HK_LU, HK_LV };
+constexpr int NOIMG = -1000000;
+template <int K>
+__device__ __forceinline__ void put_images(const DevState& s, double* f, int i, int j, double v) {
+  const int W = s.W, nx = s.nx, ny = s.ny;
+  f[IX(W, i, j)] = v;
+  if (i > 2 && i < nx - 1 && j > 2 && j < ny - 1) return;
+  const int xa = (i <= 2) ? i + nx : NOIMG, xb = (i >= nx - 1) ? i - nx : NOIMG;
+  const int ya = (j <= 2) ? j + ny : NOIMG, yb = (j >= ny - 1) ? j - ny : NOIMG;
+  if (xa != NOIMG) f[IX(W, xa, j)] = v;
+  if (xb != NOIMG) f[IX(W, xb, j)] = v;
+  if (ya != NOIMG) {
+    if (xa != NOIMG) f[IX(W, xa, ya)] = v;
+    if (xb != NOIMG) f[IX(W, xb, ya)] = v;
+  }
+  if (yb != NOIMG) {
+    if (xa != NOIMG) f[IX(W, xa, yb)] = v;
+    if (xb != NOIMG) f[IX(W, xb, yb)] = v;
+  }
+  if (K == HK_WRAP || s.polar != 0) {
+    if (ya != NOIMG) f[IX(W, i, ya)] = v;
+    if (yb != NOIMG) f[IX(W, i, yb)] = v;
+  } else if (K == HK_LE) {
+    if (j == ny) {
+      f[IX(W, i, ny + 1)] = v;
+      f[IX(W, i, ny + 2)] = v;
+    }
+    if (j == 1) f[IX(W, i, 0)] = v;
+    if (j == ny - 1) f[IX(W, i, -1)] = v;
+  } else if (K == HK_ZE) {
+    if (j == ny - 1) f[IX(W, i, -1)] = v;
+    if (j == 1) {
+      f[IX(W, i, 0)] = 0.0;
+      f[IX(W, i, ny + 1)] = v;
+    }
+    if (j == 2) f[IX(W, i, ny + 2)] = v;
+  } else if (K == HK_DI) {
+    if (j == ny - 1) f[IX(W, i, -1)] = v;
+    if (j == ny) f[IX(W, i, 0)] = v;
+    if (j == 2) f[IX(W, i, ny + 2)] = v;
+  } else if (K == HK_LU) {
+    if (j == ny - 1) f[IX(W, i, -1)] = v;
+    if (j == 1) f[IX(W, i, 0)] = v;
+    if (j == ny) f[IX(W, i, ny + 1)] = v;
+    if (j == 2) f[IX(W, i, ny + 2)] = v;
+  } else {  // HK_LV
+    if (j == ny - 1) f[IX(W, i, -1)] = v;
+    if (j == 1) f[IX(W, i, 0)] = 0.0;
+    if (j == ny) f[IX(W, i, ny + 1)] = 0.0;
+    if (j == 2) f[IX(W, i, ny + 2)] = v;
+  }
+}
+
 // laplacian_eta first pass (laplacian.c:120-123)
 __global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* xi) {
   INTERIOR_IJ
@@ -695,22 +763,15 @@ __global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* x
 }
 
 // laplacian_eta second pass (laplacian.c:125-127)
+// (with its halo update and wall rows written from here, laplacian.c:129-146)
 __global__ void k_lape_pass2(DevState s, const double* psi, const double* xi, double* eo) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
-  eo[q] = RW(s, R_KC, j) * (div_rcp(psi[q] - psi[IX(W, i - 1, j)], RW(s, R_DXE, j), RW(s, R_IDXE, j)) +
-                            div_rcp(xi[q] - xi[IX(W, i, j - 1)], RW(s, R_DYN, j), RW(s, R_IDYN, j)));
+  const double v = RW(s, R_KC, j) * (div_rcp(psi[q] - psi[IX(W, i - 1, j)], RW(s, R_DXE, j), RW(s, R_IDXE, j)) +
+                                     div_rcp(xi[q] - xi[IX(W, i, j - 1)], RW(s, R_DYN, j), RW(s, R_IDYN, j)));
+  put_images<HK_LE>(s, eo, i, j, v);
 }
 
-// laplacian_eta wall rows after its halo update (laplacian.c:131-146)
-__global__ void k_lape_fix(int nx, int ny, double* eo) {
-  const int W = nx + 4;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (i > nx) return;
-  eo[IX(W, i, ny + 1)] = eo[IX(W, i, ny)];
-  eo[IX(W, i, ny + 2)] = eo[IX(W, i, ny + 1)];
-  eo[IX(W, i, 0)] = eo[IX(W, i, 1)];
-}
 
 // Deta_n += nu*Dt*L (calc.c:346-350); Du/Dv the same (core.c:258-266), with
 // nu*Dt formed once on the host by the same multiplication. A term whose nu
@@ -812,46 +873,36 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
 }
 
 // laplacian_vels first pass (laplacian.c:59-65)
+// (with the halo update and wall fixes of ze and di written from here, laplacian.c:67-81)
 __global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, double* ze, double* di) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
   double a = RW(s, R_IDXV, j), b = -RW(s, R_IDYC, j + 1);
-  ze[q] = a * ((vv[IX(W, i + 1, j)] - vv[q]) + b * (RW(s, R_DXC, j + 1) * uu[IX(W, i, j + 1)] - RW(s, R_DXC, j) * uu[q]));
+  const double z = a * ((vv[IX(W, i + 1, j)] - vv[q]) + b * (RW(s, R_DXC, j + 1) * uu[IX(W, i, j + 1)] - RW(s, R_DXC, j) * uu[q]));
   a = RW(s, R_IDXE, j);
   b = RW(s, R_IDYN, j);
-  di[q] = a * ((uu[q] - uu[IX(W, i - 1, j)]) + b * (RW(s, R_DXV, j) * vv[q] - RW(s, R_DXV, j - 1) * vv[IX(W, i, j - 1)]));
+  const double d = a * ((uu[q] - uu[IX(W, i - 1, j)]) + b * (RW(s, R_DXV, j) * vv[q] - RW(s, R_DXV, j - 1) * vv[IX(W, i, j - 1)]));
+  put_images<HK_ZE>(s, ze, i, j, z);
+  put_images<HK_DI>(s, di, i, j, d);
+  if (j == s.ny && s.polar == 0)  // laplacian.c:73
+    di[IX(W, i, s.ny + 1)] = (uu[IX(W, i, s.ny)] - uu[IX(W, i - 1, s.ny)]) / RW(s, R_DXE, s.ny);
 }
 
-// laplacian_vels wall fix after the halo update of dseta/div (laplacian.c:70-81)
-__global__ void k_lapv_fix1(DevState s, const double* uu, double* ze, double* di) {
-  const int W = s.W, ny = s.ny;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (i > s.nx) return;
-  di[IX(W, i, ny + 1)] = (uu[IX(W, i, ny)] - uu[IX(W, i - 1, ny)]) / RW(s, R_DXE, ny);
-  ze[IX(W, i, 0)] = 0;
-}
 
 // laplacian_vels second pass (laplacian.c:83-89)
+// (with the halo update and wall fixes of lu and lv written from here, laplacian.c:91-107)
 __global__ void k_lapv_pass2(DevState s, const double* ze, const double* di, double* lu, double* lv) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
   double a = -RW(s, R_IDYN, j), b = RW(s, R_IDXC, j);
-  lu[q] = a * (ze[q] - ze[IX(W, i, j - 1)]) + b * (di[IX(W, i + 1, j)] - di[q]);
+  const double vu = a * (ze[q] - ze[IX(W, i, j - 1)]) + b * (di[IX(W, i + 1, j)] - di[q]);
   a = RW(s, R_IDXV, j);
   b = RW(s, R_IDYC, j + 1);
-  lv[q] = a * (ze[q] - ze[IX(W, i - 1, j)]) + b * (di[IX(W, i, j + 1)] - di[q]);
+  const double vl = a * (ze[q] - ze[IX(W, i - 1, j)]) + b * (di[IX(W, i, j + 1)] - di[q]);
+  put_images<HK_LU>(s, lu, i, j, vu);
+  put_images<HK_LV>(s, lv, i, j, vl);
 }
 
-// laplacian_vels wall fix of the outputs (laplacian.c:94-107)
-__global__ void k_lapv_fix2(int nx, int ny, double* lu, double* lv) {
-  const int W = nx + 4;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  if (i > nx) return;
-  lu[IX(W, i, ny + 1)] = lu[IX(W, i, ny)];
-  lv[IX(W, i, ny + 1)] = 0;
-  lu[IX(W, i, 0)] = lu[IX(W, i, 1)];
-  lv[IX(W, i, 0)] = 0;
-}
 
 // solve_Coriolis_u (calc.c:542-569), in place
 __global__ void k_coriolis_u(DevState s, double* u, const double* v, const double* duab) {
@@ -1218,7 +1269,6 @@ namespace {
 int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
               cudaStream_t st, Timers* tm) {
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
-  const int gw = (s.nx + 127) / 128;
   int nl = 0;
   auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
   const bool hyper = (s.nu2 != 0 || s.nu4 != 0 || s.nu6 != 0);
@@ -1248,10 +1298,8 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
     for (int q = 0; q < nlap; q++) {
       LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
+      // halo and wall rows of Le are written by the pass (a polar cap has no walls)
       LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
-      LAUNCH("halo", halo_wrap(b.Le[q], s.nx, s.ny, st));
-      // the wall rows of a band (laplacian.c:131-146); a polar cap is periodic in y and has none
-      if (s.polar == 0) LAUNCH("lape_fix", k_lape_fix<<<gw, 128, 0, st>>>(s.nx, s.ny, b.Le[q]));
     }
     if (k < 2) LAUNCH("hyper_add", hyper_add(s, g, st, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
   }
@@ -1280,12 +1328,9 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     for (int q = 0; q < nlap; q++) {
       const double* uu = q == 0 ? b.f[1] : b.L[2 * q - 2];
       const double* vv = q == 0 ? b.f[2] : b.L[2 * q - 1];
+      // halos and wall fixes of ze, di and of the outputs are written by the passes
       LAUNCH("lapv_pass1", k_lapv_pass1<<<g, TX, 0, st>>>(s, uu, vv, b.ze, b.di));
-      LAUNCH("halo", halo_wrap2(b.ze, b.di, s.nx, s.ny, st));
-      if (s.polar == 0) LAUNCH("lapv_fix1", k_lapv_fix1<<<gw, 128, 0, st>>>(s, uu, b.ze, b.di));
       LAUNCH("lapv_pass2", k_lapv_pass2<<<g, TX, 0, st>>>(s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
-      LAUNCH("halo", halo_wrap2(b.L[2 * q], b.L[2 * q + 1], s.nx, s.ny, st));
-      if (s.polar == 0) LAUNCH("lapv_fix2", k_lapv_fix2<<<gw, 128, 0, st>>>(s.nx, s.ny, b.L[2 * q], b.L[2 * q + 1]));
     }
     if (k < 2) {
       LAUNCH("hyper_add", hyper_add(s, g, st, b.du[0], b.L[0], b.L[2], b.L[4]));
