@@ -873,21 +873,37 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
 }
 
 // laplacian_vels first pass (laplacian.c:59-65)
-// (with the halo update and wall fixes of ze and di written from here, laplacian.c:67-81)
+// (with the halo update and wall fixes of ze and di written from here,
+// laplacian.c:67-81). A thread marches down LV_ROWS rows of its column, so
+// the products DXC(j+1)*u(i,j+1) and DXV(j)*v(i,j) of one row are the
+// DXC(j)*u(i,j) and DXV(j-1)*v(i,j-1) of the next: the same operands and the
+// same products, formed once.
+constexpr int LV_ROWS = 8;
 __global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, double* ze, double* di) {
-  INTERIOR_IJ
-  const int q = IX(W, i, j);
-  double a = RW(s, R_IDXV, j), b = -RW(s, R_IDYC, j + 1);
-  const double z = a * ((vv[IX(W, i + 1, j)] - vv[q]) + b * (RW(s, R_DXC, j + 1) * uu[IX(W, i, j + 1)] - RW(s, R_DXC, j) * uu[q]));
-  a = RW(s, R_IDXE, j);
-  b = RW(s, R_IDYN, j);
-  const double d = a * ((uu[q] - uu[IX(W, i - 1, j)]) + b * (RW(s, R_DXV, j) * vv[q] - RW(s, R_DXV, j - 1) * vv[IX(W, i, j - 1)]));
-  put_images<HK_ZE>(s, ze, i, j, z);
-  put_images<HK_DI>(s, di, i, j, d);
-  if (j == s.ny && s.polar == 0)  // laplacian.c:73
-    di[IX(W, i, s.ny + 1)] = (uu[IX(W, i, s.ny)] - uu[IX(W, i - 1, s.ny)]) / RW(s, R_DXE, s.ny);
+  const int W = s.W;
+  const int i = blockIdx.x * TX + threadIdx.x + 1;
+  const int j0 = blockIdx.y * LV_ROWS + 1;
+  if (i > s.nx) return;
+  const int j1 = min(j0 + LV_ROWS - 1, s.ny);
+  double pu = RW(s, R_DXC, j0) * uu[IX(W, i, j0)];
+  double qv = RW(s, R_DXV, j0 - 1) * vv[IX(W, i, j0 - 1)];
+  for (int j = j0; j <= j1; j++) {
+    const int q = IX(W, i, j);
+    const double pu1 = RW(s, R_DXC, j + 1) * uu[IX(W, i, j + 1)];
+    const double qv1 = RW(s, R_DXV, j) * vv[q];
+    double a = RW(s, R_IDXV, j), b = -RW(s, R_IDYC, j + 1);
+    const double z = a * ((vv[IX(W, i + 1, j)] - vv[q]) + b * (pu1 - pu));
+    a = RW(s, R_IDXE, j);
+    b = RW(s, R_IDYN, j);
+    const double d = a * ((uu[q] - uu[IX(W, i - 1, j)]) + b * (qv1 - qv));
+    put_images<HK_ZE>(s, ze, i, j, z);
+    put_images<HK_DI>(s, di, i, j, d);
+    if (j == s.ny && s.polar == 0)  // laplacian.c:73
+      di[IX(W, i, s.ny + 1)] = (uu[IX(W, i, s.ny)] - uu[IX(W, i - 1, s.ny)]) / RW(s, R_DXE, s.ny);
+    pu = pu1;
+    qv = qv1;
+  }
 }
-
 
 // laplacian_vels second pass (laplacian.c:83-89)
 // (with the halo update and wall fixes of lu and lv written from here, laplacian.c:91-107)
@@ -926,6 +942,15 @@ __global__ void k_coriolis_v(DevState s, const double* u, double* v, const doubl
   v[q] = (v[q] + dvab[q] - be * v[q] - al * semi) / (1.0 + be);
 }
 
+// check_stats_scaf (sppde_core.c:346-395) as the reference evaluates it: min and
+// max start from the first interior value and skip NaNs after it, so the step
+// aborts iff the first value is not finite or some value lies outside +-1e10.
+// Tested on the bits (|x| > 1e10 and not NaN), for up to four fields at once.
+__device__ __forceinline__ bool range_bad(double x, bool first) {
+  const long long m = dbits(x) & 0x7fffffffffffffffLL;
+  if (first) return m > 0x4202a05f20000000LL;  // beyond 1e10, inf or NaN
+  return m > 0x4202a05f20000000LL && m <= 0x7ff0000000000000LL;
+}
 // From the third step on (AB3), the tail of each tendency is fused into one
 // kernel per field, with the operations of the separate kernels in their
 // order: the hyperviscosity terms (into the stored tendency), the
@@ -941,9 +966,15 @@ __device__ __forceinline__ double plus_pos_zero(double v) {
   return (dbits(v) == (long long)0x8000000000000000ULL) ? 0.0 : v;
 }
 
+// With `bad` given (a whole step, no forcing between its halves), the range
+// check of the new value (core.c:309-312) is done here as well.
+__device__ __forceinline__ void check_range(int* bad, double x, int i, int j) {
+  if (bad && range_bad(x, i == 1 && j == 1)) atomicOr(bad, 1);
+}
+
 template <int NZ, bool PL>
 __global__ void k_eta_ab3(DevState s, F7 f, double* eta, double* dn, const double* dm1, const double* dm2,
-                          const double* l2, const double* l4, const double* l6) {
+                          const double* l2, const double* l4, const double* l6, int* bad) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
@@ -956,12 +987,15 @@ __global__ void k_eta_ab3(DevState s, F7 f, double* eta, double* dn, const doubl
   } else {
     ab -= (HALF(RW(s, R_GEO, j) * HH(i, j)) * (VW(i, j) + VW(i, j - 1)));
   }
-  eta[q] = e + ab;
+  const double en = e + ab;
+  eta[q] = en;
+  check_range(bad, en, i, j);
 }
 
 template <int NZ>
 __global__ void k_coriolis_u_ab3(DevState s, double* u, const double* v, double* dn, const double* dm1,
-                                 const double* dm2, const double* l2, const double* l4, const double* l6) {
+                                 const double* dm2, const double* l2, const double* l4, const double* l6,
+                                 int* bad) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
@@ -971,12 +1005,15 @@ __global__ void k_coriolis_u_ab3(DevState s, double* u, const double* v, double*
   const double dtf = s.polar ? s.Dt * PF(s, P_FE, q) : RW(s, R_DTFE, j);
   const double al = dtf + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
   const double be = QUARTER(al) * al;
-  u[q] = (u[q] + duab - be * u[q] + al * semi) / (1.0 + be);
+  const double un = (u[q] + duab - be * u[q] + al * semi) / (1.0 + be);
+  u[q] = un;
+  check_range(bad, un, i, j);
 }
 
 template <int NZ>
 __global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double* dn, const double* dm1,
-                                 const double* dm2, const double* l2, const double* l4, const double* l6) {
+                                 const double* dm2, const double* l2, const double* l4, const double* l6,
+                                 int* bad) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
@@ -986,34 +1023,41 @@ __global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double*
   const double dtf = s.polar ? s.Dt * PF(s, P_FN, q) : RW(s, R_DTFN, j);
   const double al = dtf + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
   const double be = QUARTER(al) * al;
-  v[q] = (v[q] + dvab - be * v[q] - al * semi) / (1.0 + be);
+  const double vn = (v[q] + dvab - be * v[q] - al * semi) / (1.0 + be);
+  v[q] = vn;
+  check_range(bad, vn, i, j);
 }
 
 template <int NZ>
-void fused_tails(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which) {
+void fused_tails(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which, int* bad) {
   if (which == 0) {
     if (s.plain)
-      k_eta_ab3<NZ, true><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2]);
+      k_eta_ab3<NZ, true><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2],
+                                            bad);
     else
-      k_eta_ab3<NZ, false><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2]);
+      k_eta_ab3<NZ, false><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1],
+                                             b.Le[2], bad);
   } else if (which == 1) {
-    k_coriolis_u_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.du[0], b.du[1], b.du[2], b.L[0], b.L[2], b.L[4]);
+    k_coriolis_u_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.du[0], b.du[1], b.du[2], b.L[0], b.L[2], b.L[4],
+                                           bad);
   } else {
-    k_coriolis_v_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dv[0], b.dv[1], b.dv[2], b.L[1], b.L[3], b.L[5]);
+    k_coriolis_v_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dv[0], b.dv[1], b.dv[2], b.L[1], b.L[3], b.L[5],
+                                           bad);
   }
 }
-// which: 0 eta (hyper + AB3 + geofactor + update), 1 u, 2 v (hyper + AB3 + Coriolis)
-void fused_tail(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which) {
+// which: 0 eta (hyper + AB3 + geofactor + update), 1 u, 2 v (hyper + AB3 + Coriolis);
+// bad: the step's range flag when the range check is done here, else null
+void fused_tail(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which, int* bad) {
   switch (hyper_mask(s)) {
-    case 0: fused_tails<0>(s, g, st, f, b, which); break;
-    case 1: fused_tails<1>(s, g, st, f, b, which); break;
-    case 2: fused_tails<2>(s, g, st, f, b, which); break;
-    case 3: fused_tails<3>(s, g, st, f, b, which); break;
-    case 4: fused_tails<4>(s, g, st, f, b, which); break;
-    case 5: fused_tails<5>(s, g, st, f, b, which); break;
-    case 6: fused_tails<6>(s, g, st, f, b, which); break;
-    case 7: fused_tails<7>(s, g, st, f, b, which); break;
-    default: fused_tails<kNoHyper>(s, g, st, f, b, which); break;
+    case 0: fused_tails<0>(s, g, st, f, b, which, bad); break;
+    case 1: fused_tails<1>(s, g, st, f, b, which, bad); break;
+    case 2: fused_tails<2>(s, g, st, f, b, which, bad); break;
+    case 3: fused_tails<3>(s, g, st, f, b, which, bad); break;
+    case 4: fused_tails<4>(s, g, st, f, b, which, bad); break;
+    case 5: fused_tails<5>(s, g, st, f, b, which, bad); break;
+    case 6: fused_tails<6>(s, g, st, f, b, which, bad); break;
+    case 7: fused_tails<7>(s, g, st, f, b, which, bad); break;
+    default: fused_tails<kNoHyper>(s, g, st, f, b, which, bad); break;
   }
 }
 
@@ -1110,15 +1154,6 @@ __global__ void __launch_bounds__(CFL_T) k_cfl(DevState s, F7 f, unsigned long l
   }
 }
 
-// check_stats_scaf (sppde_core.c:346-395) as the reference evaluates it: min and
-// max start from the first interior value and skip NaNs after it, so the step
-// aborts iff the first value is not finite or some value lies outside +-1e10.
-// Tested on the bits (|x| > 1e10 and not NaN), for up to four fields at once.
-__device__ __forceinline__ bool range_bad(double x, bool first) {
-  const long long m = dbits(x) & 0x7fffffffffffffffLL;
-  if (first) return m > 0x4202a05f20000000LL;  // beyond 1e10, inf or NaN
-  return m > 0x4202a05f20000000LL && m <= 0x7ff0000000000000LL;
-}
 struct RangeFields {
   const double* f[4];
   int n;
@@ -1266,8 +1301,11 @@ namespace {
   } while (0)
 
 // Head of a step: core.c:134-290, through the velocity halos.
+// fused_checks: the range checks of eta, u and v are done by the kernels that
+// write their new values (a whole step with a zero tracer, from the third step).
 int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
-              cudaStream_t st, Timers* tm) {
+              cudaStream_t st, Timers* tm, bool fused_checks) {
+  int* const fbad = fused_checks ? chk.bad + slot : nullptr;
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   int nl = 0;
   auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
@@ -1304,7 +1342,7 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     if (k < 2) LAUNCH("hyper_add", hyper_add(s, g, st, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
   }
   if (k >= 2) {
-    LAUNCH("eta_ab3", fused_tail(s, g, st, F(), b, 0));
+    LAUNCH("eta_ab3", fused_tail(s, g, st, F(), b, 0, fbad));
     rotate3(b.deta);
   } else {
     LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
@@ -1329,7 +1367,7 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
       const double* uu = q == 0 ? b.f[1] : b.L[2 * q - 2];
       const double* vv = q == 0 ? b.f[2] : b.L[2 * q - 1];
       // halos and wall fixes of ze, di and of the outputs are written by the passes
-      LAUNCH("lapv_pass1", k_lapv_pass1<<<g, TX, 0, st>>>(s, uu, vv, b.ze, b.di));
+      LAUNCH("lapv_pass1", k_lapv_pass1<<<dim3(g.x, (s.ny + LV_ROWS - 1) / LV_ROWS), TX, 0, st>>>(s, uu, vv, b.ze, b.di));
       LAUNCH("lapv_pass2", k_lapv_pass2<<<g, TX, 0, st>>>(s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
     }
     if (k < 2) {
@@ -1340,8 +1378,8 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   if (k >= 2) {
     // AB3 of u and v folded into the Coriolis updates (core.c:271-285); the v
     // tendency does not depend on the new u
-    LAUNCH("coriolis_u", fused_tail(s, g, st, F(), b, 1));
-    LAUNCH("coriolis_v", fused_tail(s, g, st, F(), b, 2));
+    LAUNCH("coriolis_u", fused_tail(s, g, st, F(), b, 1, fbad));
+    LAUNCH("coriolis_v", fused_tail(s, g, st, F(), b, 2, fbad));
     rotate3(b.du);
     rotate3(b.dv);
   } else {
@@ -1364,7 +1402,7 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
 // forcing (core.c:296-300) is done by the forcing calls themselves, so the
 // tail is do_channel and the range checks (core.c:303-312).
 int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, int slot, cudaStream_t st,
-              Timers* tm) {
+              Timers* tm, bool fused_checks) {
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   const int gw = (s.nx + 127) / 128;
   int nl = 0;
@@ -1377,7 +1415,7 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
   r.f[r.n++] = b.f[0];
   r.f[r.n++] = b.f[1];
   r.f[r.n++] = b.f[2];
-  LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, r, chk.bad + slot));
+  if (!fused_checks) LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, r, chk.bad + slot));
   return nl;
 }
 #undef LAUNCH
@@ -1387,8 +1425,9 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
               cudaStream_t st, Timers* tm, int parts) {
   int nl = 0;
-  if (parts & STEP_HEAD) nl += step_head(s, b, sch, k, tracer, chk, slot, st, tm);
-  if (parts & STEP_TAIL) nl += step_tail(s, b, tracer, chk, slot, st, tm);
+  const bool fused_checks = (parts == STEP_FULL) && !tracer && k >= 2;
+  if (parts & STEP_HEAD) nl += step_head(s, b, sch, k, tracer, chk, slot, st, tm, fused_checks);
+  if (parts & STEP_TAIL) nl += step_tail(s, b, tracer, chk, slot, st, tm, fused_checks);
   return nl;
 }
 
