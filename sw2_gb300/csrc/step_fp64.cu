@@ -988,7 +988,7 @@ __global__ void k_eta_ab3(DevState s, F7 f, double* eta, double* dn, const doubl
     ab -= (HALF(RW(s, R_GEO, j) * HH(i, j)) * (VW(i, j) + VW(i, j - 1)));
   }
   const double en = e + ab;
-  eta[q] = en;
+  put_images<HK_WRAP>(s, eta, i, j, en);  // with eta's halo update (core.c:206-210)
   check_range(bad, en, i, j);
 }
 
@@ -1342,15 +1342,15 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     if (k < 2) LAUNCH("hyper_add", hyper_add(s, g, st, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
   }
   if (k >= 2) {
-    LAUNCH("eta_ab3", fused_tail(s, g, st, F(), b, 0, fbad));
+    LAUNCH("eta_ab3", fused_tail(s, g, st, F(), b, 0, fbad));  // writes eta's halo images too
     rotate3(b.deta);
   } else {
     LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
     LAUNCH("geofactor", k_geofactor<<<g, TX, 0, st>>>(s, F(), b.detaAB));
     rotate3(b.deta);
     LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[0], b.detaAB));
+    LAUNCH("halo", halo_wrap(b.f[0], s.nx, s.ny, st));
   }
-  LAUNCH("halo", halo_wrap(b.f[0], s.nx, s.ny, st));
 
   // momentum (core.c:212-280)
   LAUNCH("adv_u", body(2, sch, g, st, s, F(), b.duadv));
