@@ -74,6 +74,13 @@ KERNEL_BYTES = {
 # of each input is still in L2 from the kernel before, and most of the output
 # leaves L2 later, so DRAM bytes are below the algorithmic bytes.
 NCU_TRAFFIC = {("band2048", "mass"): 53.87e6, ("band2048", "adv_u"): 34.07e6, ("band2048", "adv_v"): 34.26e6}
+# FP64 thread instructions (DADD + DMUL + DFMA) per interior cell of the
+# dominant kernels on the 2048x1024 workload, from ncu's instruction counters
+# of the same step (profiles/fp64_step_band2048_fp64_instruction_counts.md),
+# and GB300's FP64 peak per cycle over the whole GPU (ncu's peak for DFMA:
+# 304 = 2 lanes per SM x 152 SMs). The FP64 form is bound by this unit.
+NCU_FP64_PER_CELL = {("band2048", "mass"): 63.3, ("band2048", "adv_u"): 78.4, ("band2048", "adv_v"): 78.8}
+FP64_LANES_PER_CYCLE = 304
 # The whole step: read eta u v, write eta u v, read two history levels of
 # three tendencies, write one (SURVEY-style count for the FP64 form).
 STEP_BYTES = 120
@@ -419,6 +426,16 @@ def main():
                 "kernel_frac_of_measured_hbm": (m["achieved_gbs"] / peak) if m["achieved_gbs"] else None,
                 "kernels_ms_per_step": m["kernels_ms_per_step"]}
 
+    clocks = clk.summary()
+    fp64_roof = None
+    n64 = NCU_FP64_PER_CELL.get((args.config, m64["kernel"]))
+    if n64 and m64["per_launch_ms"] and clocks.get("sm_mhz"):
+        ach = n64 * cells / (m64["per_launch_ms"] * 1e-3)
+        pk = FP64_LANES_PER_CYCLE * clocks["sm_mhz"] * 1e6
+        fp64_roof = {"bound": "fp64", "kernel": m64["kernel"], "achieved": ach, "peak": pk,
+                     "unit": "FP64 instr/s", "frac": ach / pk, "instr_per_cell": n64,
+                     "peak_kind": "ncu per-cycle FP64 peak x median SM clock under load"}
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -432,11 +449,13 @@ def main():
                      "traffic": NCU_TRAFFIC.get((args.config, m64["kernel"])), "peak_kind": peak_kind,
                      "bytes_per_cell": m64["bytes_per_cell"],
                      "per_launch_ms": m64["per_launch_ms"], "kernel_share": m64["kernel_share"],
-                     "note": "the FP64 form is bound by GB300's FP64 unit (85 % busy in ncu), not by HBM"},
+                     "note": "the FP64 form is bound by GB300's FP64 unit (85 % busy in ncu), not by HBM: "
+                             "see roofline_fp64"},
+        "roofline_fp64": fp64_roof,
         "kernels_ms_per_step": m64["kernels_ms_per_step"],
         "gpu_launches": m64["launches"],
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "cpu_baseline": cpu,
         "forms": {
             "fp64": form_line(m64, args.config, cells),
