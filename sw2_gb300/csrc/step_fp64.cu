@@ -264,7 +264,6 @@ __device__ __noinline__ double advv_cell_ool(const DevState& s, const F7& f, int
 // The Van Leer limiter in its reference form (0/0 at r = -1) keeps the
 // literal kernels.
 constexpr int FW = 31;      // cells per strip along x (32 faces)
-constexpr int FK = 8;       // rows per strip
 constexpr int FWARPS = 4;   // warps per block; each warp takes strips in turn
 // Resident blocks per SM the register allocation must allow: 5 blocks (20
 // warps) at 96 registers hide the FP64 unit's latency better than 4 at ~120.
@@ -433,12 +432,14 @@ __device__ __forceinline__ XN x_neighbours(double v, double aux, int lane) {
   return n;
 }
 
-// A strip is 31 columns x FK rows; the warps of the grid take strips in turn
+// A strip is 31 columns x s.fk rows (chosen per launch, see fast_launch);
+// the warps of the grid take strips in turn
 // (strip = warp id + k * warps in the grid), so a grid sized to the resident
 // warps keeps every SM busy to the end.
 #define FAST_SETUP                                                                          \
   const int W = s.W, nx = s.nx, ny = s.ny;                                                  \
   const int lane = threadIdx.x & 31;                                                        \
+  const int FK = s.fk;                                                                      \
   const int nsx = (nx + FW - 1) / FW, nstrips = nsx * ((ny + FK - 1) / FK);                  \
   const double Dt = s.Dt;                                                                   \
   for (int strip = blockIdx.x * FWARPS + (threadIdx.x >> 5); strip < nstrips;               \
@@ -1173,18 +1174,34 @@ __global__ void k_range(DevState s, RangeFields r, int* bad) {
 #undef VW
 #undef HH
 
-// Grid of a fast body: the blocks resident on the device at once, or fewer
-// when the grid has fewer strips.
+// Launch of a fast body. Its warps take strips of 31 columns x fk rows in
+// turn (strip = warp + k * warps in the grid), and the grid is the blocks
+// resident on the device at once (or fewer when there are fewer strips).
+// Measured on the 2048x1024 and 4096x2048 workloads (bodies' CUDA-event
+// times for 8, 12, 16 and 24 rows): 12 rows is the best or within 0.2 % of
+// it on both, 16 loses 10 % at 2048x1024, where its 1.4 rounds of strips
+// leave most warps idle in the second. A grid with fewer 12-row strips than
+// resident warps takes shorter strips, down to 4 rows, to use more warps.
+int choose_strip_rows(int nx, int ny, long long warps) {
+  for (int fk : {12, 8, 6}) {
+    const long long strips = (long long)((nx + FW - 1) / FW) * ((ny + fk - 1) / fk);
+    if (strips >= warps) return fk;
+  }
+  return 4;
+}
+
 template <typename K>
-int fast_grid(K kernel, const DevState& s) {
+void fast_launch(K kernel, cudaStream_t st, const DevState& s0, const F7& f, double* out) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 32 * FWARPS, 0);
-  const long long strips = (long long)((s.nx + FW - 1) / FW) * ((s.ny + FK - 1) / FK);
-  const long long need = (strips + FWARPS - 1) / FWARPS;
   const long long full = (long long)(sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
-  return (int)(need < full ? need : full);
+  DevState s = s0;
+  s.fk = choose_strip_rows(s.nx, s.ny, full * FWARPS);
+  const long long strips = (long long)((s.nx + FW - 1) / FW) * ((s.ny + s.fk - 1) / s.fk);
+  const long long need = (strips + FWARPS - 1) / FWARPS;
+  kernel<<<(int)(need < full ? need : full), 32 * FWARPS, 0, st>>>(s, f, out);
 }
 
 template <int SCH>
@@ -1192,16 +1209,16 @@ void launch_bodies(int which, dim3 g, cudaStream_t st, const DevState& s, const 
   if constexpr (SCH != 3) {
     const bool ud = !s.polar && s.sigma == 0.0;
     if (s.plain && ud) {
-      if (which == 0) { k_mass_fast<SCH, true, true><<<fast_grid(k_mass_fast<SCH, true, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 0) { fast_launch(k_mass_fast<SCH, true, true>, st, s, f, out); return; }
     }
     if (s.plain) {
-      if (which == 0) { k_mass_fast<SCH, true, false><<<fast_grid(k_mass_fast<SCH, true, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
-      if (which == 2) { k_adv_u_fast<SCH, true><<<fast_grid(k_adv_u_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
-      if (which == 3) { k_adv_v_fast<SCH, true><<<fast_grid(k_adv_v_fast<SCH, true>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 0) { fast_launch(k_mass_fast<SCH, true, false>, st, s, f, out); return; }
+      if (which == 2) { fast_launch(k_adv_u_fast<SCH, true>, st, s, f, out); return; }
+      if (which == 3) { fast_launch(k_adv_v_fast<SCH, true>, st, s, f, out); return; }
     } else {
-      if (which == 0) { k_mass_fast<SCH, false, false><<<fast_grid(k_mass_fast<SCH, false, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
-      if (which == 2) { k_adv_u_fast<SCH, false><<<fast_grid(k_adv_u_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
-      if (which == 3) { k_adv_v_fast<SCH, false><<<fast_grid(k_adv_v_fast<SCH, false>, s), 32 * FWARPS, 0, st>>>(s, f, out); return; }
+      if (which == 0) { fast_launch(k_mass_fast<SCH, false, false>, st, s, f, out); return; }
+      if (which == 2) { fast_launch(k_adv_u_fast<SCH, false>, st, s, f, out); return; }
+      if (which == 3) { fast_launch(k_adv_v_fast<SCH, false>, st, s, f, out); return; }
     }
   }
   if (which == 0) k_mass<SCH><<<g, TX, 0, st>>>(s, f, out);

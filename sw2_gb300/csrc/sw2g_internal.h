@@ -51,6 +51,7 @@ struct DevState {
   double nu2dt, nu4dt, nu6dt;  // (nu)*(Dt) as the reference forms it (calc.c:346-348)
   int plain;           // windx, windy and hB are +0.0 in every padded cell
   int lape_eta;        // laplacian_eta of eta instead of u (SW2G_FLAG_LAPE_ETA)
+  int fk;              // rows per strip of the fast TVD bodies (set per launch)
   int polar;           // 0: band; +-1: polar cap, with the fields below
   const double* pf;    // P_NUM * W * H (polar only)
 };
