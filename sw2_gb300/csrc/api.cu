@@ -709,7 +709,7 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
       if (bad[t]) {
         x->err_step = (int)(x->steps + t);
         x->steps += t + 1;
-        return SW2G_ERR_NONFINITE;
+        return (bad[t] & kCheckTimeout) ? SW2G_ERR_TIMEOUT : SW2G_ERR_NONFINITE;
       }
     }
     x->steps += n;
@@ -1182,7 +1182,8 @@ sw2g_status sw2g_batch_step(sw2g_batch* b, int nsteps) {
           b->err_step = done + t;
           x->err_step = (int)(x->steps + t);
           for (sw2g_ctx* y : b->mem) y->steps += (y == x) ? t : n;
-          return cfl_bad ? SW2G_ERR_CFL : SW2G_ERR_NONFINITE;
+          if (cfl_bad) return SW2G_ERR_CFL;
+          return (bad[(size_t)m * kChunk + t] & kCheckTimeout) ? SW2G_ERR_TIMEOUT : SW2G_ERR_NONFINITE;
         }
       }
     }

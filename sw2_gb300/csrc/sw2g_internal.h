@@ -177,6 +177,9 @@ struct Fp32Engine {
 
 // Steps whose checks are kept on the device before the host reads them back.
 constexpr int kCheckSlots = 1024;
+// Bits of a step's check word: 1 a value out of range, 2 a device wait that
+// ran out of iterations (the FP32 form's tile loads).
+constexpr int kCheckTimeout = 2;
 
 // Descriptor of one member of an FP32-form batch (a context is a batch of
 // one), passed to the kernels in their launch parameters. Pointers are fixed;
