@@ -73,7 +73,7 @@ KERNEL_BYTES = {
 # third step). With zero winds the plain bodies read eta or u and v only; part
 # of each input is still in L2 from the kernel before, and most of the output
 # leaves L2 later, so DRAM bytes are below the algorithmic bytes.
-NCU_TRAFFIC = {("band2048", "mass"): 53.87e6, ("band2048", "adv_u"): 34.07e6, ("band2048", "adv_v"): 34.26e6}
+NCU_TRAFFIC = {("band2048", "mass"): 57.15e6, ("band2048", "adv_u"): 36.03e6, ("band2048", "adv_v"): 36.00e6}
 # FP64 thread instructions (DADD + DMUL + DFMA) per interior cell of the
 # dominant kernels on the 2048x1024 workload, from ncu's instruction counters
 # of the same step (profiles/fp64_step_band2048_fp64_instruction_counts.md),
