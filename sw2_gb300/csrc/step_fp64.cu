@@ -1,10 +1,14 @@
-// Reference-exact FP64 step: one kernel per reference routine, in core.c's
-// order (core.c:134-338). Compiled with -fmad=false so that no a*b+c is fused:
-// every expression below keeps the association of the reference expression it
-// restates, which makes the results bit-identical to the reference's own
-// single-rank run (divisions and square roots are IEEE-rounded by default;
-// a division by a per-row metric factor goes through div_rcp, which returns
-// the same IEEE quotient with fewer FP64 instructions).
+// Reference-exact FP64 step, in core.c's order (core.c:134-338). The first
+// two steps after an upload run one kernel per reference routine; from the
+// third (AB3) the tails of the tendencies are fused, the Laplacian passes
+// write their own halo images and wall fixes, and the range checks are made
+// by the kernels that write the state. Compiled with -fmad=false so that no
+// a*b+c is fused: every expression keeps the association of the reference
+// expression it restates, which makes the results bit-identical to the
+// reference's own single-rank run. Divisions by a per-row metric factor go
+// through div_rcp (the same IEEE quotient with fewer FP64 instructions), and
+// scalings by powers of two, zero numerators and bit tests are answered on
+// the integer pipe, since GB300 executes FP64 at 2 lanes per SM per clock.
 #include <cuda_runtime.h>
 
 #include "sw2g_internal.h"
