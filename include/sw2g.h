@@ -31,7 +31,8 @@ typedef enum {
   SW2G_ERR_BAD_ARG = 1,   /* invalid case or argument (the reference CRASHes in init.c) */
   SW2G_ERR_CFL = 2,       /* Dt > Dt_CFL at the start of a step (core.c:156-158) */
   SW2G_ERR_NONFINITE = 3, /* field range check failed after a step (core.c:309-312) */
-  SW2G_ERR_TIMEOUT = 4,   /* a bounded device wait gave up */
+  SW2G_ERR_TIMEOUT = 4,   /* a bounded device wait gave up (the FP32 form's TMA tile loads;
+                             the step's state is then not advanced consistently) */
   SW2G_ERR_CUDA = 5,      /* a CUDA runtime call failed */
   SW2G_ERR_NOMEM = 6,     /* device or host allocation failed */
   SW2G_ERR_STATE = 7      /* call out of order (e.g. step before upload) */
