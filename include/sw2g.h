@@ -134,6 +134,14 @@ sw2g_status sw2g_diag(sw2g_ctx *ctx, double *ke, double *ape, double *mass);
 /* Restarts the Adams-Bashforth sequence with an Euler step (as after LoadFrom). */
 sw2g_status sw2g_reset_ab(sw2g_ctx *ctx);
 
+/* Test of the failure path of the FP32 form's bounded device waits: with
+ * waits > 0 the tile loads of the following steps, once their rows have
+ * arrived, also wait for a barrier phase that nothing completes, give up
+ * after `waits` tries, and the step returns SW2G_ERR_TIMEOUT with the device
+ * still usable; waits = 0 restores normal operation. FP32 contexts only. No
+ * counterpart in the reference. */
+sw2g_status sw2g_test_tile_timeout(sw2g_ctx *ctx, int waits);
+
 /* Exact restart of an FP64 context. The reference restarts from a frame
  * (interior only, halos rewrapped) with the Adams-Bashforth index reset
  * (core.c:115-134), so its restarted run departs from the uninterrupted one.

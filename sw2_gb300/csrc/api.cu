@@ -826,6 +826,12 @@ sw2g_status sw2g_diag(sw2g_ctx* x, double* ke, double* ape, double* mass) {
   return SW2G_OK;
 }
 
+sw2g_status sw2g_test_tile_timeout(sw2g_ctx* x, int waits) {
+  if (!x || x->precision != SW2G_FP32 || waits < 0) return SW2G_ERR_BAD_ARG;
+  x->c32.tile_test = waits;
+  return SW2G_OK;
+}
+
 sw2g_status sw2g_reset_ab(sw2g_ctx* x) {
   if (!x) return SW2G_ERR_BAD_ARG;
   x->k = 0;

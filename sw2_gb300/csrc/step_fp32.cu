@@ -250,7 +250,10 @@ __device__ __forceinline__ void load_tile(const float* __restrict__ f, int P, in
 // CHECK_TIMEOUT in the step's check word (SW2G_ERR_TIMEOUT on the host) and
 // the whole block returns without computing.
 constexpr int TILE_ROWS = TH + 4, TILE_ROW_BYTES = (TW + 4) * 4;
-constexpr long long TILE_WAIT_LIMIT = 1LL << 22;
+// Each wait suspends the thread for at most TILE_WAIT_HINT_NS, so the limit
+// bounds a wait to about 1.3 s.
+constexpr int TILE_WAIT_LIMIT = 1 << 16;
+constexpr unsigned TILE_WAIT_HINT_NS = 20000;
 constexpr int CHECK_TIMEOUT = kCheckTimeout;
 static_assert(TILE_ROW_BYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
 
@@ -278,17 +281,29 @@ __device__ __forceinline__ void tile_row_copy(unsigned long long* bar, const flo
                : "memory");
 }
 
-// True when every row arrived; all threads of the block return the same answer.
-__device__ __forceinline__ bool tiles_wait(unsigned long long* bar, int* bad) {
-  const unsigned b = smem_u32(bar);
+// One thread's bounded wait for the completion of the barrier phase of the
+// given parity; true if it completed.
+__device__ __forceinline__ bool phase_wait(unsigned bar, unsigned parity, int limit) {
   unsigned done = 0;
-  for (long long it = 0; it < TILE_WAIT_LIMIT && !done; it++) {
+  for (int it = 0; it < limit && !done; it++) {
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, "
+        "p;\n\t}"
         : "=r"(done)
-        : "r"(b), "r"(0u)
+        : "r"(bar), "r"(parity), "r"(TILE_WAIT_HINT_NS)
         : "memory");
   }
+  return done != 0;
+}
+
+// True when every row arrived; all threads of the block return the same
+// answer. test_waits > 0 (the failure-path test): after the rows have
+// arrived, also wait for the next phase, which nothing completes, giving up
+// after test_waits tries; no copy is then in flight when the block leaves.
+__device__ __forceinline__ bool tiles_wait(unsigned long long* bar, int* bad, int test_waits) {
+  const unsigned b = smem_u32(bar);
+  bool done = phase_wait(b, 0u, TILE_WAIT_LIMIT);
+  if (test_waits > 0 && done) done = phase_wait(b, 1u, test_waits);
   const int failed = __syncthreads_or(!done);
   if (failed && threadIdx.x == 0 && bad) atomicOr(bad, CHECK_TIMEOUT);
   return !failed;
@@ -559,7 +574,7 @@ struct Main2Io {
 };
 
 // Pressure (calc.c:500-540), AB, Coriolis u then v (calc.c:542-598).
-__device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2Io& io) {
+__device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2Io& io, int tile_test) {
   __shared__ __align__(16) Tile se, su, sv;  // ring-2 windows, ring 1 used
   __shared__ float un[TH + 1][TW + 1];       // new u at (i0-1+a, j0+b)
   __shared__ RowCache sq;
@@ -601,7 +616,7 @@ __device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2
   }
   fill_rows(p, j0, sq);
   const Rows rc{sq, j0};
-  if (!tiles_wait(&tbar, io.bad)) return;
+  if (!tiles_wait(&tbar, io.bad, tile_test)) return;
   // new u on [i0-1, i0+TW-1] x [j0, j0+TH]: interior cells recomputed, the
   // halo column 0 and the halo row ny+1 keep the old u (the v update reads
   // them before the halo refresh, core.c:283-289)
@@ -749,7 +764,7 @@ __global__ void __launch_bounds__(NT, 6) kb_main2(const __grid_constant__ DescSe
   const Main2Io io{d.es[1 - v.cur], d.u[v.cur], d.v[v.cur], d.us[v.cur], d.vs[v.cur], d.u[1 - v.cur],
                    d.v[1 - v.cur], d.us[1 - v.cur], d.vs[1 - v.cur], d.dup, d.dvp, d.hu[v.h1], d.hu[v.h2],
                    d.hv[v.h1], d.hv[v.h2], d.hu[v.w], d.hv[v.w], d.bad + v.slot};
-  d_main2(kp_of(d, v.k), t.y, t.z, io);
+  d_main2(kp_of(d, v.k), t.y, t.z, io, d.tile_test);
 }
 
 __global__ void kb_advance(int* counter) { *counter += 1; }
@@ -803,6 +818,7 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
   d.cur0 = e.cur;
   d.w0 = e.w;
   d.k0 = k > 2 ? 2 : k;
+  d.tile_test = c.tile_test;
   return d;
 }
 

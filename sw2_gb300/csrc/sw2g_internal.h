@@ -151,6 +151,10 @@ struct Fp32Ctx {
   const float* q;
   float sig2dt, sigdt, nu2dt, nu4dt;
   const float* wx; const float* wy; const float* hb;
+  // Test of the failure path (sw2g_test_tile_timeout): > 0 makes the tile
+  // loads of the next steps also wait for a barrier phase that never
+  // completes, giving up after that many tries; 0 in normal use.
+  int tile_test = 0;
 };
 
 struct Fp32Engine {
@@ -197,7 +201,7 @@ struct MemberDesc {
   float* heta[3]; float* hu[3]; float* hv[3];
   float* Lu; float* Lv; float* dup; float* dvp;
   unsigned* cfl; int* bad;
-  int cur0, w0, k0, pad;
+  int cur0, w0, k0, tile_test;
 };
 
 // Most members of one batch: their descriptors fill at most ~28 KB of the

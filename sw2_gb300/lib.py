@@ -32,7 +32,7 @@ SYMBOLS = [
     "sw2g_destroy", "sw2g_last_step_ms", "sw2g_timers_enable", "sw2g_timers_reset", "sw2g_timers_count",
     "sw2g_timer_read", "sw2g_selfcheck_division", "sw2g_add_field", "sw2g_set_field_where",
     "sw2g_apply_channel", "sw2g_step_open", "sw2g_step_close", "sw2g_checkpoint_doubles",
-    "sw2g_checkpoint_save", "sw2g_checkpoint_load",
+    "sw2g_checkpoint_save", "sw2g_checkpoint_load", "sw2g_test_tile_timeout",
 ]
 
 
@@ -217,6 +217,13 @@ class Solver:
         buf = np.empty(n, dtype=np.float64)
         self._check(L.sw2g_checkpoint_save(self.h, _ptr(buf), n), "sw2g_checkpoint_save")
         return buf
+
+    def test_tile_timeout(self, waits: int):
+        """FP32 contexts: make the following steps' tile loads also wait for a
+        barrier phase that never completes (waits > 0 tries each), or restore (0)."""
+        L = load()
+        L.sw2g_test_tile_timeout.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        self._check(L.sw2g_test_tile_timeout(self.h, int(waits)), "sw2g_test_tile_timeout")
 
     def restore(self, buf):
         L = load()

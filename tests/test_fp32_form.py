@@ -99,3 +99,27 @@ def test_fp32_band256_500_steps_error_bar():
     ka, pa, ma = sa.diag()
     kb, pb, mb = sb.diag()
     assert abs(ma - mb) <= 1e-9 * abs(mb)
+
+
+def test_fp32_bounded_tile_wait_reports_timeout():
+    """Failure path of the FP32 form's bounded device waits (TMA tile loads on
+    an mbarrier): tiles that never complete make every block give up after
+    its wait limit and the step return SW2G_ERR_TIMEOUT, with the device and
+    the library still usable afterwards."""
+    case = cases.make_case(nx=64, ny=32, sch=2, seed=4)
+    s = lib.Solver(case.params, precision=lib.FP32)
+    s.upload(*case.fields())
+    assert s.step(2) == lib.OK
+    s.test_tile_timeout(3)
+    with pytest.raises(lib.SW2GError) as err:
+        s.step(1)
+    assert err.value.code == lib.ERR_TIMEOUT
+    s.test_tile_timeout(0)
+    s.upload(*case.fields())
+    assert s.step(3) == lib.OK
+    # a fresh context of either form runs normally on the same device
+    s64 = lib.Solver(case.params)
+    s64.upload(*case.fields())
+    assert s64.step(3) == lib.OK
+    with pytest.raises(lib.SW2GError):
+        s64.test_tile_timeout(3)  # FP64 contexts have no such waits
