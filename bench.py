@@ -371,8 +371,9 @@ def main():
     ms = secs * 1e3
     s = m64["solver"]
 
-    # end to end through the C ABI: every step uploads the state from pinned
-    # host memory, steps once, and downloads it again
+    # end to end through the C ABI: every step is one sw2g_step_host call on
+    # the state held in pinned host arrays (copied in, stepped once, copied
+    # back into the same arrays)
     W, H = p.nx + 4, p.ny + 4
     host = [torch.empty((H, W), dtype=torch.float64, pin_memory=True).numpy() for _ in range(3)]
     d = s.download()
@@ -381,10 +382,8 @@ def main():
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        s.upload(host[0], host[1], host[2], mode=lib.UPLOAD_CONTINUE)
-        if s.step(1) != lib.OK:
+        if s.step_host(host[0], host[1], host[2], 1) != lib.OK:
             raise RuntimeError("e2e step failed")
-        lib.load().sw2g_download(s.h, *[lib._ptr(h) for h in host], None)
     barrier()
     e2e, _, _ = aggregate(cells * args.steps, time.perf_counter() - t0, dev)
     bytes_io = 3 * W * H * 8

@@ -120,6 +120,16 @@ sw2g_status sw2g_step(sw2g_ctx *ctx, int nsteps);
 sw2g_status sw2g_step_open(sw2g_ctx *ctx);
 sw2g_status sw2g_step_close(sw2g_ctx *ctx);
 
+/* The per-step call of a caller that keeps the state in its own padded host
+ * arrays, as the reference's loop keeps SW->eta, SW->u and SW->v (core.c:134-338):
+ * copies eta, u and v in (as sw2g_upload with SW2G_UPLOAD_CONTINUE), advances
+ * nsteps steps (as sw2g_step) and copies the new state back into the same
+ * arrays (as sw2g_download), also when a step fails. In the FP64 form the
+ * copies of eta overlap the step: it goes in while the step's first kernels,
+ * which read only u and v, run, and comes out while the step goes on with u
+ * and v. Needs an earlier sw2g_upload (winds, bottom, tracer, history). */
+sw2g_status sw2g_step_host(sw2g_ctx *ctx, double *eta, double *u, double *v, int nsteps);
+
 /* Step index of the last CFL/range failure, -1 if none. */
 int sw2g_error_step(const sw2g_ctx *ctx);
 

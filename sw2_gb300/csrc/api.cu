@@ -174,6 +174,10 @@ struct sw2g_ctx {
   // forcing between steps (FP64 form): staging of one padded field and a mask
   double* d_force = nullptr;
   void* d_mask = nullptr;
+  // sw2g_step_host: a second stream for the copies of eta, and the events
+  // u/v copied in, eta copied in, eta final, eta copied out (made on first use)
+  cudaStream_t side = nullptr;
+  cudaEvent_t hev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -634,10 +638,57 @@ sw2g_status sw2g_upload(sw2g_ctx* x, const double* eta, const double* u, const d
   return SW2G_OK;
 }
 
+// The caller's arrays of sw2g_step_host: copied out at the end of the last
+// step, eta as soon as the step has finished it (FP64 form).
+struct HostIO {
+  double *eta, *u, *v;
+  bool copied;
+};
+
+static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io);
+
 sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
   if (!x || nsteps < 0) return SW2G_ERR_BAD_ARG;
   if (!x->uploaded || x->open) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
+  return run_steps(x, nsteps, nullptr);
+}
+
+sw2g_status sw2g_step_host(sw2g_ctx* x, double* eta, double* u, double* v, int nsteps) {
+  if (!x || !eta || !u || !v || nsteps < 1) return SW2G_ERR_BAD_ARG;
+  if (!x->uploaded || x->open) return SW2G_ERR_STATE;
+  if (x->precision == SW2G_FP32) {  // the FP32 form converts on the way in and out: in sequence
+    sw2g_status st = sw2g_upload(x, eta, u, v, nullptr, nullptr, nullptr, nullptr, SW2G_UPLOAD_CONTINUE);
+    if (st != SW2G_OK) return st;
+    const sw2g_status ss = sw2g_step(x, nsteps);
+    st = sw2g_download(x, eta, u, v, nullptr);
+    return ss != SW2G_OK ? ss : st;
+  }
+  CK(cudaSetDevice(x->device));
+  if (!x->side) {
+    CK(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
+    for (int e = 0; e < 4; e++) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
+  }
+  // u and v first: the step's first kernels (the CFL maxima, the advection
+  // of u and v) read only them, while eta is still on its way in.
+  const size_t bytes = sizeof(double) * (size_t)x->s.W * x->s.H;
+  CK(cudaMemcpyAsync(x->b.f[1], u, bytes, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->b.f[2], v, bytes, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaEventRecord(x->hev[0], x->stream));
+  CK(cudaStreamWaitEvent(x->side, x->hev[0], 0));
+  CK(cudaMemcpyAsync(x->b.f[0], eta, bytes, cudaMemcpyHostToDevice, x->side));
+  CK(cudaEventRecord(x->hev[1], x->side));
+  HostIO io{eta, u, v, false};
+  const sw2g_status st = run_steps(x, nsteps, &io);
+  if (!io.copied) {  // a failure before the last chunk of steps was queued
+    const sw2g_status sd = sw2g_download(x, eta, u, v, nullptr);
+    return st != SW2G_OK ? st : sd;
+  }
+  CK(cudaStreamSynchronize(x->side));
+  return st;
+}
+
+static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
   x->last_launches = 0;
   std::vector<unsigned long long> cfl(2 * kChunk);
   std::vector<int> bad(kChunk);
@@ -666,12 +717,27 @@ sw2g_status sw2g_step(sw2g_ctx* x, int nsteps) {
       x->k += n;
     } else {
       for (int t = 0; t < n; t++) {
-        x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers);
+        StepHooks hk;
+        if (io && done + t == 0) hk.eta_in = x->hev[1];
+        if (io && done + t == nsteps - 1) hk.eta_out = x->hev[2];
+        x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers,
+                                      STEP_FULL, hk);
         x->k++;
       }
     }
     CK(cudaEventRecord(x->ev[1], x->stream));
     CK(cudaGetLastError());
+    if (io && done + n == nsteps) {
+      // eta goes out on the side stream while the step computes u and v
+      const size_t bytes = sizeof(double) * (size_t)x->s.W * x->s.H;
+      CK(cudaStreamWaitEvent(x->side, x->hev[2], 0));
+      CK(cudaMemcpyAsync(io->eta, x->b.f[0], bytes, cudaMemcpyDeviceToHost, x->side));
+      CK(cudaEventRecord(x->hev[3], x->side));
+      CK(cudaMemcpyAsync(io->u, x->b.f[1], bytes, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaMemcpyAsync(io->v, x->b.f[2], bytes, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaStreamWaitEvent(x->stream, x->hev[3], 0));
+      io->copied = true;
+    }
     if (f32) {
       CK(cudaMemcpyAsync(cfl32.data(), x->e32.cfl + 2 * slot0, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost,
                          x->stream));
@@ -1004,6 +1070,12 @@ void sw2g_destroy(sw2g_ctx* x) {
   x->run32.release();
   for (int e = 0; e < 2; e++)
     if (x->ev[e]) cudaEventDestroy(x->ev[e]);
+  for (int e = 0; e < 4; e++)
+    if (x->hev[e]) cudaEventDestroy(x->hev[e]);
+  if (x->side) {
+    cudaStreamSynchronize(x->side);
+    cudaStreamDestroy(x->side);
+  }
   if (x->stream) cudaStreamDestroy(x->stream);
   delete x;
 }

@@ -1324,8 +1324,12 @@ namespace {
 // Head of a step: core.c:134-290, through the velocity halos.
 // fused_checks: the range checks of eta, u and v are done by the kernels that
 // write their new values (a whole step with a zero tracer, from the third step).
+// The advection sweeps of u and v (core.c:212-215) run before the mass
+// update: they read only u, v, the winds and the geometry, and write only
+// their own tendencies, so the order changes no value, and a caller that
+// copies eta in can overlap that copy with them (StepHooks).
 int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
-              cudaStream_t st, Timers* tm, bool fused_checks) {
+              cudaStream_t st, Timers* tm, bool fused_checks, StepHooks hk) {
   int* const fbad = fused_checks ? chk.bad + slot : nullptr;
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   int nl = 0;
@@ -1345,7 +1349,12 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     LAUNCH("halo", halo_wrap(b.f[3], s.nx, s.ny, st));
   }
 
+  // advection of u and v (core.c:212-215)
+  LAUNCH("adv_u", body(2, sch, g, st, s, F(), b.duadv));
+  LAUNCH("adv_v", body(3, sch, g, st, s, F(), b.dvadv));
+
   // mass (core.c:184-210; calc.c:289-355)
+  if (hk.eta_in) cudaStreamWaitEvent(st, hk.eta_in, 0);
   LAUNCH("mass", body(0, sch, g, st, s, F(), b.deta[0]));
   if (hyper) {
     // The reference zeroes Le, psi and xi before the Laplacians (calc.c:325-327,
@@ -1372,10 +1381,9 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[0], b.detaAB));
     LAUNCH("halo", halo_wrap(b.f[0], s.nx, s.ny, st));
   }
+  if (hk.eta_out) cudaEventRecord(hk.eta_out, st);  // eta is final for this step
 
   // momentum (core.c:212-280)
-  LAUNCH("adv_u", body(2, sch, g, st, s, F(), b.duadv));
-  LAUNCH("adv_v", body(3, sch, g, st, s, F(), b.dvadv));
   if (s.polar == 0 && s.sigma == 0.0)
     LAUNCH("pres_sum", k_pres_sum<true><<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
   else
@@ -1444,10 +1452,10 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
 }  // namespace
 
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int slot,
-              cudaStream_t st, Timers* tm, int parts) {
+              cudaStream_t st, Timers* tm, int parts, StepHooks hk) {
   int nl = 0;
   const bool fused_checks = (parts == STEP_FULL) && !tracer && k >= 2;
-  if (parts & STEP_HEAD) nl += step_head(s, b, sch, k, tracer, chk, slot, st, tm, fused_checks);
+  if (parts & STEP_HEAD) nl += step_head(s, b, sch, k, tracer, chk, slot, st, tm, fused_checks, hk);
   if (parts & STEP_TAIL) nl += step_tail(s, b, tracer, chk, slot, st, tm, fused_checks);
   return nl;
 }

@@ -32,7 +32,7 @@ SYMBOLS = [
     "sw2g_destroy", "sw2g_last_step_ms", "sw2g_timers_enable", "sw2g_timers_reset", "sw2g_timers_count",
     "sw2g_timer_read", "sw2g_selfcheck_division", "sw2g_add_field", "sw2g_set_field_where",
     "sw2g_apply_channel", "sw2g_step_open", "sw2g_step_close", "sw2g_checkpoint_doubles",
-    "sw2g_checkpoint_save", "sw2g_checkpoint_load", "sw2g_test_tile_timeout",
+    "sw2g_checkpoint_save", "sw2g_checkpoint_load", "sw2g_test_tile_timeout", "sw2g_step_host",
 ]
 
 
@@ -71,6 +71,7 @@ def load():
         L.sw2g_create.argtypes = [ctypes.POINTER(Case), ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
         L.sw2g_upload.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int]
         L.sw2g_step.argtypes = [vp, ctypes.c_int]
+        L.sw2g_step_host.argtypes = [vp, dp, dp, dp, ctypes.c_int]
         L.sw2g_error_step.argtypes = [vp]
         L.sw2g_download.argtypes = [vp, dp, dp, dp, dp]
         L.sw2g_diag.argtypes = [vp, dp, dp, dp]
@@ -181,6 +182,19 @@ class Solver:
         if rc in (OK, ERR_CFL, ERR_NONFINITE):
             return rc
         self._check(rc, "sw2g_step")
+
+    def step_host(self, eta, u, v, n: int = 1):
+        """sw2g_step_host: n steps of the state held in the caller's padded
+        float64 arrays (C order, writable), which receive the new state in
+        place; returns the status code as step() does."""
+        for a in (eta, u, v):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+                    and a.flags.writeable and a.shape == (self.ny + 4, self.nx + 4)):
+                raise ValueError("step_host takes writable C-contiguous float64 arrays of the padded shape")
+        rc = load().sw2g_step_host(self.h, _ptr(eta), _ptr(u), _ptr(v), int(n))
+        if rc in (OK, ERR_CFL, ERR_NONFINITE):
+            return rc
+        self._check(rc, "sw2g_step_host")
 
     def error_step(self) -> int:
         return load().sw2g_error_step(self.h)
