@@ -174,10 +174,17 @@ struct sw2g_ctx {
   // forcing between steps (FP64 form): staging of one padded field and a mask
   double* d_force = nullptr;
   void* d_mask = nullptr;
-  // sw2g_step_host: a second stream for the copies of eta, and the events
-  // u/v copied in, eta copied in, eta final, eta copied out (made on first use)
+  // sw2g_step_host: a second stream for the copies of eta and u, and the
+  // events u/v copied in, eta copied in, eta final, side copies done, u's
+  // interior final, step done (made on first use)
   cudaStream_t side = nullptr;
-  cudaEvent_t hev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t hev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  // pinned host copies of a chunk's checks (CFL maxima of either form, range
+  // flags), so that reading them back is one more asynchronous copy
+  void* h_chk = nullptr;
+  unsigned long long* h_cfl = nullptr;
+  unsigned* h_cfl32 = nullptr;
+  int* h_bad = nullptr;
 };
 
 namespace {
@@ -560,6 +567,15 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
     return fail(st);
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_bad, sizeof(int) * kChunk), "bad")) != SW2G_OK) return fail(st);
+  {
+    const size_t b64 = sizeof(unsigned long long) * 2 * kChunk, b32 = sizeof(unsigned) * 2 * kChunk;
+    if ((st = cuda_fail(cudaHostAlloc(&x->h_chk, b64 + b32 + sizeof(int) * kChunk, cudaHostAllocDefault),
+                        "pinned checks")) != SW2G_OK)
+      return fail(st);
+    x->h_cfl = (unsigned long long*)x->h_chk;
+    x->h_cfl32 = (unsigned*)((char*)x->h_chk + b64);
+    x->h_bad = (int*)((char*)x->h_chk + b64 + b32);
+  }
   if ((st = dalloc(x, &x->d_energy, 3 * (size_t)c->ny + 3)) != SW2G_OK) return fail(st);
   if ((st = cuda_fail(cudaStreamSynchronize(x->stream), "sync")) != SW2G_OK) return fail(st);
   *out = x;
@@ -667,7 +683,7 @@ sw2g_status sw2g_step_host(sw2g_ctx* x, double* eta, double* u, double* v, int n
   CK(cudaSetDevice(x->device));
   if (!x->side) {
     CK(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
-    for (int e = 0; e < 4; e++) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
+    for (int e = 0; e < 6; e++) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
   }
   // u and v first: the step's first kernels (the CFL maxima, the advection
   // of u and v) read only them, while eta is still on its way in.
@@ -690,12 +706,12 @@ sw2g_status sw2g_step_host(sw2g_ctx* x, double* eta, double* u, double* v, int n
 
 static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
   x->last_launches = 0;
-  std::vector<unsigned long long> cfl(2 * kChunk);
-  std::vector<int> bad(kChunk);
+  unsigned long long* const cfl = x->h_cfl;
+  unsigned* const cfl32 = x->h_cfl32;
+  int* const bad = x->h_bad;
   int done = 0;
   x->last_step_ms = 0;
   const bool f32 = (x->precision == SW2G_FP32);
-  std::vector<unsigned> cfl32(f32 ? 2 * kChunk : 0);
   while (done < nsteps) {
     int n = (nsteps - done) < kChunk ? (nsteps - done) : kChunk;
     int slot0 = 0;  // check slot of the chunk's first step
@@ -719,7 +735,10 @@ static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
       for (int t = 0; t < n; t++) {
         StepHooks hk;
         if (io && done + t == 0) hk.eta_in = x->hev[1];
-        if (io && done + t == nsteps - 1) hk.eta_out = x->hev[2];
+        if (io && done + t == nsteps - 1) {
+          hk.eta_out = x->hev[2];
+          hk.u_out = x->hev[4];
+        }
         x->last_launches += fp64_step(x->s, x->b, x->sch, x->k, x->tracer_active, chk, t, x->stream, &x->timers,
                                       STEP_FULL, hk);
         x->k++;
@@ -728,24 +747,36 @@ static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
     CK(cudaEventRecord(x->ev[1], x->stream));
     CK(cudaGetLastError());
     if (io && done + n == nsteps) {
-      // eta goes out on the side stream while the step computes u and v
-      const size_t bytes = sizeof(double) * (size_t)x->s.W * x->s.H;
+      // On the side stream, eta goes out while the step computes u and v, and
+      // u while it computes v; u's halo columns and wall rows, which the end
+      // of the step rewrites, follow once it is done.
+      const size_t W = x->s.W, H = x->s.H, row = sizeof(double) * W, bytes = row * H;
+      const int nx = x->s.nx, ny = x->s.ny;
+      CK(cudaEventRecord(x->hev[5], x->stream));
       CK(cudaStreamWaitEvent(x->side, x->hev[2], 0));
       CK(cudaMemcpyAsync(io->eta, x->b.f[0], bytes, cudaMemcpyDeviceToHost, x->side));
+      CK(cudaStreamWaitEvent(x->side, x->hev[4], 0));
+      CK(cudaMemcpyAsync(io->u, x->b.f[1], bytes, cudaMemcpyDeviceToHost, x->side));
+      CK(cudaStreamWaitEvent(x->side, x->hev[5], 0));
+      const double* du = x->b.f[1];
+      CK(cudaMemcpyAsync(io->u, du, 2 * row, cudaMemcpyDeviceToHost, x->side));  // rows -1, 0
+      CK(cudaMemcpyAsync(io->u + (ny + 2) * W, du + (ny + 2) * W, 2 * row, cudaMemcpyDeviceToHost,
+                         x->side));  // rows ny+1, ny+2
+      for (size_t c : {(size_t)0, (size_t)nx + 2})  // columns -1, 0 and nx+1, nx+2 of the interior rows
+        CK(cudaMemcpy2DAsync(io->u + 2 * W + c, row, du + 2 * W + c, row, 2 * sizeof(double), ny,
+                             cudaMemcpyDeviceToHost, x->side));
       CK(cudaEventRecord(x->hev[3], x->side));
-      CK(cudaMemcpyAsync(io->u, x->b.f[1], bytes, cudaMemcpyDeviceToHost, x->stream));
       CK(cudaMemcpyAsync(io->v, x->b.f[2], bytes, cudaMemcpyDeviceToHost, x->stream));
       CK(cudaStreamWaitEvent(x->stream, x->hev[3], 0));
       io->copied = true;
     }
     if (f32) {
-      CK(cudaMemcpyAsync(cfl32.data(), x->e32.cfl + 2 * slot0, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost,
+      CK(cudaMemcpyAsync(cfl32, x->e32.cfl + 2 * slot0, sizeof(unsigned) * 2 * n, cudaMemcpyDeviceToHost,
                          x->stream));
-      CK(cudaMemcpyAsync(bad.data(), x->e32.bad + slot0, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaMemcpyAsync(bad, x->e32.bad + slot0, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
     } else {
-      CK(cudaMemcpyAsync(cfl.data(), x->d_cfl, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost,
-                         x->stream));
-      CK(cudaMemcpyAsync(bad.data(), x->d_bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaMemcpyAsync(cfl, x->d_cfl, sizeof(unsigned long long) * 2 * n, cudaMemcpyDeviceToHost, x->stream));
+      CK(cudaMemcpyAsync(bad, x->d_bad, sizeof(int) * n, cudaMemcpyDeviceToHost, x->stream));
     }
     CK(cudaStreamSynchronize(x->stream));
     float ms = 0;
@@ -810,10 +841,10 @@ sw2g_status sw2g_step_close(sw2g_ctx* x) {
   CK(cudaEventRecord(x->ev[1], x->stream));
   CK(cudaGetLastError());
   x->open = false;
-  unsigned long long cfl[2] = {0, 0};
-  int bad = 0;
-  CK(cudaMemcpyAsync(cfl, x->d_cfl, sizeof cfl, cudaMemcpyDeviceToHost, x->stream));
-  CK(cudaMemcpyAsync(&bad, x->d_bad, sizeof bad, cudaMemcpyDeviceToHost, x->stream));
+  unsigned long long* const cfl = x->h_cfl;
+  int* const bad = x->h_bad;
+  CK(cudaMemcpyAsync(cfl, x->d_cfl, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaMemcpyAsync(bad, x->d_bad, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
   CK(cudaStreamSynchronize(x->stream));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
@@ -828,7 +859,7 @@ sw2g_status sw2g_step_close(sw2g_ctx* x) {
     return SW2G_ERR_CFL;
   }
   x->steps += 1;
-  if (bad) {
+  if (bad[0]) {
     x->err_step = (int)(x->steps - 1);
     return SW2G_ERR_NONFINITE;
   }
@@ -1066,11 +1097,12 @@ void sw2g_destroy(sw2g_ctx* x) {
   if (x->d_cfl) cudaFree(x->d_cfl);
   if (x->d_bad) cudaFree(x->d_bad);
   if (x->d_mask) cudaFree(x->d_mask);
+  if (x->h_chk) cudaFreeHost(x->h_chk);
   x->timers.release();
   x->run32.release();
   for (int e = 0; e < 2; e++)
     if (x->ev[e]) cudaEventDestroy(x->ev[e]);
-  for (int e = 0; e < 4; e++)
+  for (int e = 0; e < 6; e++)
     if (x->hev[e]) cudaEventDestroy(x->hev[e]);
   if (x->side) {
     cudaStreamSynchronize(x->side);

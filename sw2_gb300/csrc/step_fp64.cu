@@ -1030,7 +1030,9 @@ __global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double*
   const double be = QUARTER(al) * al;
   const double vn = (v[q] + dvab - be * v[q] - al * semi) / (1.0 + be);
   v[q] = vn;
-  check_range(bad, vn, i, j);
+  // a band's row ny is a wall: do_channel zeroes it before the range check
+  // (core.c:303-312), so the check sees +0 there
+  if (s.polar != 0 || j != s.ny) check_range(bad, vn, i, j);
 }
 
 template <int NZ>
@@ -1408,6 +1410,7 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     // AB3 of u and v folded into the Coriolis updates (core.c:271-285); the v
     // tendency does not depend on the new u
     LAUNCH("coriolis_u", fused_tail(s, g, st, F(), b, 1, fbad));
+    if (hk.u_out) cudaEventRecord(hk.u_out, st);  // u's interior is final
     LAUNCH("coriolis_v", fused_tail(s, g, st, F(), b, 2, fbad));
     rotate3(b.du);
     rotate3(b.dv);
@@ -1418,6 +1421,7 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     rotate3(b.dv);
     // Coriolis (core.c:282-285)
     LAUNCH("coriolis_u", k_coriolis_u<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.duAB));
+    if (hk.u_out) cudaEventRecord(hk.u_out, st);
     LAUNCH("coriolis_v", k_coriolis_v<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dvAB));
   }
 

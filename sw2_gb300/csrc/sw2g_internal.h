@@ -116,13 +116,16 @@ class Timers {
 // the tail the wall fixes and range checks (core.c:303-312); the reference's
 // forcing goes between them.
 constexpr int STEP_HEAD = 1, STEP_TAIL = 2, STEP_FULL = 3;
-// Events around eta within a step, for callers that overlap host copies with
-// it: the stream waits for eta_in before the first kernel that reads eta (the
-// advection of u and v, which do not read it, come first), and records
-// eta_out as soon as eta holds the step's result. Null events are skipped.
+// Events within a step, for callers that overlap host copies with it: the
+// stream waits for eta_in before the first kernel that reads eta (the
+// advection of u and v, which do not read it, come first), records eta_out as
+// soon as eta holds the step's result, and u_out once the interior of u does
+// (its halo columns and wall rows are still rewritten at the end of the
+// step). Null events are skipped.
 struct StepHooks {
   cudaEvent_t eta_in = nullptr;
   cudaEvent_t eta_out = nullptr;
+  cudaEvent_t u_out = nullptr;
 };
 int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, StepChecks chk, int step_slot,
               cudaStream_t st, Timers* tm, int parts = STEP_FULL, StepHooks hk = StepHooks{});

@@ -172,6 +172,26 @@ def test_gpu_nonfinite_values_follow_the_reference_checks(plant):
             assert same(got[q], o.field(q)), q
 
 
+def test_gpu_range_check_sees_the_wall_row_after_do_channel():
+    """A value beyond 1e10 that only ever reaches v on the north wall row
+    (from a huge eta in the halo row above it, kept by a raw upload) is zeroed
+    by do_channel before the range check runs (core.c:303-312), so the
+    reference does not abort; neither may the check fused into the step."""
+    case = cases.make_case(nx=40, ny=20, sch=2, seed=24)
+    f = [a.copy() for a in case.fields()]
+    f[0][case.params.ny + 2, 2:-2] = 1e17  # eta, halo row j = ny+1
+    s = lib.Solver(case.params)
+    s.upload(*f, mode=lib.UPLOAD_RAW)
+    o = orc.Oracle(case.params)
+    o.load(f, raw=True)
+    rc_o, bad = o.step(6)
+    assert rc_o == 0, bad
+    assert s.step(6) == lib.OK
+    got = s.download()
+    for q in FIELDS:
+        assert same(got[q], o.field(q)), q
+
+
 def test_gpu_energy_matches_oracle():
     case = cases.make_case(nx=96, ny=48, sch=2, seed=3, bumps=3)
     s, o = run_both(case, 30)
