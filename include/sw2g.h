@@ -257,6 +257,15 @@ void sw2g_batch_destroy(sw2g_batch *b);
 sw2g_status sw2g_selfcheck_division(const double *divisors, int n, long long samples, unsigned long long seed,
                                     int device, long long *mismatches);
 
+/* Self-check of the FP64 step's additions done on the integer pipe (a + b and
+ * a - b rounded to nearest even from the operands' bits; results must equal
+ * the FP64 unit's bit for bit, NaNs as NaNs). Draws `samples` operand pairs,
+ * random and at the adder's edge cases (cancellation, ties, carries, the
+ * overflow and subnormal limits, zeros, inf, NaN), on CUDA device `device`,
+ * and returns in *mismatches how many of the 2 * samples results differ.
+ * No counterpart in the reference. */
+sw2g_status sw2g_selfcheck_add(long long samples, unsigned long long seed, int device, long long *mismatches);
+
 /* Largest ny accepted by sw2g_energy_noalloc. */
 #define SW2G_NOALLOC_MAX_ROWS 8192
 

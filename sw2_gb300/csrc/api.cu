@@ -1168,6 +1168,30 @@ extern "C" sw2g_status sw2g_selfcheck_division(const double* divisors, int n, lo
   return rc;
 }
 
+extern "C" sw2g_status sw2g_selfcheck_add(long long samples, unsigned long long seed, int device,
+                                         long long* mismatches) {
+  if (samples < 1 || !mismatches) return SW2G_ERR_BAD_ARG;
+  CK(cudaSetDevice(device));
+  unsigned long long* bad = nullptr;
+  cudaStream_t st = nullptr;
+  auto run = [&]() -> sw2g_status {
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    CK(cudaMalloc((void**)&bad, sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned long long), st));
+    fp64_check_add(samples, seed, bad, st);
+    CK(cudaGetLastError());
+    unsigned long long h = 0;
+    CK(cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *mismatches = (long long)h;
+    return SW2G_OK;
+  };
+  const sw2g_status rc = run();
+  if (bad) cudaFree(bad);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}
+
 // ------------------------------------------------------------------ batches
 struct sw2g_batch {
   std::vector<sw2g_ctx*> mem;

@@ -6,9 +6,11 @@
 // a*b+c is fused: every expression keeps the association of the reference
 // expression it restates, which makes the results bit-identical to the
 // reference's own single-rank run. Divisions by a per-row metric factor go
-// through div_rcp (the same IEEE quotient with fewer FP64 instructions), and
+// through div_rcp (the same IEEE quotient with fewer FP64 instructions),
 // scalings by powers of two, zero numerators and bit tests are answered on
-// the integer pipe, since GB300 executes FP64 at 2 lanes per SM per clock.
+// the integer pipe, since GB300 executes FP64 at 2 lanes per SM per clock,
+// and so are some of the small kernels' additions (sadd, ssub: the same
+// IEEE sums).
 #include <cuda_runtime.h>
 
 #include "sw2g_internal.h"
@@ -71,6 +73,81 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
   const double q1 = __fma_rn(r0, y, q0);
   const double r1 = __fma_rn(-b, q1, a);
   return __fma_rn(r1, y, q1);
+}
+
+// a + b rounded to nearest, ties to even, computed on the integer pipe (the
+// textbook IEEE 754 adder: order the operands by magnitude, align the
+// smaller significand with ten guard bits and a sticky bit, add or subtract,
+// renormalise, round) when the operands are normal numbers, or one is a zero
+// and the other finite, and the sum is normal. Everything else (two zeros,
+// subnormals, inf, NaN, a sum that overflows or falls below the normal
+// range) adds on the FP64 unit, out of line. Exact cancellation gives +0, as
+// the FP64 unit's round-to-nearest does. fp64_check_add compares sadd and
+// ssub with the FP64 unit on random and edge-case operands.
+// An integer-pipe addition takes about a hundred instructions where the FP64
+// unit takes one, but GB300 issues 128 integer operations per SM and clock
+// against 2 FP64 lanes: the small kernels below are bound by the FP64 unit
+// with most issue slots idle, so moving some of their additions off it makes
+// them faster, up to the point where issue becomes the bound. Which additions
+// move was measured per kernel at 2048x1024 (CUDA-event times of each mix):
+// all of the Coriolis updates' and of the second velocity-Laplacian pass,
+// the two outer sums of the first pass, the final sum of the second
+// eta-Laplacian pass, the Adams-Bashforth and hyperviscosity sums, the two
+// tendency sums of k_pres_sum; none in the first eta-Laplacian pass (no gain)
+// or in the TVD bodies (their 96 registers per thread leave too few warps to
+// hide the longer dependency chains).
+__device__ __noinline__ double add_fp64(double a, double b) { return a + b; }
+__device__ __forceinline__ double sadd(double a, double b) {
+  constexpr unsigned long long MAG = 0x7fffffffffffffffULL, FRAC = 0x000fffffffffffffULL, ONE = 1ULL << 52;
+  unsigned long long A = (unsigned long long)dbits(a), B = (unsigned long long)dbits(b);
+  if ((A & MAG) < (B & MAG)) {  // |A| >= |B| from here on
+    const unsigned long long t = A;
+    A = B;
+    B = t;
+  }
+  const int ea = (int)((A >> 52) & 0x7ff), eb = (int)((B >> 52) & 0x7ff);
+  if ((B & MAG) == 0) {  // the smaller is a zero: the larger, if a finite nonzero
+    if ((A & MAG) != 0 && ea != 0x7ff) return __longlong_as_double((long long)A);
+    return add_fp64(a, b);
+  }
+  if (ea == 0x7ff || eb == 0) return add_fp64(a, b);  // inf, NaN or a subnormal operand
+  const int d = ea - eb;
+  const unsigned long long ma = ((A & FRAC) | ONE) << 10;  // significand at bits 62..10
+  unsigned long long mb = ((B & FRAC) | ONE) << 10;
+  if (d >= 63) {
+    mb = 1;  // only the sticky bit is left
+  } else if (d > 0) {
+    mb = (mb >> d) | ((mb << (64 - d)) != 0 ? 1ULL : 0ULL);
+  }
+  int e = ea;
+  unsigned long long m;
+  if (((A ^ B) >> 63) == 0) {
+    m = ma + mb;
+    if (m >> 63) {  // carry: one bit right, keeping the sticky bit
+      m = (m >> 1) | (m & 1ULL);
+      e += 1;
+    }
+  } else {
+    m = ma - mb;
+    if (m == 0) return 0.0;
+    const int lz = __clzll((long long)m) - 1;  // back to bit 62 (at most one place when bits were lost)
+    m <<= lz;
+    e -= lz;
+  }
+  unsigned long long r = m >> 10;
+  const unsigned long long rem = m & 0x3ffULL;
+  if (rem > 0x200ULL || (rem == 0x200ULL && (r & 1ULL))) r += 1;
+  if (r >> 53) {
+    r >>= 1;
+    e += 1;
+  }
+  if (e <= 0 || e >= 0x7ff) return add_fp64(a, b);
+  return __longlong_as_double((long long)((A & ~MAG) | ((unsigned long long)e << 52) | (r & FRAC)));
+}
+// a - b = a + (-b), exactly and for every operand (a NaN operand gives a
+// NaN either way; NaN bit patterns are not compared anywhere).
+__device__ __forceinline__ double ssub(double a, double b) {
+  return sadd(a, __longlong_as_double(dbits(b) ^ (long long)0x8000000000000000ULL));
 }
 
 // calc.c:54-63 with sw.h:104-105 MIN/MAX as ternaries (NaN order as written).
@@ -670,6 +747,68 @@ __global__ void k_check_division(const double* div, int n, long long samples, un
   if (miss) atomicAdd(bad, miss);
 }
 
+// Self-check of sadd and ssub against the FP64 unit: operand pairs from a
+// SplitMix64 stream, in classes that reach every branch of the adder: any two
+// normal numbers; exponents within 64 of each other (alignment, carries,
+// cancellation); b = -a give or take a few ulps (total and near-total
+// cancellation); b a tie (an odd multiple of half an ulp of a); sums near
+// the overflow and subnormal limits; zeros, subnormals, inf and NaN.
+__device__ __forceinline__ double rnd_double(unsigned long long r, int e, bool neg) {
+  return __longlong_as_double((long long)(((unsigned long long)e << 52) | (r & 0xFFFFFFFFFFFFFULL) |
+                                          (neg ? 1ULL << 63 : 0ULL)));
+}
+__global__ void k_check_add(long long samples, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long miss = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < samples;
+       t += (long long)gridDim.x * blockDim.x) {
+    unsigned long long st = seed ^ (unsigned long long)t * 0xD1B54A32D192ED03ULL;
+    const unsigned long long r1 = splitmix(st), r2 = splitmix(st), r3 = splitmix(st);
+    const int cls = (int)(r3 % 8);
+    double a, b;
+    if (cls == 0) {
+      a = rnd_double(r1, 1 + (int)((r3 >> 8) % 2046), r2 & 1);
+      b = rnd_double(r2, 1 + (int)((r3 >> 20) % 2046), r2 & 2);
+    } else if (cls <= 2) {
+      const int e = 70 + (int)((r3 >> 8) % 1900);
+      a = rnd_double(r1, e, r2 & 1);
+      b = rnd_double(r2, e - (int)((r3 >> 20) % 64), r2 & 2);
+    } else if (cls == 3) {
+      a = rnd_double(r1, 3 + (int)((r3 >> 8) % 2040), r2 & 1);
+      b = __longlong_as_double((dbits(a) ^ (long long)0x8000000000000000ULL) + (long long)((r2 >> 8) % 9) - 4);
+    } else if (cls == 4) {  // |b| = k/2 ulp(a), k odd, with or without a few more low bits
+      const int e = 60 + (int)((r3 >> 8) % 1900);
+      a = rnd_double(r1, e, r2 & 1);
+      const double k = (double)(2 * ((r2 >> 8) % 16) + 1);
+      b = k * __longlong_as_double((long long)((unsigned long long)(e - 53) << 52));
+      if (r2 & 4) b = __longlong_as_double(dbits(b) + (long long)((r2 >> 20) % 3) - 1);
+      if (r2 & 2) b = -b;
+    } else if (cls == 5) {  // near the top of the range
+      a = rnd_double(r1, 2046 - (int)((r3 >> 8) % 3), r2 & 1);
+      b = rnd_double(r2, 2046 - (int)((r3 >> 20) % 60), r2 & 2);
+    } else if (cls == 6) {  // near the bottom: subnormal sums and operands
+      a = rnd_double(r1, (int)((r3 >> 8) % 4), r2 & 1);
+      b = rnd_double(r2, (int)((r3 >> 20) % 60), r2 & 2);
+    } else {  // zeros, inf, NaN against anything
+      const double sp[6] = {0.0, -0.0, __longlong_as_double(0x7ff0000000000000LL),
+                            __longlong_as_double((long long)0xfff0000000000000ULL),
+                            __longlong_as_double(0x7ff8000000000000LL), 1.0};
+      a = sp[(r3 >> 8) % 6];
+      b = (r2 & 1) ? sp[(r3 >> 20) % 6] : rnd_double(r2, 1 + (int)((r3 >> 24) % 2046), r2 & 2);
+      if (r2 & 4) {
+        const double t = a;
+        a = b;
+        b = t;
+      }
+    }
+    const double s1 = a + b, s2 = sadd(a, b), d1 = a - b, d2 = ssub(a, b);
+    const bool nan1 = (dbits(s1) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    const bool nan2 = (dbits(d1) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    if (nan1 ? !((dbits(s2) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) : dbits(s1) != dbits(s2)) miss++;
+    if (nan2 ? !((dbits(d2) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) : dbits(d1) != dbits(d2)) miss++;
+  }
+  if (miss) atomicAdd(bad, miss);
+}
+
 // do_AdamsBashforth (calc.c:651-699) via copy_scaf/linop_scaf (sppde_core.c:247-298)
 __global__ void k_ab(DevState s, int k, double* ab, const double* dn, const double* dm1, const double* dm2) {
   INTERIOR_IJ
@@ -772,8 +911,9 @@ __global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* x
 __global__ void k_lape_pass2(DevState s, const double* psi, const double* xi, double* eo) {
   INTERIOR_IJ
   const int q = IX(W, i, j);
-  const double v = RW(s, R_KC, j) * (div_rcp(psi[q] - psi[IX(W, i - 1, j)], RW(s, R_DXE, j), RW(s, R_IDXE, j)) +
-                                     div_rcp(xi[q] - xi[IX(W, i, j - 1)], RW(s, R_DYN, j), RW(s, R_IDYN, j)));
+  const double v =
+      RW(s, R_KC, j) * sadd(div_rcp(psi[q] - psi[IX(W, i - 1, j)], RW(s, R_DXE, j), RW(s, R_IDXE, j)),
+                        div_rcp(xi[q] - xi[IX(W, i, j - 1)], RW(s, R_DYN, j), RW(s, R_IDYN, j)));
   put_images<HK_LE>(s, eo, i, j, v);
 }
 
@@ -805,7 +945,7 @@ __device__ __forceinline__ double hyper_terms(const DevState& s, double x, const
 #pragma unroll
     for (int t = 0; t < 3; t++) {
       const double v = V[t];
-      if ((NZ >> t) & 1) x = x + nd[t] * v;
+      if ((NZ >> t) & 1) x = sadd(x, nd[t] * v);
       else if (!zero_term_is_exact(x, v)) x = add_product(x, nd[t], v);
     }
     return x;
@@ -862,16 +1002,16 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
   const double mgn = s.polar ? -PF(s, P_GN, q) * s.Dt : RW(s, R_MGNDT, j);
   const double dup = div_rcp(mge * (e[IX(W, i + 1, j)] - e[q]), RW(s, R_DXC, j), RW(s, R_IDXC, j));
   const double dvp = div_rcp(mgn * (e[IX(W, i, j + 1)] - e[q]), RW(s, R_DYC, j + 1), RW(s, R_IDYC, j + 1));
-  double a = duadv[q] + dup;
-  double b = dvadv[q] + dvp;
+  double a = sadd(duadv[q], dup);
+  double b = sadd(dvadv[q], dvp);
   if constexpr (UD) {
     const double U = f.u[q], V = f.v[q];
     if (!zero_term_is_exact(a, U)) a = minus_damping(a, U, s.sigma, s.Dt);
     if (!zero_term_is_exact(b, V)) b = minus_damping(b, V, s.sigma, s.Dt);
   } else {
     const double su = s.polar ? PF(s, P_SU, q) : s.sigma, sv = s.polar ? PF(s, P_SV, q) : s.sigma;  // calc.c:374-394
-    a -= f.u[q] * su * s.Dt;
-    b -= f.v[q] * sv * s.Dt;
+    a = ssub(a, f.u[q] * su * s.Dt);
+    b = ssub(b, f.v[q] * sv * s.Dt);
   }
   dun[q] = a;
   dvn[q] = b;
@@ -897,10 +1037,10 @@ __global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, dou
     const double pu1 = RW(s, R_DXC, j + 1) * uu[IX(W, i, j + 1)];
     const double qv1 = RW(s, R_DXV, j) * vv[q];
     double a = RW(s, R_IDXV, j), b = -RW(s, R_IDYC, j + 1);
-    const double z = a * ((vv[IX(W, i + 1, j)] - vv[q]) + b * (pu1 - pu));
+    const double z = a * sadd((vv[IX(W, i + 1, j)] - vv[q]), b * (pu1 - pu));
     a = RW(s, R_IDXE, j);
     b = RW(s, R_IDYN, j);
-    const double d = a * ((uu[q] - uu[IX(W, i - 1, j)]) + b * (qv1 - qv));
+    const double d = a * sadd((uu[q] - uu[IX(W, i - 1, j)]), b * (qv1 - qv));
     put_images<HK_ZE>(s, ze, i, j, z);
     put_images<HK_DI>(s, di, i, j, d);
     if (j == s.ny && s.polar == 0)  // laplacian.c:73
@@ -916,10 +1056,10 @@ __global__ void k_lapv_pass2(DevState s, const double* ze, const double* di, dou
   INTERIOR_IJ
   const int q = IX(W, i, j);
   double a = -RW(s, R_IDYN, j), b = RW(s, R_IDXC, j);
-  const double vu = a * (ze[q] - ze[IX(W, i, j - 1)]) + b * (di[IX(W, i + 1, j)] - di[q]);
+  const double vu = sadd(a * ssub(ze[q], ze[IX(W, i, j - 1)]), b * ssub(di[IX(W, i + 1, j)], di[q]));
   a = RW(s, R_IDXV, j);
   b = RW(s, R_IDYC, j + 1);
-  const double vl = a * (ze[q] - ze[IX(W, i - 1, j)]) + b * (di[IX(W, i, j + 1)] - di[q]);
+  const double vl = sadd(a * ssub(ze[q], ze[IX(W, i - 1, j)]), b * ssub(di[IX(W, i, j + 1)], di[q]));
   put_images<HK_LU>(s, lu, i, j, vu);
   put_images<HK_LV>(s, lv, i, j, vl);
 }
@@ -931,7 +1071,7 @@ __global__ void k_coriolis_u(DevState s, double* u, const double* v, const doubl
   const int q = IX(W, i, j);
   const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
   const double dtf = s.polar ? s.Dt * PF(s, P_FE, q) : RW(s, R_DTFE, j);  // Dt*FE, calc.c:563
-  const double al = dtf + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
+  const double al = sadd(dtf, div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j)));
   const double be = 0.25 * al * al;
   u[q] = (u[q] + duab[q] - be * u[q] + al * semi) / (1.0 + be);
 }
@@ -942,7 +1082,7 @@ __global__ void k_coriolis_v(DevState s, const double* u, double* v, const doubl
   const int q = IX(W, i, j);
   const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
   const double dtf = s.polar ? s.Dt * PF(s, P_FN, q) : RW(s, R_DTFN, j);  // Dt*FN, calc.c:592
-  const double al = dtf + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
+  const double al = sadd(dtf, div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j)));
   const double be = 0.25 * al * al;
   v[q] = (v[q] + dvab[q] - be * v[q] - al * semi) / (1.0 + be);
 }
@@ -963,8 +1103,8 @@ __device__ __forceinline__ bool range_bad(double x, bool first) {
 //   eta: the geofactor (calc.c:403-422) and eta += D (core.c:203-205);
 //   u, v: the Coriolis update (calc.c:542-598).
 __device__ __forceinline__ double ab3(double dn, double dm1, double dm2) {
-  const double t = -(4.0 / 3.0) * dm1 + +(5.0 / 12.0) * dm2;
-  return (23.0 / 12.0) * dn + 1.0 * t;
+  const double t = sadd(-(4.0 / 3.0) * dm1, +(5.0 / 12.0) * dm2);
+  return sadd((23.0 / 12.0) * dn, t);  // 1.0 * t is t
 }
 // v + (+0): v, except that -0 becomes +0 (the plain form's zero winds).
 __device__ __forceinline__ double plus_pos_zero(double v) {
@@ -1006,11 +1146,12 @@ __global__ void k_coriolis_u_ab3(DevState s, double* u, const double* v, double*
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
   if constexpr (NZ != kNoHyper) dn[q] = x;
   const double duab = ab3(x, dm1[q], dm2[q]);
-  const double semi = QUARTER(v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
+  const double semi =
+      QUARTER(sadd(sadd(sadd(v[IX(W, i, j)], v[IX(W, i + 1, j)]), v[IX(W, i, j - 1)]), v[IX(W, i + 1, j - 1)]));
   const double dtf = s.polar ? s.Dt * PF(s, P_FE, q) : RW(s, R_DTFE, j);
-  const double al = dtf + div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j));
+  const double al = sadd(dtf, div_rcp(s.Dt * u[q] * RW(s, R_SINC, j), RW(s, R_RZC, j), RW(s, R_IRZC, j)));
   const double be = QUARTER(al) * al;
-  const double un = (u[q] + duab - be * u[q] + al * semi) / (1.0 + be);
+  const double un = sadd(ssub(sadd(u[q], duab), be * u[q]), al * semi) / sadd(1.0, be);
   u[q] = un;
   check_range(bad, un, i, j);
 }
@@ -1024,11 +1165,12 @@ __global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double*
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
   if constexpr (NZ != kNoHyper) dn[q] = x;
   const double dvab = ab3(x, dm1[q], dm2[q]);
-  const double semi = QUARTER(u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
+  const double semi =
+      QUARTER(sadd(sadd(sadd(u[IX(W, i - 1, j + 1)], u[IX(W, i, j + 1)]), u[IX(W, i, j)]), u[IX(W, i - 1, j)]));
   const double dtf = s.polar ? s.Dt * PF(s, P_FN, q) : RW(s, R_DTFN, j);
-  const double al = dtf + div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j));
+  const double al = sadd(dtf, div_rcp(s.Dt * semi * RW(s, R_SINN, j), RW(s, R_RZN, j), RW(s, R_IRZN, j)));
   const double be = QUARTER(al) * al;
-  const double vn = (v[q] + dvab - be * v[q] - al * semi) / (1.0 + be);
+  const double vn = ssub(ssub(sadd(v[q], dvab), be * v[q]), al * semi) / sadd(1.0, be);
   v[q] = vn;
   // a band's row ny is a wall: do_channel zeroes it before the range check
   // (core.c:303-312), so the check sees +0 there
@@ -1293,6 +1435,10 @@ void fp64_set_where(double* f, const double* val, const unsigned char* mask, int
 
 void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, cudaStream_t st) {
   k_channel<<<(nx + 127) / 128, 128, 0, st>>>(nx, ny, u, v, wx, wy);
+}
+
+void fp64_check_add(long long samples, unsigned long long seed, unsigned long long* bad, cudaStream_t st) {
+  k_check_add<<<152 * 8, 256, 0, st>>>(samples, seed, bad);
 }
 
 void fp64_check_division(const double* d_div, int n, long long samples, unsigned long long seed,

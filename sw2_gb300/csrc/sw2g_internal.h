@@ -139,6 +139,9 @@ void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, 
 // *bad (device pointer) once the stream is done.
 void fp64_check_division(const double* d_div, int n, long long samples, unsigned long long seed,
                          unsigned long long* bad, cudaStream_t st);
+// Compares the step's integer-pipe additions (sadd, ssub) with the FP64
+// unit's on `samples` operand pairs; mismatch count in *bad (device pointer).
+void fp64_check_add(long long samples, unsigned long long seed, unsigned long long* bad, cudaStream_t st);
 // FP32 precision form (step_fp32.cu). Per-row FP32 constants, index j+1.
 enum Q32 {
   Q_KXE, Q_KYN, Q_KXC, Q_KYV, Q_KXV, Q_KYC,  // Dt/DXE, Dt/DYN, Dt/DXC, Dt/DYV, Dt/DXV, Dt/DYC

@@ -33,6 +33,7 @@ SYMBOLS = [
     "sw2g_timer_read", "sw2g_selfcheck_division", "sw2g_add_field", "sw2g_set_field_where",
     "sw2g_apply_channel", "sw2g_step_open", "sw2g_step_close", "sw2g_checkpoint_doubles",
     "sw2g_checkpoint_save", "sw2g_checkpoint_load", "sw2g_test_tile_timeout", "sw2g_step_host",
+    "sw2g_selfcheck_add",
 ]
 
 
@@ -107,6 +108,18 @@ def selfcheck_division(divisors, samples: int, seed: int = 1, device: int = 0) -
     rc = L.sw2g_selfcheck_division(_ptr(d), len(d), int(samples), int(seed), int(device), ctypes.byref(out))
     if rc != OK:
         raise SW2GError(rc, "sw2g_selfcheck_division")
+    return out.value
+
+
+def selfcheck_add(samples: int, seed: int = 1, device: int = 0) -> int:
+    """Mismatches of the step's integer-pipe additions against the FP64 unit."""
+    L = load()
+    L.sw2g_selfcheck_add.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_longlong)]
+    out = ctypes.c_longlong()
+    rc = L.sw2g_selfcheck_add(int(samples), int(seed), int(device), ctypes.byref(out))
+    if rc != OK:
+        raise SW2GError(rc, "sw2g_selfcheck_add")
     return out.value
 
 

@@ -2,7 +2,8 @@
 with multiplications and fused multiply-adds using each factor's correctly
 rounded reciprocal (Markstein's method). Its quotients must equal IEEE
 division bit for bit; the library's self-check draws random numerators and
-numerators whose quotient lies next to a rounding midpoint."""
+numerators whose quotient lies next to a rounding midpoint. The same holds
+for the additions the step computes on the integer pipe."""
 import numpy as np
 import pytest
 
@@ -35,3 +36,10 @@ def test_random_divisors_match_ieee():
     # significands with all-ones tails and powers of two
     d = np.concatenate([d, np.nextafter(np.ldexp(1.0, np.arange(-20, 40)), 0), np.ldexp(1.0, np.arange(-20, 40))])
     assert lib.selfcheck_division(d, samples=5_000, seed=12) == 0
+
+
+def test_integer_pipe_addition_matches_the_fp64_unit():
+    """The step's additions on the integer pipe (sadd, ssub) against the FP64
+    unit: 2^27 operand pairs per seed over the adder's edge cases."""
+    for seed in (21, 22, 23):
+        assert lib.selfcheck_add(samples=1 << 27, seed=seed) == 0
