@@ -93,9 +93,11 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
 // all of the Coriolis updates' and of the second velocity-Laplacian pass,
 // the two outer sums of the first pass, the final sum of the second
 // eta-Laplacian pass, the Adams-Bashforth and hyperviscosity sums, the two
-// tendency sums of k_pres_sum; none in the first eta-Laplacian pass (no gain)
-// or in the TVD bodies (their 96 registers per thread leave too few warps to
-// hide the longer dependency chains).
+// tendency sums of k_pres_sum; in the TVD bodies only the four-face sum of a
+// cell and, in the mass body, the last sum of each side term (their 96
+// registers per thread leave too few warps to hide longer chains: more
+// integer-pipe additions there made them slower); none in the first
+// eta-Laplacian pass (no gain).
 __device__ __noinline__ double add_fp64(double a, double b) { return a + b; }
 __device__ __forceinline__ double sadd(double a, double b) {
   constexpr unsigned long long MAG = 0x7fffffffffffffffULL, FRAC = 0x000fffffffffffffULL, ONE = 1ULL << 52;
@@ -398,10 +400,13 @@ __device__ __forceinline__ double half_psi(double n, double d) {
 
 // c*B of one side: B2BP (pos) = q0 + psi*0.5*(1-c)*(q1-q0), or B2BM =
 // q1 - psi*0.5*(1+c)*(q1-q0); 1 + c = 1 - (-c) and q1 - X = q1 + (-X) exactly.
+// SB: the last sum on the integer pipe (measured faster in the mass body only).
+template <bool SB>
 __device__ __forceinline__ double side_term(bool pos, double c, double hpsi, double q0, double q1, double d) {
   const double g = 1.0 - (pos ? c : -c);
   const double X = (hpsi * g) * d;
-  return c * ((pos ? q0 : q1) + (pos ? X : -X));
+  if constexpr (SB) return c * sadd(pos ? q0 : q1, pos ? X : -X);
+  else return c * ((pos ? q0 : q1) + (pos ? X : -X));
 }
 
 // Shared part of a face q0|q1 (outer neighbours qm, q2), with the Courant
@@ -435,14 +440,15 @@ __device__ __forceinline__ Face make_face(double qm, double q0, double q1, doubl
 }
 
 // The face's two terms for a cell whose metric divisor is dx (idx = 1.0/dx).
+template <bool SB>
 __device__ __forceinline__ void face_terms(const Face& F, double Dt, double dx, double idx, double& tP,
                                            double& tM) {
   const double c1 = div_rcp((F.pos1 ? F.pn : F.mn) * Dt, dx, idx);
-  const double t1 = F.act ? side_term(F.pos1, c1, F.hp1, F.q0, F.q1, F.d) : 0.0;
+  const double t1 = F.act ? side_term<SB>(F.pos1, c1, F.hp1, F.q0, F.q1, F.d) : 0.0;
   tP = F.pos1 ? t1 : 0.0;
   tM = F.pos1 ? 0.0 : t1;
   if (__any_sync(FULL, F.both)) {
-    if (F.both) tM = side_term(false, div_rcp(F.mn * Dt, dx, idx), F.hp2, F.q0, F.q1, F.d);
+    if (F.both) tM = side_term<SB>(false, div_rcp(F.mn * Dt, dx, idx), F.hp2, F.q0, F.q1, F.d);
   }
 }
 #define ROW2(t, it, j) RW(s, t, j), RW(s, it, j)
@@ -473,7 +479,7 @@ __device__ __forceinline__ double sum_faces(const Side& w, const Side& e, const 
     return sum_faces8(w.P, w.M, e.P, e.M, so.P, so.M, n.P, n.M);
   const double tw = w.pos ? w.P : w.M, te = e.pos ? e.P : e.M;
   const double ts = so.pos ? so.P : so.M, tn = n.pos ? n.P : n.M;
-  return ((tw - te) + ts) - tn;
+  return ssub(sadd(ssub(tw, te), ts), tn);
 }
 __device__ __forceinline__ Side east_of(const Side& w, int lane) {
   Side e;
@@ -483,9 +489,10 @@ __device__ __forceinline__ Side east_of(const Side& w, int lane) {
   e.both = __shfl_sync(FULL, (int)w.both, (lane + 1) & 31) != 0;
   return e;
 }
+template <bool SB = false>
 __device__ __forceinline__ Side side_of(const Face& F, double Dt, double dx, double idx) {
   Side t;
-  face_terms(F, Dt, dx, idx, t.P, t.M);
+  face_terms<SB>(F, Dt, dx, idx, t.P, t.M);
   t.pos = F.pos1;
   t.both = F.both;
   return t;
@@ -555,7 +562,7 @@ __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_mass_fast(DevS
   {
     const double b = VF(ic, j0 - 1);
     const Face F = make_face<SCH>(HF(ic, j0 - 2), h1, h2, h3, up_p(b), up_m(b), fin(b));
-    ts = side_of(F, Dt, ROW2(R_DYN, R_IDYN, j0));
+    ts = side_of<true>(F, Dt, ROW2(R_DYN, R_IDYN, j0));
     oks = F.ok;
   }
   for (int j = j0; j <= jn; j++) {
@@ -564,14 +571,14 @@ __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_mass_fast(DevS
     const XN xn = x_neighbours(h2, HF(ia, j), lane);
     const double a = UF(iu, j);
     const Face FX = make_face<SCH>(xn.m2, xn.m1, h2, xn.p1, up_p(a), up_m(a), fin(a));
-    const Side tw = side_of(FX, Dt, ROW2(R_DXE, R_IDXE, j));
+    const Side tw = side_of<true>(FX, Dt, ROW2(R_DXE, R_IDXE, j));
     const Side te = east_of(tw, lane);
     const bool oke = __shfl_sync(FULL, (int)FX.ok, (lane + 1) & 31) != 0;
     // y face north of row j: shared by this cell and the cell above
     const double b = VF(ic, j);
     const Face FY = make_face<SCH>(h1, h2, h3, h4, up_p(b), up_m(b), fin(b));
-    const Side tn = side_of(FY, Dt, ROW2(R_DYN, R_IDYN, j));
-    const Side ns = side_of(FY, Dt, ROW2(R_DYN, R_IDYN, j + 1));
+    const Side tn = side_of<true>(FY, Dt, ROW2(R_DYN, R_IDYN, j));
+    const Side ns = side_of<true>(FY, Dt, ROW2(R_DYN, R_IDYN, j + 1));
     const double S = sum_faces(tw, te, ts, tn);  // calc.c:100 in its order: +w -e +s -n
     const bool slow = !(FX.ok && oke && oks && FY.ok) || !nz(S);
     if (own) {
