@@ -73,16 +73,16 @@ KERNEL_BYTES = {
 # third step). With zero winds the plain bodies read eta or u and v only; part
 # of each input is still in L2 from the kernel before, and most of the output
 # leaves L2 later, so DRAM bytes are below the algorithmic bytes.
-NCU_TRAFFIC = {("band2048", "mass"): 57.15e6, ("band2048", "adv_u"): 36.03e6, ("band2048", "adv_v"): 36.00e6}
+NCU_TRAFFIC = {("band2048", "mass"): 57.15e6, ("band2048", "adv_u"): 37.34e6, ("band2048", "adv_v"): 36.00e6}
 # FP64 thread instructions (DADD + DMUL + DFMA) per interior cell of the
 # dominant kernels on the 2048x1024 workload, from ncu's instruction counters
 # of the same step (profiles/fp64_step_band2048_fp64_instruction_counts.md),
 # and GB300's FP64 peak per cycle over the whole GPU (ncu's peak for DFMA:
 # 304 = 2 lanes per SM x 152 SMs). The FP64 form is bound by this unit.
-NCU_FP64_PER_CELL = {("band2048", "mass"): 63.3, ("band2048", "adv_u"): 78.4, ("band2048", "adv_v"): 78.8}
+NCU_FP64_PER_CELL = {("band2048", "mass"): 57.9, ("band2048", "adv_u"): 76.3, ("band2048", "adv_v"): 76.7}
 FP64_LANES_PER_CYCLE = 304
 # The whole step: read eta u v, write eta u v, read two history levels of
-# three tendencies, write one (SURVEY-style count for the FP64 form).
+# three tendencies, write one (a per-cell count for the step's GB/s figure).
 STEP_BYTES = 120
 
 
@@ -106,8 +106,9 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{device}.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else f"/tmp/sw2g_clocks_{os.getpid()}.csv"
+        # the raw samples: a folder named by SW2G_CLOCKS_DIR, else /tmp
+        out = os.environ.get("SW2G_CLOCKS_DIR") or "/tmp"
+        self.path = os.path.join(out, f"sw2g_clocks_rank{device}_{os.getpid()}.csv")
 
     def __enter__(self):
         try:

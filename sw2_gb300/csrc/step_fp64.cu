@@ -78,12 +78,12 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
 // a + b rounded to nearest, ties to even, computed on the integer pipe (the
 // textbook IEEE 754 adder: order the operands by magnitude, align the
 // smaller significand with ten guard bits and a sticky bit, add or subtract,
-// renormalise, round) when the operands are normal numbers, or one is a zero
-// and the other finite, and the sum is normal. Everything else (two zeros,
-// subnormals, inf, NaN, a sum that overflows or falls below the normal
-// range) adds on the FP64 unit, out of line. Exact cancellation gives +0, as
-// the FP64 unit's round-to-nearest does. fp64_check_add compares sadd and
-// ssub with the FP64 unit on random and edge-case operands.
+// renormalise, round) when both operands and the sum are normal numbers. A
+// zero operand gives the other operand (two zeros give -0 only if both are
+// -0), and exact cancellation gives +0, as the FP64 unit's round-to-nearest
+// does. Everything else (subnormals, inf, NaN, a sum that overflows or falls
+// below the normal range) adds on the FP64 unit, out of line. fp64_check_add
+// compares sadd and ssub with the FP64 unit on random and edge-case operands.
 // An integer-pipe addition takes about a hundred instructions where the FP64
 // unit takes one, but GB300 issues 128 integer operations per SM and clock
 // against 2 FP64 lanes: the small kernels below are bound by the FP64 unit
@@ -108,10 +108,9 @@ __device__ __forceinline__ double sadd(double a, double b) {
     B = t;
   }
   const int ea = (int)((A >> 52) & 0x7ff), eb = (int)((B >> 52) & 0x7ff);
-  if ((B & MAG) == 0) {  // the smaller is a zero: the larger, if a finite nonzero
-    if ((A & MAG) != 0 && ea != 0x7ff) return __longlong_as_double((long long)A);
-    return add_fp64(a, b);
-  }
+  if ((B & MAG) == 0)  // the smaller is a zero: the larger (a NaN stays a NaN);
+    // two zeros: -0 if both are, else +0
+    return __longlong_as_double((long long)(((A & MAG) == 0) ? (A & B) : A));
   if (ea == 0x7ff || eb == 0) return add_fp64(a, b);  // inf, NaN or a subnormal operand
   const int d = ea - eb;
   const unsigned long long ma = ((A & FRAC) | ONE) << 10;  // significand at bits 62..10
