@@ -1028,8 +1028,9 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
 // laplacian.c:67-81). A thread marches down LV_ROWS rows of its column, so
 // the products DXC(j+1)*u(i,j+1) and DXV(j)*v(i,j) of one row are the
 // DXC(j)*u(i,j) and DXV(j-1)*v(i,j-1) of the next: the same operands and the
-// same products, formed once.
-constexpr int LV_ROWS = 8;
+// same products, formed once. Four rows (measured against 2, 8 and 16 at
+// 2048x1024) keep enough threads in flight for the integer-pipe additions.
+constexpr int LV_ROWS = 4;
 __global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, double* ze, double* di) {
   const int W = s.W;
   const int i = blockIdx.x * TX + threadIdx.x + 1;
