@@ -147,6 +147,7 @@ struct sw2g_ctx {
   std::vector<double*> allocs;
   unsigned long long* d_cfl = nullptr;
   int* d_bad = nullptr;
+  unsigned* d_strips = nullptr;  // DevState::strips
   double* d_energy = nullptr;  // 3*ny row partials + 3 totals
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -567,6 +568,10 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
     return fail(st);
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_bad, sizeof(int) * kChunk), "bad")) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaMalloc((void**)&x->d_strips, 2 * sizeof(unsigned)), "strips")) != SW2G_OK) return fail(st);
+  if ((st = cuda_fail(cudaMemsetAsync(x->d_strips, 0, 2 * sizeof(unsigned), x->stream), "strips")) != SW2G_OK)
+    return fail(st);
+  x->s.strips = x->d_strips;
   {
     const size_t b64 = sizeof(unsigned long long) * 2 * kChunk, b32 = sizeof(unsigned) * 2 * kChunk;
     if ((st = cuda_fail(cudaHostAlloc(&x->h_chk, b64 + b32 + sizeof(int) * kChunk, cudaHostAllocDefault),
@@ -1096,6 +1101,7 @@ void sw2g_destroy(sw2g_ctx* x) {
   for (void* p : x->allocs32) cudaFree(p);
   if (x->d_cfl) cudaFree(x->d_cfl);
   if (x->d_bad) cudaFree(x->d_bad);
+  if (x->d_strips) cudaFree(x->d_strips);
   if (x->d_mask) cudaFree(x->d_mask);
   if (x->h_chk) cudaFreeHost(x->h_chk);
   x->timers.release();

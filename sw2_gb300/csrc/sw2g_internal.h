@@ -52,6 +52,7 @@ struct DevState {
   int plain;           // windx, windy and hB are +0.0 in every padded cell
   int lape_eta;        // laplacian_eta of eta instead of u (SW2G_FLAG_LAPE_ETA)
   int fk;              // rows per strip of the fast TVD bodies (set per launch)
+  unsigned* strips;    // the fast bodies' strip queue: next strip, warps done (zero between launches)
   int polar;           // 0: band; +-1: polar cap, with the fields below
   const double* pf;    // P_NUM * W * H (polar only)
 };
