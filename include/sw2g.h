@@ -124,10 +124,12 @@ sw2g_status sw2g_step_close(sw2g_ctx *ctx);
  * arrays, as the reference's loop keeps SW->eta, SW->u and SW->v (core.c:134-338):
  * copies eta, u and v in (as sw2g_upload with SW2G_UPLOAD_CONTINUE), advances
  * nsteps steps (as sw2g_step) and copies the new state back into the same
- * arrays (as sw2g_download), also when a step fails. In the FP64 form the
- * copies of eta overlap the step: it goes in while the step's first kernels,
- * which read only u and v, run, and comes out while the step goes on with u
- * and v. Needs an earlier sw2g_upload (winds, bottom, tracer, history). */
+ * arrays (as sw2g_download), also when a step fails. In the FP64 form most
+ * of the copies overlap the step: v and eta go in while the step's first
+ * kernels, which read only u (the eta Laplacians) or only u and v (the
+ * advection of u and v), run; eta comes out while the step goes on with u
+ * and v, and u while it computes v. Needs an earlier sw2g_upload (winds,
+ * bottom, tracer, history). */
 sw2g_status sw2g_step_host(sw2g_ctx *ctx, double *eta, double *u, double *v, int nsteps);
 
 /* Step index of the last CFL/range failure, -1 if none. */

@@ -175,11 +175,11 @@ struct sw2g_ctx {
   // forcing between steps (FP64 form): staging of one padded field and a mask
   double* d_force = nullptr;
   void* d_mask = nullptr;
-  // sw2g_step_host: a second stream for the copies of eta and u, and the
-  // events u/v copied in, eta copied in, eta final, side copies done, u's
-  // interior final, step done (made on first use)
+  // sw2g_step_host: a second stream for the copies of v, eta and u, and the
+  // events u copied in, eta copied in, eta final, side copies done, u's
+  // interior final, step done, v copied in (made on first use)
   cudaStream_t side = nullptr;
-  cudaEvent_t hev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t hev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   // pinned host copies of a chunk's checks (CFL maxima of either form, range
   // flags), so that reading them back is one more asynchronous copy
   void* h_chk = nullptr;
@@ -688,15 +688,17 @@ sw2g_status sw2g_step_host(sw2g_ctx* x, double* eta, double* u, double* v, int n
   CK(cudaSetDevice(x->device));
   if (!x->side) {
     CK(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
-    for (int e = 0; e < 6; e++) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
+    for (int e = 0; e < 7; e++) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
   }
-  // u and v first: the step's first kernels (the CFL maxima, the advection
-  // of u and v) read only them, while eta is still on its way in.
+  // u first, then v and eta on the side stream: the step's first kernels
+  // (the eta Laplacians) read only u, the next ones (the CFL maxima, the
+  // advection of u and v) u and v, while eta is still on its way in.
   const size_t bytes = sizeof(double) * (size_t)x->s.W * x->s.H;
   CK(cudaMemcpyAsync(x->b.f[1], u, bytes, cudaMemcpyHostToDevice, x->stream));
-  CK(cudaMemcpyAsync(x->b.f[2], v, bytes, cudaMemcpyHostToDevice, x->stream));
   CK(cudaEventRecord(x->hev[0], x->stream));
   CK(cudaStreamWaitEvent(x->side, x->hev[0], 0));
+  CK(cudaMemcpyAsync(x->b.f[2], v, bytes, cudaMemcpyHostToDevice, x->side));
+  CK(cudaEventRecord(x->hev[6], x->side));
   CK(cudaMemcpyAsync(x->b.f[0], eta, bytes, cudaMemcpyHostToDevice, x->side));
   CK(cudaEventRecord(x->hev[1], x->side));
   HostIO io{eta, u, v, false};
@@ -739,7 +741,10 @@ static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
     } else {
       for (int t = 0; t < n; t++) {
         StepHooks hk;
-        if (io && done + t == 0) hk.eta_in = x->hev[1];
+        if (io && done + t == 0) {
+          hk.v_in = x->hev[6];
+          hk.eta_in = x->hev[1];
+        }
         if (io && done + t == nsteps - 1) {
           hk.eta_out = x->hev[2];
           hk.u_out = x->hev[4];
@@ -1108,7 +1113,7 @@ void sw2g_destroy(sw2g_ctx* x) {
   x->run32.release();
   for (int e = 0; e < 2; e++)
     if (x->ev[e]) cudaEventDestroy(x->ev[e]);
-  for (int e = 0; e < 6; e++)
+  for (int e = 0; e < 7; e++)
     if (x->hev[e]) cudaEventDestroy(x->hev[e]);
   if (x->side) {
     cudaStreamSynchronize(x->side);

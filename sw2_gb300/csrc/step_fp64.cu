@@ -1506,6 +1506,29 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   auto F = [&]() { return F7{b.f[0], b.f[1], b.f[2], b.f[3], b.f[4], b.f[5], b.f[6]}; };
   const bool hyper = (s.nu2 != 0 || s.nu4 != 0 || s.nu6 != 0);
 
+  // The Laplacians of the mass equation's hyperviscosity (calc.c:325-335,
+  // laplacian.c:110-146). The reference zeroes Le, psi and xi before them
+  // (calc.c:325-327, laplacian.c:116-118). Here they are zeroed once at
+  // allocation: every level that runs rewrites all cells of its Le
+  // (interior, halo wrap, wall rows) and the interior of psi and xi, whose
+  // halos stay zero; levels that do not run leave their Le zero.
+  auto eta_laplacians = [&]() {
+    const double* src = s.lape_eta ? b.f[0] : b.f[1];  // the reference passes u, not eta (calc.c:332)
+    const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
+    for (int q = 0; q < nlap; q++) {
+      LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
+      // halo and wall rows of Le are written by the pass (a polar cap has no walls)
+      LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
+    }
+  };
+  // Reading u alone, and nothing that the kernels before their place in the
+  // reference's order write, they run first when a caller copies the fields
+  // in, which then overlaps the copies of v and eta with them (StepHooks);
+  // otherwise they keep their place after the mass body.
+  const bool laplacians_first = hyper && !s.lape_eta && hk.v_in;
+  if (laplacians_first) eta_laplacians();
+  if (hk.v_in) cudaStreamWaitEvent(st, hk.v_in, 0);
+
   // compute_Dt (core.c:155-159): maxima at the start of the step
   LAUNCH("cfl", k_cfl<<<s.ny, CFL_T, 0, st>>>(s, F(), chk.cfl + 2 * slot));
 
@@ -1527,18 +1550,7 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   if (hk.eta_in) cudaStreamWaitEvent(st, hk.eta_in, 0);
   LAUNCH("mass", body(0, sch, g, st, s, F(), b.deta[0]));
   if (hyper) {
-    // The reference zeroes Le, psi and xi before the Laplacians (calc.c:325-327,
-    // laplacian.c:116-118). Here they are zeroed once at allocation: every
-    // level that runs rewrites all cells of its Le (interior, halo wrap, wall
-    // rows) and the interior of psi and xi, whose halos stay zero; levels that
-    // do not run leave their Le zero.
-    const double* src = s.lape_eta ? b.f[0] : b.f[1];  // the reference passes u, not eta (calc.c:332)
-    const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
-    for (int q = 0; q < nlap; q++) {
-      LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
-      // halo and wall rows of Le are written by the pass (a polar cap has no walls)
-      LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
-    }
+    if (!laplacians_first) eta_laplacians();
     if (k < 2) LAUNCH("hyper_add", hyper_add(s, g, st, b.deta[0], b.Le[0], b.Le[1], b.Le[2]));
   }
   if (k >= 2) {

@@ -118,12 +118,14 @@ class Timers {
 // forcing goes between them.
 constexpr int STEP_HEAD = 1, STEP_TAIL = 2, STEP_FULL = 3;
 // Events within a step, for callers that overlap host copies with it: the
-// stream waits for eta_in before the first kernel that reads eta (the
-// advection of u and v, which do not read it, come first), records eta_out as
-// soon as eta holds the step's result, and u_out once the interior of u does
-// (its halo columns and wall rows are still rewritten at the end of the
-// step). Null events are skipped.
+// stream waits for v_in before the first kernel that reads v (the eta
+// Laplacians, which read only u, come first), for eta_in before the first
+// kernel that reads eta (the advection of u and v, which do not read it, come
+// first), records eta_out as soon as eta holds the step's result, and u_out
+// once the interior of u does (its halo columns and wall rows are still
+// rewritten at the end of the step). Null events are skipped.
 struct StepHooks {
+  cudaEvent_t v_in = nullptr;
   cudaEvent_t eta_in = nullptr;
   cudaEvent_t eta_out = nullptr;
   cudaEvent_t u_out = nullptr;

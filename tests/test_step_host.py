@@ -49,6 +49,28 @@ def test_gpu_step_host_matches_oracle_every_step(sch, tracer, winds):
     assert s.steps_done() == 13
 
 
+@pytest.mark.parametrize("lape_eta,hyper", [(True, True), (False, False)])
+def test_gpu_step_host_other_step_orders(lape_eta, hyper):
+    """The eta Laplacians run first only when they read u alone: with
+    SW2G_FLAG_LAPE_ETA they read eta and keep their place, and without
+    hyperviscosity there are none; both still match the oracle."""
+    case = cases.make_case(nx=48, ny=24, sch=2, seed=61, bumps=2, hyper=hyper)
+    if hyper:
+        nu4 = case.params.hypernu[1]
+        case.params.hypernu = (1e-3 * nu4 ** 0.5, nu4, 1e-4 * nu4 ** 1.5)
+    s = lib.Solver(case.params, flags=lib.FLAG_LAPE_ETA if lape_eta else 0)
+    s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    o = orc.Oracle(case.params, lape_eta=lape_eta)
+    o.load(case.fields())
+    d = s.download()
+    eta, u, v = (d[k].copy() for k in ("eta", "u", "v"))
+    for n in (1, 1, 2, 4):
+        assert s.step_host(eta, u, v, n) == lib.OK
+        assert o.step(n) == (0, -1)
+        for k, a in zip(("eta", "u", "v"), (eta, u, v)):
+            assert same(a, o.field(k)), k
+
+
 def test_gpu_step_host_equals_upload_step_download():
     case = cases.make_case(nx=128, ny=48, sch=2, seed=3, bumps=3)
     a = lib.Solver(case.params)
