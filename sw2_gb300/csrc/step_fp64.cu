@@ -1350,12 +1350,14 @@ __global__ void k_range(DevState s, RangeFields r, int* bad) {
 // 8, 12, 16 and 24 rows): 12 rows is the best or within 0.2 % of it on both,
 // 16 loses 10 % at 2048x1024, where its 1.4 rounds of strips leave most warps
 // idle in the second. The queue instead of the fixed turns: the same time at
-// 2048x1024, 1 % less at 4096x2048. A grid with fewer 12-row strips than
-// resident warps takes shorter strips, down to 4 rows, to use more warps.
+// 2048x1024, 1 % less at 4096x2048. With the queue, 8 rows beat 12 by 0.6 %
+// at 2048x1024 (1.9 rounds of 12-row strips, 2.8 of 8-row ones) and lose
+// 0.6 % at 4096x2048 (7.5 rounds of 12-row strips): the tallest strip that
+// gives every resident warp at least 2.5 strips, down to 4 rows.
 int choose_strip_rows(int nx, int ny, long long warps) {
   for (int fk : {12, 8, 6}) {
     const long long strips = (long long)((nx + FW - 1) / FW) * ((ny + fk - 1) / fk);
-    if (strips >= warps) return fk;
+    if (2 * strips >= 5 * warps) return fk;
   }
   return 4;
 }
