@@ -686,10 +686,9 @@ sw2g_status sw2g_step_host(sw2g_ctx* x, double* eta, double* u, double* v, int n
     return ss != SW2G_OK ? ss : st;
   }
   CK(cudaSetDevice(x->device));
-  if (!x->side) {
-    CK(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
-    for (int e = 0; e < 7; e++) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
-  }
+  for (int e = 0; e < 7; e++)  // made on first use (and again after a failed attempt)
+    if (!x->hev[e]) CK(cudaEventCreateWithFlags(&x->hev[e], cudaEventDisableTiming));
+  if (!x->side) CK(cudaStreamCreateWithFlags(&x->side, cudaStreamNonBlocking));
   // u first, then v and eta on the side stream: the step's first kernels
   // (the eta Laplacians) read only u, the next ones (the CFL maxima, the
   // advection of u and v) u and v, while eta is still on its way in.
