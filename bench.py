@@ -79,7 +79,7 @@ NCU_TRAFFIC = {("band2048", "mass"): 57.15e6, ("band2048", "adv_u"): 37.34e6, ("
 # of the same step (profiles/fp64_step_band2048_fp64_instruction_counts.md),
 # and GB300's FP64 peak per cycle over the whole GPU (ncu's peak for DFMA:
 # 304 = 2 lanes per SM x 152 SMs). The FP64 form is bound by this unit.
-NCU_FP64_PER_CELL = {("band2048", "mass"): 57.9, ("band2048", "adv_u"): 76.3, ("band2048", "adv_v"): 76.7}
+NCU_FP64_PER_CELL = {("band2048", "mass"): 59.0, ("band2048", "adv_u"): 77.4, ("band2048", "adv_v"): 77.8}
 FP64_LANES_PER_CYCLE = 304
 # The whole step: read eta u v, write eta u v, read two history levels of
 # three tendencies, write one (a per-cell count for the step's GB/s figure).
