@@ -62,3 +62,16 @@ def test_null_context_calls_are_rejected(L):
     assert L.sw2g_download(None, None, None, None, None) == lib.ERR_BAD_ARG
     assert L.sw2g_error_step(None) == -1
     L.sw2g_destroy(None)
+
+
+def test_host_array_step_and_add_selfcheck_reject_bad_arguments(L):
+    """Checked on the host before any CUDA call."""
+    buf = (ctypes.c_double * 16)()
+    p = ctypes.cast(buf, ctypes.POINTER(ctypes.c_double))
+    assert L.sw2g_step_host(None, p, p, p, 1) == lib.ERR_BAD_ARG
+    L.sw2g_selfcheck_add.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_longlong)]
+    out = ctypes.c_longlong(-7)
+    assert L.sw2g_selfcheck_add(0, 1, 0, ctypes.byref(out)) == lib.ERR_BAD_ARG
+    assert L.sw2g_selfcheck_add(10, 1, 0, None) == lib.ERR_BAD_ARG
+    assert out.value == -7
