@@ -1,0 +1,111 @@
+"""The FP64 step's integer-pipe additions (sadd, ssub in step_fp64.cu), on the
+CPU: their source text is taken from the CUDA file as it stands, compiled for
+the host with the bit helpers it uses mapped to host equivalents, and
+compared bit for bit with the host's IEEE double addition (round to nearest
+even; NaNs compared as NaNs) on random and edge-case operand pairs. The GPU
+self-check (tests/test_division.py) runs the same comparison on the device."""
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "sw2_gb300", "csrc", "step_fp64.cu")
+
+
+def function_text(src, signature):
+    start = src.index(signature)
+    depth, i = 0, src.index("{", start)
+    while True:
+        if src[i] == "{":
+            depth += 1
+        elif src[i] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[start:i + 1]
+        i += 1
+
+
+HARNESS = r"""
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+static inline long long dbits(double x) { long long r; std::memcpy(&r, &x, 8); return r; }
+static inline double __longlong_as_double(long long b) { double r; std::memcpy(&r, &b, 8); return r; }
+static inline int __clzll(long long x) { return __builtin_clzll((unsigned long long)x); }
+static double add_fp64(double a, double b) { return a + b; }
+%s
+%s
+static uint64_t st = 0x9E3779B97F4A7C15ULL;
+static uint64_t next() {  // SplitMix64
+  uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+static double mk(uint64_t r, int e, bool neg) {
+  return __longlong_as_double((long long)(((uint64_t)e << 52) | (r & 0xFFFFFFFFFFFFFULL) | (neg ? 1ULL << 63 : 0)));
+}
+static bool isnan_bits(double x) { return (dbits(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+static bool same(double want, double got) {
+  if (isnan_bits(want)) return isnan_bits(got);
+  return dbits(want) == dbits(got);
+}
+int main(int argc, char** argv) {
+  long long n = atoll(argv[1]), bad = 0;
+  for (long long t = 0; t < n; t++) {
+    const uint64_t r1 = next(), r2 = next(), r3 = next();
+    double a, b;
+    switch (r3 %% 8) {
+      case 0: a = mk(r1, 1 + (r3 >> 8) %% 2046, r2 & 1); b = mk(r2, 1 + (r3 >> 20) %% 2046, r2 & 2); break;
+      case 1: case 2: {  // exponents within 64: alignment, carries, cancellation
+        const int e = 70 + (r3 >> 8) %% 1900;
+        a = mk(r1, e, r2 & 1); b = mk(r2, e - (int)((r3 >> 20) %% 64), r2 & 2); break;
+      }
+      case 3:  // b = -a give or take a few ulps
+        a = mk(r1, 3 + (r3 >> 8) %% 2040, r2 & 1);
+        b = __longlong_as_double((dbits(a) ^ (long long)0x8000000000000000ULL) + (long long)((r2 >> 8) %% 9) - 4);
+        break;
+      case 4: {  // ties: an odd multiple of half an ulp of a, or next to one
+        const int e = 60 + (r3 >> 8) %% 1900;
+        a = mk(r1, e, r2 & 1);
+        b = (double)(2 * ((r2 >> 8) %% 16) + 1) * mk(0, e - 53, false);
+        if (r2 & 4) b = __longlong_as_double(dbits(b) + (long long)((r2 >> 20) %% 3) - 1);
+        if (r2 & 2) b = -b;
+        break;
+      }
+      case 5: a = mk(r1, 2046 - (r3 >> 8) %% 3, r2 & 1); b = mk(r2, 2046 - (r3 >> 20) %% 60, r2 & 2); break;
+      case 6: a = mk(r1, (r3 >> 8) %% 4, r2 & 1); b = mk(r2, (r3 >> 20) %% 60, r2 & 2); break;
+      default: {  // zeros, inf, NaN, against anything
+        const double sp[6] = {0.0, -0.0, __longlong_as_double(0x7ff0000000000000LL),
+                              __longlong_as_double((long long)0xfff0000000000000ULL),
+                              __longlong_as_double(0x7ff8000000000000LL), 1.0};
+        a = sp[(r3 >> 8) %% 6];
+        b = (r2 & 1) ? sp[(r3 >> 20) %% 6] : mk(r2, 1 + (r3 >> 24) %% 2046, r2 & 2);
+        if (r2 & 4) { const double t2 = a; a = b; b = t2; }
+      }
+    }
+    if (!same(a + b, sadd(a, b))) bad++;
+    if (!same(a - b, ssub(a, b))) bad++;
+  }
+  printf("%%lld\n", bad);
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_integer_pipe_addition_source_matches_ieee_on_the_host(tmp_path):
+    src = open(SRC).read()
+    sadd = function_text(src, "__device__ __forceinline__ double sadd(double a, double b) {")
+    ssub = function_text(src, "__device__ __forceinline__ double ssub(double a, double b) {")
+    sadd, ssub = (re.sub(r"__device__ __forceinline__", "static inline", f) for f in (sadd, ssub))
+    c = tmp_path / "soft_add.cpp"
+    c.write_text(HARNESS % (sadd, ssub))
+    exe = tmp_path / "soft_add"
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-o", str(exe), str(c)], check=True)
+    out = subprocess.run([str(exe), str(40_000_000)], check=True, capture_output=True, text=True).stdout
+    assert int(out.strip()) == 0
