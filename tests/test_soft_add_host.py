@@ -1,9 +1,12 @@
-"""The FP64 step's integer-pipe additions (sadd, ssub in step_fp64.cu), on the
-CPU: their source text is taken from the CUDA file as it stands, compiled for
-the host with the bit helpers it uses mapped to host equivalents, and
-compared bit for bit with the host's IEEE double addition (round to nearest
-even; NaNs compared as NaNs) on random and edge-case operand pairs. The GPU
-self-check (tests/test_division.py) runs the same comparison on the device."""
+"""The FP64 step's exact arithmetic helpers in step_fp64.cu, on the CPU: the
+integer-pipe additions (sadd, ssub), the division by a row metric with its
+correctly rounded reciprocal (div_rcp) and the power-of-two scalings
+(mul_pow2). Their source text is taken from the CUDA file as it stands,
+compiled for the host with the intrinsics it uses mapped to host
+equivalents (the host's fma is correctly rounded, as the GPU's is), and
+compared bit for bit with the host's IEEE operations (NaNs compared as NaNs)
+on random and edge-case operands. The GPU self-checks (tests/test_division.py)
+run the first two comparisons on the device."""
 import os
 import re
 import shutil
@@ -109,3 +112,79 @@ def test_integer_pipe_addition_source_matches_ieee_on_the_host(tmp_path):
     subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-o", str(exe), str(c)], check=True)
     out = subprocess.run([str(exe), str(40_000_000)], check=True, capture_output=True, text=True).stdout
     assert int(out.strip()) == 0
+
+
+DIV_HARNESS = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+static inline long long dbits(double x) { long long r; std::memcpy(&r, &x, 8); return r; }
+static inline double __longlong_as_double(long long b) { double r; std::memcpy(&r, &b, 8); return r; }
+static inline int dexp(double x) { return (int)(((unsigned long long)dbits(x) >> 52) & 0x7ffULL); }
+static inline double __dmul_rn(double a, double b) { return a * b; }
+static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
+static double mul_pow2_fp64(double x, double p) { return x * p; }
+%s
+%s
+static uint64_t st = 0x243F6A8885A308D3ULL;
+static uint64_t next() {
+  uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+static double mk(uint64_t r, int e, bool neg) {
+  return __longlong_as_double((long long)(((uint64_t)e << 52) | (r & 0xFFFFFFFFFFFFFULL) | (neg ? 1ULL << 63 : 0)));
+}
+static bool same(double want, double got) {
+  const bool n1 = (dbits(want) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+  const bool n2 = (dbits(got) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+  return n1 ? n2 : dbits(want) == dbits(got);
+}
+int main(int argc, char** argv) {
+  long long n = atoll(argv[1]), bad_div = 0, bad_pow = 0;
+  for (long long t = 0; t < n; t++) {
+    const uint64_t r1 = next(), r2 = next(), r3 = next();
+    // divisors: positive normal numbers over the range of metric factors and
+    // beyond, including all-ones significands and powers of two
+    double b = mk(r2, 1023 - 40 + (int)((r3 >> 40) %% 90), false);
+    if ((r3 & 15) == 0) b = mk(~0ULL, 1023 - 40 + (int)((r3 >> 40) %% 90), false);
+    if ((r3 & 15) == 1) b = mk(0, 1023 - 40 + (int)((r3 >> 40) %% 90), false);
+    const double y = 1.0 / b;
+    double a;
+    if (r3 & 16) {  // random numerators, every exponent, both signs, zeros
+      a = mk(r1, (int)((r3 >> 8) %% 2047), r3 & 32);
+    } else {  // a = b * (q + half an ulp of q, give or take a little): quotient near a midpoint
+      const int e = 523 + (int)((r3 >> 8) %% 500);
+      const double q = mk(r1, e, false);
+      const double h = mk(0, e - 53, false) * (double)(((r3 >> 20) & 7) + 1) * 0.5;
+      a = b * (q + h);
+      if (r3 & 64) a = __longlong_as_double(dbits(a) + (long long)((r3 >> 24) %% 5) - 2);
+    }
+    if (!same(a / b, div_rcp(a, b, y))) bad_div++;
+    // power-of-two scalings of anything, the exponent field's edges included
+    const double x = mk(r1, (r3 & 128) ? (int)((r3 >> 8) %% 2048) : ((r3 & 256) ? (int)((r3 >> 8) %% 4) : 2043 + (int)((r3 >> 8) %% 5)), r3 & 512);
+    if (!same(x * 0.5, mul_pow2(x, -1, 0.5))) bad_pow++;
+    if (!same(x * 0.25, mul_pow2(x, -2, 0.25))) bad_pow++;
+    if (!same(x * 2.0, mul_pow2(x, 1, 2.0))) bad_pow++;
+  }
+  printf("%%lld %%lld\n", bad_div, bad_pow);
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_metric_division_and_power_of_two_scaling_sources_match_ieee_on_the_host(tmp_path):
+    src = open(SRC).read()
+    div = function_text(src, "__device__ __forceinline__ double div_rcp(double a, double b, double y) {")
+    pw = function_text(src, "__device__ __forceinline__ double mul_pow2(double x, int k, double p) {")
+    div, pw = (re.sub(r"__device__ __forceinline__", "static inline", f) for f in (div, pw))
+    c = tmp_path / "div.cpp"
+    c.write_text(DIV_HARNESS % (pw, div))
+    exe = tmp_path / "div"
+    subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-o", str(exe), str(c)], check=True)
+    out = subprocess.run([str(exe), str(4_000_000)], check=True, capture_output=True, text=True).stdout
+    assert out.split() == ["0", "0"]
