@@ -1,7 +1,9 @@
-"""The FP64 step's exact arithmetic helpers in step_fp64.cu, on the CPU: the
+"""The FP64 step's exact helpers in step_fp64.cu, on the CPU: the
 integer-pipe additions (sadd, ssub), the division by a row metric with its
 correctly rounded reciprocal (div_rcp) and the power-of-two scalings
-(mul_pow2). Their source text is taken from the CUDA file as it stands,
+(mul_pow2), the limiters on integer images (limiter_fast) and the range
+test behind the checks (range_bad). Their source text is taken from the CUDA
+file as it stands,
 compiled for the host with the intrinsics it uses mapped to host
 equivalents (the host's fma is correctly rounded, as the GPU's is), and
 compared bit for bit with the host's IEEE operations (NaNs compared as NaNs)
@@ -188,3 +190,137 @@ def test_metric_division_and_power_of_two_scaling_sources_match_ieee_on_the_host
     subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-o", str(exe), str(c)], check=True)
     out = subprocess.run([str(exe), str(4_000_000)], check=True, capture_output=True, text=True).stdout
     assert out.split() == ["0", "0"]
+
+
+LIMITER_HARNESS = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+constexpr int kVanLeerSafe = 10;
+static inline long long dbits(double x) { long long r; std::memcpy(&r, &x, 8); return r; }
+static inline double __longlong_as_double(long long b) { double r; std::memcpy(&r, &b, 8); return r; }
+static double mul_pow2_fp64(double x, double p) { return x * p; }
+%s
+#define HALF(x) mul_pow2((x), -1, 0.5)
+#define QUARTER(x) mul_pow2((x), -2, 0.25)
+#define TWICE(x) mul_pow2((x), 1, 2.0)
+%s
+%s
+%s
+%s
+%s
+static bool ok(double want, double got) {  // equal, or both zeros
+  if (dbits(want) == dbits(got)) return true;
+  return want == 0.0 && got == 0.0;
+}
+static uint64_t st = 0x13198A2E03707344ULL;
+static uint64_t next() {
+  uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+template <int SCH> long long check(long long n) {
+  long long bad = 0;
+  const double fixed[] = {0.0, -0.0, 1.0, -1.0, 0.5, 2.0, 1.0 / 3.0, 3.0, 0.25, 0.75, 4.0, 1e-300, -1e-300,
+                          1e300, -1e300, 0x1p498, -0x1p498, 0x1p-1022, -0x1p-1022, 5e-324};
+  for (double r : fixed) {
+    if (!ok(limiter<SCH>(r), limiter_fast<SCH>(r))) bad++;
+    for (int k = -3; k <= 3; k++) {
+      const double s = __longlong_as_double(dbits(r) + k);
+      if (std::isfinite(s) && !ok(limiter<SCH>(s), limiter_fast<SCH>(s))) bad++;
+    }
+  }
+  for (long long t = 0; t < n; t++) {
+    const uint64_t a = next(), b = next();
+    // ratios of limiter interest (|r| around 1) most of the time, any finite value otherwise
+    const int e = (b & 3) ? 1023 - 8 + (int)((b >> 8) %% 16) : (int)((b >> 8) %% 2047);
+    const double r = __longlong_as_double((long long)(((uint64_t)e << 52) | (a & 0xFFFFFFFFFFFFFULL) | ((b >> 40) & 1 ? 1ULL << 63 : 0)));
+    if (!ok(limiter<SCH>(r), limiter_fast<SCH>(r))) bad++;
+  }
+  return bad;
+}
+int main(int argc, char** argv) {
+  const long long n = atoll(argv[1]);
+  printf("%%lld %%lld %%lld %%lld %%lld %%lld\n", check<0>(n), check<1>(n), check<2>(n), check<4>(n), check<7>(n),
+         check<kVanLeerSafe>(n));
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_fast_limiters_source_matches_the_literal_limiters_on_the_host(tmp_path):
+    """limiter_fast (integer-image comparisons, exponent-field scalings) gives
+    the literal limiter's value for every finite ratio, up to the sign of a
+    zero (the fast bodies recompute cells whose sum is zero literally)."""
+    src = open(SRC).read()
+    pw = function_text(src, "__device__ __forceinline__ double mul_pow2(double x, int k, double p) {")
+    key = function_text(src, "__device__ __forceinline__ long long key(double x) {")
+    one_liners = [ln for ln in src.splitlines()
+                  if ln.startswith("__device__ __forceinline__ double mn(") or
+                  ln.startswith("__device__ __forceinline__ double mx(")]
+    assert len(one_liners) == 2
+    lim = "template <int SCH>\n" + function_text(src, "__device__ __forceinline__ double limiter(double r) {")
+    fast = "template <int SCH>\n" + function_text(src, "__device__ __forceinline__ double limiter_fast(double r) {")
+    parts = [pw, key, "\n".join(one_liners), lim, fast]
+    parts = [re.sub(r"__device__ __forceinline__", "static inline", f) for f in parts]
+    c = tmp_path / "lim.cpp"
+    c.write_text(LIMITER_HARNESS % (parts[0], parts[1], parts[2], parts[3], parts[4], ""))
+    exe = tmp_path / "lim"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-o", str(exe), str(c)],
+                   check=True)
+    out = subprocess.run([str(exe), str(2_000_000)], check=True, capture_output=True, text=True).stdout
+    assert out.split() == ["0"] * 6
+
+
+RANGE_HARNESS = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+static inline long long dbits(double x) { long long r; std::memcpy(&r, &x, 8); return r; }
+static inline double from(uint64_t b) { double r; std::memcpy(&r, &b, 8); return r; }
+%s
+int main() {
+  long long bad = 0, n = 0;
+  const double lim = 1e10;
+  const double edge[] = {lim, std::nextafter(lim, 0.0), std::nextafter(lim, 1e300), -lim, 0.0, -0.0, 1.0,
+                         INFINITY, -INFINITY, NAN, -NAN, 1e300, 5e-324};
+  auto test = [&](double x) {
+    for (int first = 0; first < 2; first++) {
+      // the reference: the first value seeds min and max (a non-finite one fails the check);
+      // later NaNs never win a comparison; the step aborts on min < -1e10 or max > 1e10
+      const bool want = first ? (!std::isfinite(x) || std::fabs(x) > lim) : (std::fabs(x) > lim);
+      if (range_bad(x, first) != want) bad++;
+      n++;
+    }
+  };
+  for (double x : edge) test(x);
+  uint64_t s = 0x452821E638D01377ULL;
+  for (long long t = 0; t < 20000000; t++) {
+    s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+    const uint64_t b = s ^ (s >> 29);
+    test(from((b & 1) ? b : ((b & 0x800FFFFFFFFFFFFFULL) | ((uint64_t)(1023 + 30 + (int)((b >> 52) %% 8)) << 52))));
+  }
+  printf("%%lld %%lld\n", bad, n);
+  return 0;
+}
+"""
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_range_check_source_matches_the_reference_predicate_on_the_host(tmp_path):
+    """range_bad, the bit test behind the range checks, against the
+    reference's check_stats_scaf outcome for one value (first or not)."""
+    src = open(SRC).read()
+    rb = function_text(src, "__device__ __forceinline__ bool range_bad(double x, bool first) {")
+    rb = re.sub(r"__device__ __forceinline__", "static inline", rb)
+    c = tmp_path / "range.cpp"
+    c.write_text(RANGE_HARNESS % rb)
+    exe = tmp_path / "range"
+    subprocess.run(["g++", "-O2", "-fno-fast-math", "-o", str(exe), str(c)], check=True)
+    bad, n = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert int(bad) == 0 and int(n) > 0
