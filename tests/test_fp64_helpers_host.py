@@ -1,14 +1,17 @@
-"""The FP64 step's exact helpers in step_fp64.cu, on the CPU: the
-integer-pipe additions (sadd, ssub), the division by a row metric with its
-correctly rounded reciprocal (div_rcp) and the power-of-two scalings
-(mul_pow2), the limiters on integer images (limiter_fast) and the range
-test behind the checks (range_bad). Their source text is taken from the CUDA
-file as it stands,
-compiled for the host with the intrinsics it uses mapped to host
-equivalents (the host's fma is correctly rounded, as the GPU's is), and
-compared bit for bit with the host's IEEE operations (NaNs compared as NaNs)
-on random and edge-case operands. The GPU self-checks (tests/test_division.py)
-run the first two comparisons on the device."""
+"""The FP64 step's exact helpers in step_fp64.cu, on the CPU. Their source
+text is taken from the CUDA file as it stands and compiled for the host,
+the intrinsics it uses mapped to host equivalents (the host's fma is
+correctly rounded, as the GPU's is), then compared bit for bit (NaNs as
+NaNs) on random and edge-case operands:
+- the integer-pipe additions (sadd, ssub) with IEEE addition;
+- the division by a row metric with its correctly rounded reciprocal
+  (div_rcp) with IEEE division, and the power-of-two scalings (mul_pow2)
+  with IEEE multiplication;
+- the limiters on integer images (limiter_fast) with the literal limiters,
+  up to the sign of a zero;
+- the range test behind the checks (range_bad) with the reference's check
+  outcome for one value.
+The GPU self-checks (tests/test_division.py) run the first two on the device."""
 import os
 import re
 import shutil
