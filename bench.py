@@ -76,8 +76,7 @@ KERNEL_BYTES = {
 NCU_TRAFFIC = {("band2048", "mass"): 57.15e6, ("band2048", "adv_u"): 37.34e6, ("band2048", "adv_v"): 36.00e6}
 # FP64 thread instructions (DADD + DMUL + DFMA) per interior cell of the
 # dominant kernels on the 2048x1024 workload, from ncu's instruction counters
-# of the same step (profiles/fp64_step_band2048_fp64_instruction_counts.md),
-# and GB300's FP64 peak per cycle over the whole GPU (ncu's peak for DFMA:
+# of the same step, and GB300's FP64 peak per cycle over the whole GPU (ncu's peak for DFMA:
 # 304 = 2 lanes per SM x 152 SMs). The FP64 form is bound by this unit.
 NCU_FP64_PER_CELL = {("band2048", "mass"): 59.0, ("band2048", "adv_u"): 77.4, ("band2048", "adv_v"): 77.8}
 FP64_LANES_PER_CYCLE = 304

@@ -203,16 +203,11 @@ sw2g_status cuda_fail(cudaError_t e, const char* what) {
   } while (0)
 
 bool case_ok(const sw2g_case* c) {
-  if (!c) return false;
-  if (c->nx < 3 || c->ny < 3 || c->sch < 0 || c->sch > 9) return false;
-  if ((long long)(c->nx + 4) * (c->ny + 4) > (1LL << 31) - 1) return false;
-  if (!(c->rE > 0) || !(c->rP > 0) || !(c->Dt > 0) || !(c->courant > 0)) return false;
-  if (!(c->lon1 > c->lon0) || !(c->lat1 > c->lat0)) return false;
-  const double pole = (c->flags & SW2G_FLAG_RADIANS) ? 2.0 * std::atan(1.0) : 90.0;
-  if (!(c->lat0 > -pole) || !(c->lat1 < pole)) return false;
+  if (!grid_ok(c)) return false;
+  if (c->sch < 0 || c->sch > 9) return false;
+  if (!(c->Dt > 0) || !(c->courant > 0)) return false;
   // init.c:122: hyperviscosity coefficients are entered as non-negative
   if (c->hypernu[0] < 0 || c->hypernu[1] < 0 || c->hypernu[2] < 0) return false;
-  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | SW2G_FLAG_LAPE_ETA)) return false;
   if (c->polar != 0) {  // the square around the pole (init.c:66-79)
     if ((c->polar != 1 && c->polar != -1) || c->nx != c->ny) return false;
     if (!(c->lon1 > 0) || c->lon0 != -c->lon1 || c->lat0 != c->lon0 || c->lat1 != c->lon1) return false;
@@ -398,6 +393,19 @@ sw2g_status upload_fp32(sw2g_ctx* x, const double* eta, const double* u, const d
 }  // namespace
 
 namespace sw2g {
+
+bool grid_ok(const sw2g_case* c) {
+  if (!c) return false;
+  if (c->nx < 3 || c->ny < 3) return false;
+  // cell indices are 32-bit: (i+1) + (j+1)*(nx+4) over the padded field
+  if ((long long)(c->nx + 4) * (c->ny + 4) > (1LL << 31) - 1) return false;
+  if (!(c->rE > 0) || !(c->rP > 0)) return false;
+  if (!(c->lon1 > c->lon0) || !(c->lat1 > c->lat0)) return false;
+  const double pole = (c->flags & SW2G_FLAG_RADIANS) ? 2.0 * std::atan(1.0) : 90.0;
+  if (!(c->lat0 > -pole) || !(c->lat1 < pole)) return false;
+  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | SW2G_FLAG_LAPE_ETA)) return false;
+  return true;
+}
 
 cudaEvent_t Timers::take() {
   if (!free_.empty()) {
@@ -703,6 +711,10 @@ sw2g_status sw2g_step_host(sw2g_ctx* x, double* eta, double* u, double* v, int n
   HostIO io{eta, u, v, false};
   const sw2g_status st = run_steps(x, nsteps, &io);
   if (!io.copied) {  // a failure before the last chunk of steps was queued
+    // the side stream's uploads of v and eta must have landed before the
+    // read-back on the main stream reads those fields
+    const sw2g_status sw = cuda_fail(cudaStreamSynchronize(x->side), "cudaStreamSynchronize");
+    if (sw != SW2G_OK) return st != SW2G_OK ? st : sw;
     const sw2g_status sd = sw2g_download(x, eta, u, v, nullptr);
     return st != SW2G_OK ? st : sd;
   }

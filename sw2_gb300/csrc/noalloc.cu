@@ -6,13 +6,17 @@
 // own pool allocator, a step loop where cudaMalloc/cudaFree would synchronise
 // the device in the middle of a time step, or a post-processing tool that owns
 // its field buffers and never creates a sw2g context. For them this variant
-// keeps its scratch (per-row geometry and row partials) in one file-scope
-// __device__ array of fixed size, so the call needs no cudaMalloc, cudaFree or
-// any other allocating routine.
+// keeps its scratch (the row partials) in one file-scope __device__ array of
+// fixed size, so the call needs no cudaMalloc, cudaFree or any other
+// allocating routine.
+//
+// The per-row geometry (area element and gravity) is computed on the host with
+// the same expressions as the context's tables and travels to the GPU inside
+// the kernel parameters, in chunks of kRowsPerLaunch rows: no host buffer is
+// copied and nothing waits for the stream, so a call only queues work.
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 #include "sw2g_internal.h"
 
@@ -22,50 +26,44 @@ void energy_row_geometry(const sw2g_case& c, int j0, int n, double* surf, double
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-constexpr int kStage = 256;  // rows of geometry staged on the host stack per copy
+// Rows whose geometry one launch carries in its parameters (16 KiB).
+constexpr int kRowsPerLaunch = 1024;
 
-// Scratch for the no-allocation energy sum: per interior row, the area element
-// and gravity (2 * SW2G_NOALLOC_MAX_ROWS doubles), then three row partials
-// (3 * SW2G_NOALLOC_MAX_ROWS doubles): 320 KiB in all. Every GPU on which the
-// library's module is loaded holds this array until the process exits.
-__device__ __align__(256) double g_energy_scratch[5 * SW2G_NOALLOC_MAX_ROWS];
+struct RowGeometry {
+  double surf[kRowsPerLaunch];  // DXC*DYC (energy.c:40)
+  double gc[kRowsPerLaunch];    // GC, gravity at the cell centre (init.c:289)
+};
+static_assert(sizeof(RowGeometry) + 128 <= 32760, "kernel parameters are limited to 32 KB");
 
-// Device address of g_energy_scratch per device, looked up once per device.
-// In host code the symbol itself is only a host-side stand-in, never a device
-// address, so kernels are always given this looked-up pointer.
-double* g_scratch_addr[kMaxDevices];
-std::mutex g_setup;
+// Scratch of the no-allocation energy sum: three compensated partials per
+// interior row (3 * SW2G_NOALLOC_MAX_ROWS doubles, 192 KiB). Every GPU on
+// which the library's module is loaded holds this array until the process
+// exits.
+__device__ __align__(256) double g_energy_scratch[3 * SW2G_NOALLOC_MAX_ROWS];
 
+// Device address of g_energy_scratch on the current device. In host code the
+// symbol itself is only a host-side stand-in, never a device address, so the
+// kernels are given the address looked up here. The lookup is repeated on
+// every call (it allocates nothing and costs a table lookup once the module is
+// loaded), so a device reset or a reloaded module never leaves a stale pointer.
 cudaError_t scratch_on_current_device(double** out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_energy_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_setup);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_energy_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_addr[dev] = static_cast<double*>(p);
-  }
-  *out = g_scratch_addr[dev];
+  *out = static_cast<double*>(p);
   return cudaSuccess;
 }
 
 __device__ __forceinline__ int IXn(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
 
-// One block per interior row; the same per-cell terms (energy.c:36-41) and the
-// same compensated summation order as sw2g_diag.
-__global__ void k_energy_rows_noalloc(int nx, int ny, double depth, const double* eta, const double* u,
+// One block per interior row j = j0 + blockIdx.x; the same per-cell terms
+// (energy.c:36-41) and the same compensated summation order as sw2g_diag.
+__global__ void k_energy_rows_noalloc(int nx, int j0, double depth, const double* eta, const double* u,
                                       const double* v, const double* wx, const double* wy, const double* hb,
-                                      const double* scratch) {
+                                      const __grid_constant__ RowGeometry geo, double* part) {
   const int W = nx + 4;
-  const int j = blockIdx.x + 1;
-  const double* surf_rows = scratch;
-  const double* gc_rows = scratch + SW2G_NOALLOC_MAX_ROWS;
-  double* part = const_cast<double*>(scratch) + 2 * SW2G_NOALLOC_MAX_ROWS;
-  const double surf = surf_rows[j - 1], gc = gc_rows[j - 1];
+  const int j = j0 + blockIdx.x;
+  const double surf = geo.surf[blockIdx.x], gc = geo.gc[blockIdx.x];
   double acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
   for (int i = threadIdx.x + 1; i <= nx; i += blockDim.x) {
     const int q = IXn(W, i, j), qw = IXn(W, i - 1, j), qs = IXn(W, i, j - 1);
@@ -103,8 +101,7 @@ __global__ void k_energy_rows_noalloc(int nx, int ny, double depth, const double
   }
 }
 
-__global__ void k_energy_sum_noalloc(int ny, const double* scratch, double* out3) {
-  const double* part = scratch + 2 * SW2G_NOALLOC_MAX_ROWS;
+__global__ void k_energy_sum_noalloc(int ny, const double* part, double* out3) {
   const int c = threadIdx.x;
   if (c >= 3) return;
   double a = 0, e = 0;
@@ -123,10 +120,8 @@ extern "C" sw2g_status sw2g_energy_noalloc(const sw2g_case* c, const double* eta
                                            const double* v, const double* windx, const double* windy,
                                            const double* hB, double* out3, void* stream) {
   if (!c || !eta || !u || !v || !out3) return SW2G_ERR_BAD_ARG;
-  if (c->nx < 3 || c->ny < 3 || !(c->rE > 0) || !(c->rP > 0) || !(c->lon1 > c->lon0) || !(c->lat1 > c->lat0))
-    return SW2G_ERR_BAD_ARG;
-  if (c->flags & ~(SW2G_FLAG_VANLEER_SAFE | SW2G_FLAG_RADIANS | SW2G_FLAG_SIGMA | SW2G_FLAG_LAPE_ETA))
-    return SW2G_ERR_BAD_ARG;
+  // the grid checks of sw2g_create: sizes, 32-bit cell indices, the poles
+  if (!sw2g::grid_ok(c)) return SW2G_ERR_BAD_ARG;
   if (c->polar != 0) return SW2G_ERR_BAD_ARG;  // its gravity is two-dimensional: sw2g_diag covers caps
   if (c->ny > SW2G_NOALLOC_MAX_ROWS) {
     fprintf(stderr,
@@ -135,33 +130,28 @@ extern "C" sw2g_status sw2g_energy_noalloc(const sw2g_case* c, const double* eta
             c->ny, SW2G_NOALLOC_MAX_ROWS);
     return SW2G_ERR_BAD_ARG;
   }
-  double* scratch = nullptr;
-  cudaError_t e = scratch_on_current_device(&scratch);
+  double* part = nullptr;
+  cudaError_t e = scratch_on_current_device(&part);
   if (e != cudaSuccess) {
     fprintf(stderr, "sw2g_energy_noalloc: cudaGetSymbolAddress: %s\n", cudaGetErrorString(e));
     return SW2G_ERR_CUDA;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // Per-row geometry, staged through a small buffer on the host stack. Each
-  // call rewrites rows 0..ny-1 of the geometry and of the partials before
-  // reading them, so nothing in the scratch needs clearing first.
-  double stage[2][kStage];
-  for (int j0 = 1; j0 <= c->ny; j0 += kStage) {
-    const int n = (c->ny - j0 + 1) < kStage ? (c->ny - j0 + 1) : kStage;
-    sw2g::energy_row_geometry(*c, j0, n, stage[0], stage[1]);
-    e = cudaMemcpyAsync(scratch + (j0 - 1), stage[0], sizeof(double) * n, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(scratch + SW2G_NOALLOC_MAX_ROWS + (j0 - 1), stage[1], sizeof(double) * n,
-                          cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the stage buffer is reused next round
-    if (e != cudaSuccess) {
-      fprintf(stderr, "sw2g_energy_noalloc: geometry copy: %s\n", cudaGetErrorString(e));
-      return SW2G_ERR_CUDA;
-    }
+  // Each call rewrites the partials of rows 1..ny before the sum reads them,
+  // so nothing in the scratch needs clearing first. The geometry is part of
+  // each launch's parameters, copied when the launch is queued.
+  RowGeometry geo;
+  for (int j0 = 1; j0 <= c->ny; j0 += kRowsPerLaunch) {
+    const int n = (c->ny - j0 + 1) < kRowsPerLaunch ? (c->ny - j0 + 1) : kRowsPerLaunch;
+    sw2g::energy_row_geometry(*c, j0, n, geo.surf, geo.gc);
+    k_energy_rows_noalloc<<<n, 256, 0, st>>>(c->nx, j0, c->depth, eta, u, v, windx, windy, hB, geo, part);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) break;
   }
-  k_energy_rows_noalloc<<<c->ny, 256, 0, st>>>(c->nx, c->ny, c->depth, eta, u, v, windx, windy, hB, scratch);
-  k_energy_sum_noalloc<<<1, 32, 0, st>>>(c->ny, scratch, out3);
-  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_energy_sum_noalloc<<<1, 32, 0, st>>>(c->ny, part, out3);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) {
     fprintf(stderr, "sw2g_energy_noalloc: launch: %s\n", cudaGetErrorString(e));
     return SW2G_ERR_CUDA;

@@ -59,6 +59,11 @@ struct DevState {
 
 struct Ctx;
 
+// Checks of a case's grid shared by every entry point that takes one: at least
+// 3x3 cells, padded cell indices within 32 bits, positive radii, increasing
+// bounds, latitudes strictly between the poles, known flags.
+bool grid_ok(const sw2g_case* c);
+
 // Host geometry (geometry.cpp): fills rows[R_NUM*H]; returns the at-rest CFL
 // maxima used by compute_Dt when the flow is at rest (calc.c:715-725).
 void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, double* rest_my);

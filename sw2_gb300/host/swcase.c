@@ -274,26 +274,38 @@ static void ex_skip(ex *e) {
 static double ex_list(ex *e);
 static double ex_power(ex *e);
 
+/* Integer part of a non-negative double not above 2^32-1, as a C cast to
+ * unsigned int gives it; NaN gives 0 (what that cast yields on x86-64 and
+ * aarch64 alike). */
+static unsigned long long to_u32(double a) { return (a == a) ? (unsigned long long)(unsigned)a : 0ULL; }
+
+/* fac and ncr give the values of the reference's expression library
+ * (sppde/sppde_tinyexpr.c:122-149): exact products in 64-bit unsigned
+ * integers, rounded to double once, and infinite as soon as a product leaves
+ * 64 bits (fac(21) already does), not when a double would overflow. */
 static double fac(double a) {
   if (a < 0.0) return NAN;
-  if (a > 170.0) return INFINITY;
-  const unsigned ua = (unsigned)a;
-  double r = 1.0;
-  for (unsigned k = 2; k <= ua; k++) r *= (double)k;
-  return r;
+  if (a > 4294967295.0) return INFINITY;
+  const unsigned long long n = to_u32(a);
+  unsigned long long p = 1;
+  for (unsigned long long k = 2; k <= n; k++)
+    if (__builtin_mul_overflow(p, k, &p)) return INFINITY;
+  return (double)p;
 }
+/* C(n, k) by the multiplicative formula over the shorter of k and n-k; after
+ * step m the running value is C(n-k+m, m), an integer, so the division is exact. */
 static double ncr(double n, double r) {
   if (n < 0.0 || r < 0.0 || n < r) return NAN;
   if (n > 4294967295.0 || r > 4294967295.0) return INFINITY;
-  unsigned long un = (unsigned)n, ur = (unsigned)r, i;
-  unsigned long result = 1;
-  if (ur > un / 2) ur = un - ur;
-  for (i = 1; i <= ur; i++) {
-    if (result > 18446744073709551615UL / (un - ur + i)) return INFINITY;
-    result *= un - ur + i;
-    result /= i;
+  const unsigned long long top = to_u32(n);
+  unsigned long long k = to_u32(r);
+  if (k > top / 2) k = top - k;
+  unsigned long long c = 1;
+  for (unsigned long long m = 1; m <= k; m++) {
+    if (__builtin_mul_overflow(c, top - k + m, &c)) return INFINITY;
+    c /= m;
   }
-  return (double)result;
+  return (double)c;
 }
 static double npr(double n, double r) { return ncr(n, r) * fac(r); }
 
