@@ -234,11 +234,13 @@ def measure(lib, case, precision, steps, warmup, local, barrier, flags=0):
     per_launch = kms / nl
     kb = KERNEL_BYTES.get(name)
     total_k = sum(v[1] for v in table.values())
+    gbs = {k: KERNEL_BYTES[k] * cells / (v[1] / v[0] * 1e-3) / 1e9 for k, v in table.items() if k in KERNEL_BYTES}
     return {"solver": s, "ms": ms, "launches": launches, "value": cells * steps / (ms * 1e-3),
             "kernel": name, "per_launch_ms": per_launch, "bytes_per_cell": kb,
             "achieved_gbs": (kb * cells / (per_launch * 1e-3) / 1e9) if kb else None,
             "kernel_share": kms / total_k,
-            "kernels_ms_per_step": {k: v[1] / steps for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])}}
+            "kernels_ms_per_step": {k: v[1] / steps for k, v in sorted(table.items(), key=lambda kv: -kv[1][1])},
+            "kernels_gbs": dict(sorted(gbs.items(), key=lambda kv: -kv[1]))}
 
 
 def accuracy(lib, case, nsteps, local):
@@ -255,6 +257,7 @@ def accuracy(lib, case, nsteps, local):
         rc = s.step(nsteps)
         if rc != lib.OK:
             return {"steps": nsteps, "error": f"{nm}: {lib.status_string(rc)} at step {s.error_step()}"}
+        out[f"value_{nm}"] = case.params.nx * case.params.ny * nsteps / (s.last_step_ms() * 1e-3)
         k1, a1, m1 = s.diag()
         res[nm] = s.download()
         out[f"mass_drift_{nm}"] = (m1 - m0) / m0
@@ -265,6 +268,47 @@ def accuracy(lib, case, nsteps, local):
     out["h_rel_l2"] = float(np.linalg.norm((a["eta"] - b["eta"])[I]) / np.linalg.norm((b["eta"] + d)[I]))
     for k in ("u", "v"):
         out[f"{k}_rel_l2"] = float(np.linalg.norm((a[k] - b[k])[I]) / np.linalg.norm(b[k][I]))
+    return out
+
+
+def parity_fp64(lib, case, nsteps, local):
+    """The FP64 CUDA step against the oracle (the C restatement of the
+    reference step, pinned to the reference's own frames) after nsteps from
+    the same state: whether every padded cell of eta, u and v is bit-identical,
+    the relative L2 over the interior of h = eta + depth, u and v, and the
+    relative mass and energy drift of each."""
+    from oracle import oracle as orc
+
+    p = case.params
+    s = lib.Solver(p, precision=lib.FP64, device=local)
+    s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+    g0 = s.diag()
+    rc = s.step(nsteps)
+    if rc != lib.OK:
+        return {"steps": nsteps, "error": f"gpu: {lib.status_string(rc)} at step {s.error_step()}"}
+    g1 = s.diag()
+    got = s.download()
+    s.close()
+    o = orc.Oracle(p)
+    o.load(case.fields())
+    r0 = o.energy()
+    t0 = time.perf_counter()
+    rc, bad = o.step(nsteps)
+    secs = time.perf_counter() - t0
+    if rc:
+        return {"steps": nsteps, "error": f"oracle: rc {rc} at step {bad}"}
+    r1 = o.energy()
+    ref = {k: o.field(k) for k in ("eta", "u", "v")}
+    I = (slice(2, -2), slice(2, -2))
+    out = {"steps": nsteps, "bit_identical": all(np.array_equal(got[k], ref[k]) for k in ref),
+           "h_rel_l2": float(np.linalg.norm((got["eta"] - ref["eta"])[I]) / np.linalg.norm((ref["eta"] + p.depth)[I]))}
+    for k in ("u", "v"):
+        out[f"{k}_rel_l2"] = float(np.linalg.norm((got[k] - ref[k])[I]) / np.linalg.norm(ref[k][I]))
+    for nm, (a, b) in (("gpu", (g0, g1)), ("oracle", (r0, r1))):
+        out[f"mass_drift_{nm}"] = (b[2] - a[2]) / a[2]
+        out[f"energy_drift_{nm}"] = ((b[0] + b[1]) - (a[0] + a[1])) / (a[0] + a[1])
+    out["oracle_seconds"] = secs
+    out["oracle_threads"] = orc.threads()
     return out
 
 
@@ -298,23 +342,29 @@ def ensemble(lib, nsteps, tune_steps, acc_steps, local, seed=7):
            "schedule": b.schedule(), "tune_ms_per_step": tune, "limiter": "Van Leer (r <= 0 -> 0)"}
     b.close()
     if acc_steps > 0:
-        worst = 0.0
-        picks = [0, 16, 40]
-        for m in picks:
-            c = cs[m]
-            d = c.params.depth
-            res = {}
-            for nm, prec in (("fp64", lib.FP64), ("fp32", lib.FP32)):
-                s = lib.Solver(c.params, precision=prec, device=local, flags=lib.FLAG_VANLEER_SAFE)
-                s.upload(*c.fields())
-                if s.step(acc_steps) != lib.OK:
-                    raise RuntimeError("ensemble accuracy run failed")
-                res[nm] = s.download()["eta"][2:-2, 2:-2]
-                s.close()
-            e = float(np.linalg.norm(res["fp32"] - res["fp64"]) / np.linalg.norm(res["fp64"] + d))
-            worst = max(worst, e)
-        out["worst_member_h_rel_l2"] = worst
-        out["accuracy_members"] = [f"{cs[m].params.nx}x{cs[m].params.ny}" for m in picks]
+        # every member from its initial state, acc_steps steps as one batch,
+        # against the FP64 step of the same member run alone
+        for s, c in zip(solvers, cs):
+            s.upload(*c.fields())
+        b = lib.Batch(solvers)
+        if b.step(acc_steps) != lib.OK:
+            raise RuntimeError(f"ensemble accuracy batch failed: {b.error()}")
+        b.close()
+        errs = []
+        for s, c in zip(solvers, cs):
+            e32 = s.download()["eta"][2:-2, 2:-2]
+            ref = lib.Solver(c.params, precision=lib.FP64, device=local, flags=lib.FLAG_VANLEER_SAFE)
+            ref.upload(*c.fields())
+            if ref.step(acc_steps) != lib.OK:
+                raise RuntimeError("ensemble FP64 reference run failed")
+            e64 = ref.download()["eta"][2:-2, 2:-2]
+            ref.close()
+            errs.append(float(np.linalg.norm(e32 - e64) / np.linalg.norm(e64 + c.params.depth)))
+        w = int(np.argmax(errs))
+        out["worst_member_h_rel_l2"] = errs[w]
+        out["worst_member"] = {"index": w, "grid": f"{cs[w].params.nx}x{cs[w].params.ny}"}
+        out["median_member_h_rel_l2"] = float(np.median(errs))
+        out["accuracy_members"] = f"all {len(cs)} (the batched run against each member's FP64 run alone)"
         out["accuracy_steps"] = acc_steps
     for s in solvers:
         s.close()
@@ -331,6 +381,10 @@ def main():
     ap.add_argument("--fp32-config", default="saturn4096", help="workload of the FP32-form throughput line")
     ap.add_argument("--accuracy-steps", type=int, default=2000)
     ap.add_argument("--ensemble-steps", type=int, default=1000, help="0 skips the 64-member ensemble leg")
+    ap.add_argument("--parity-steps", type=int, default=2000,
+                    help="steps of the FP64 step against the oracle on the headline workload (0 skips)")
+    ap.add_argument("--large-config", default="band8192", help="workload of the large case run in both forms")
+    ap.add_argument("--large-steps", type=int, default=1000, help="steps of the large case (0 skips it)")
     ap.add_argument("--cpu-steps", type=int, default=None, help="oracle steps for the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -405,6 +459,25 @@ def main():
     if acc:
         acc["workload"] = args.fp32_config
     ens = ensemble(lib, args.ensemble_steps, 5, min(args.ensemble_steps, 1000), local) if args.ensemble_steps > 0 else None
+    # the large case in both forms: per-kernel times and GB/s over a short
+    # timed run, then large_steps steps of each form (throughput over the
+    # whole run, errors of the FP32 form against the FP64 one)
+    large = None
+    if args.large_steps > 0:
+        cl, descl = make_workload(args.large_config, seed=1 + rank)
+        ml64 = measure(lib, cl, lib.FP64, args.steps, args.warmup, local, barrier)
+        ml64["solver"].close()
+        ml32 = measure(lib, cl, lib.FP32, args.steps, args.warmup, local, barrier)
+        ml32["solver"].close()
+        accl = accuracy(lib, cl, args.large_steps, local)
+        accl["workload"] = args.large_config
+        large = (cl.params.nx * cl.params.ny, descl, ml64, ml32, accl)
+        del cl
+    # the FP64 step against the oracle at the drop-in configuration's length
+    par = None
+    if args.parity_steps > 0 and rank == 0:
+        par = parity_fp64(lib, case, args.parity_steps, local)
+        par["workload"] = args.config
 
     if rank != 0:
         pg.destroy_process_group()
@@ -426,7 +499,7 @@ def main():
                 "dominant_kernel": m["kernel"], "kernel_per_launch_ms": m["per_launch_ms"],
                 "kernel_bytes_per_cell": m["bytes_per_cell"], "kernel_achieved_gbs": m["achieved_gbs"],
                 "kernel_frac_of_measured_hbm": (m["achieved_gbs"] / peak) if m["achieved_gbs"] else None,
-                "kernels_ms_per_step": m["kernels_ms_per_step"]}
+                "kernels_ms_per_step": m["kernels_ms_per_step"], "kernels_gbs": m["kernels_gbs"]}
 
     clocks = clk.summary()
     fp64_roof = None
@@ -438,6 +511,16 @@ def main():
                      "unit": "FP64 instr/s", "frac": ach / pk, "instr_per_cell": n64,
                      "peak_kind": "ncu per-cycle FP64 peak x median SM clock under load"}
 
+    forms = {
+        "fp64": form_line(m64, args.config, cells),
+        "fp32": form_line(m32, args.config, cells),
+        "fp32_large": form_line(m32b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
+        "fp64_large": form_line(m64b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
+    }
+    if large:
+        nl, descl, ml64, ml32, accl = large
+        forms["fp64_" + args.large_config] = form_line(ml64, f"{args.large_config}: {descl}", nl)
+        forms["fp32_" + args.large_config] = form_line(ml32, f"{args.large_config}: {descl}", nl)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -459,15 +542,12 @@ def main():
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_out},
         "clocks": clocks,
         "cpu_baseline": cpu,
-        "forms": {
-            "fp64": form_line(m64, args.config, cells),
-            "fp32": form_line(m32, args.config, cells),
-            "fp32_large": form_line(m32b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
-            "fp64_large": form_line(m64b, f"{args.fp32_config}: {desc32}", c32.params.nx * c32.params.ny),
-        },
+        "forms": forms,
+        "large_case_both_forms": large[4] if large else None,
         "fp32_over_fp64": m32["value"] / m64["value"],
         "fp32_over_fp64_large": m32b["value"] / m64b["value"],
         "accuracy_fp32_vs_fp64": acc,
+        "parity_fp64_vs_oracle": par,
         "ensemble_fp32_batched": ens,
         "fp32_batched_over_fp64": (ens["value"] / m64["value"]) if ens else None,
     }

@@ -191,6 +191,24 @@ sw2g_status sw2g_add_field(sw2g_ctx *ctx, int which, const double *delta, double
 sw2g_status sw2g_set_field_where(sw2g_ctx *ctx, int which, const double *value, const unsigned char *mask);
 sw2g_status sw2g_apply_channel(sw2g_ctx *ctx);
 
+/* The same forcing on a list of cells, for injections that touch few cells
+ * (a Gaussian truncated at its radius, get_Gaussian_field, perturbs.c:333-364):
+ * only the list crosses to the GPU. `cells` holds n padded indices
+ * (i+1)+(j+1)*(nx+4) of interior cells, strictly increasing; `values` their n
+ * values. Each call ends with the single-rank halo wrap of the field.
+ *   sw2g_add_cells: field(i,j) += scale * value for listed cells and
+ *                   field(i,j) += scale * 0.0 for every other interior cell,
+ *                   exactly the reference's loop over the whole grid
+ *                   (perturbs.c:305-309), so the result is that of
+ *                   sw2g_add_field with a delta that is zero off the list;
+ *   sw2g_set_cells: field(i,j) = value for listed cells (TRACER inside the
+ *                   radius, perturbs.c:356), others unchanged.
+ * The lists are copied before the call returns; the work is queued on the
+ * context's stream without waiting for it. FP64 contexts only. */
+sw2g_status sw2g_add_cells(sw2g_ctx *ctx, int which, const int *cells, const double *values, int n,
+                           double scale);
+sw2g_status sw2g_set_cells(sw2g_ctx *ctx, int which, const int *cells, const double *values, int n);
+
 /* Device pointer of a padded state field (0 eta, 1 u, 2 v, 3 tracer) for
  * callers that keep data on the GPU; NULL on a bad index. */
 void *sw2g_device_field(sw2g_ctx *ctx, int which);

@@ -175,6 +175,22 @@ struct sw2g_ctx {
   // forcing between steps (FP64 form): staging of one padded field and a mask
   double* d_force = nullptr;
   void* d_mask = nullptr;
+  // forcing on listed cells: two pinned staging slots for the caller's index
+  // and value lists (used in turn, each free again once its event has
+  // completed), the lists on the device, and a padded field that is zero
+  // outside the cells of the call in progress
+  struct CellSlot {
+    int* idx = nullptr;
+    double* val = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+  } cell_slot[2];
+  int cell_next = 0;
+  int* d_cells = nullptr;
+  double* d_cellv = nullptr;
+  size_t d_cell_cap = 0;
+  double* d_delta = nullptr;
   // sw2g_step_host: a second stream for the copies of v, eta and u, and the
   // events u copied in, eta copied in, eta final, side copies done, u's
   // interior final, step done, v copied in (made on first use)
@@ -1087,6 +1103,93 @@ sw2g_status sw2g_set_field_where(sw2g_ctx* x, int which, const double* value, co
   return SW2G_OK;
 }
 
+namespace {
+// Checks a cell list (strictly increasing padded indices of interior cells)
+// and queues its copy to the device through the next staging slot; returns
+// with d_cells/d_cellv holding the list in stream order.
+sw2g_status stage_cells(sw2g_ctx* x, const int* cells, const double* values, int n) {
+  const DevState& s = x->s;
+  if (n < 0 || (long long)n > (long long)s.nx * s.ny) return SW2G_ERR_BAD_ARG;
+  if (n > 0 && (!cells || !values)) return SW2G_ERR_BAD_ARG;
+  for (int k = 0; k < n; k++) {
+    const int q = cells[k], j = q / s.W - 1, i = q - (j + 1) * s.W - 1;
+    if (q < 0 || i < 1 || i > s.nx || j < 1 || j > s.ny) return SW2G_ERR_BAD_ARG;
+    if (k > 0 && q <= cells[k - 1]) return SW2G_ERR_BAD_ARG;
+  }
+  if (!x->d_delta) {
+    sw2g_status st = dalloc(x, &x->d_delta, (size_t)s.W * s.H);  // zeroed
+    if (st != SW2G_OK) return st;
+  }
+  if (n == 0) return SW2G_OK;
+  if ((size_t)n > x->d_cell_cap) {  // grows rarely: cudaFree orders itself after the queued work
+    if (x->d_cells) CK(cudaFree(x->d_cells));
+    if (x->d_cellv) CK(cudaFree(x->d_cellv));
+    x->d_cells = nullptr;
+    x->d_cellv = nullptr;
+    x->d_cell_cap = 0;
+    CK(cudaMalloc((void**)&x->d_cells, sizeof(int) * (size_t)n));
+    CK(cudaMalloc((void**)&x->d_cellv, sizeof(double) * (size_t)n));
+    x->d_cell_cap = (size_t)n;
+  }
+  auto& sl = x->cell_slot[x->cell_next];
+  x->cell_next ^= 1;
+  if (!sl.done) CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
+  if (sl.pending) CK(cudaEventSynchronize(sl.done));  // the copy that last used this slot
+  sl.pending = false;
+  if ((size_t)n > sl.cap) {
+    if (sl.idx) CK(cudaFreeHost(sl.idx));
+    if (sl.val) CK(cudaFreeHost(sl.val));
+    sl.idx = nullptr;
+    sl.val = nullptr;
+    sl.cap = 0;
+    CK(cudaHostAlloc((void**)&sl.idx, sizeof(int) * (size_t)n, cudaHostAllocDefault));
+    CK(cudaHostAlloc((void**)&sl.val, sizeof(double) * (size_t)n, cudaHostAllocDefault));
+    sl.cap = (size_t)n;
+  }
+  std::memcpy(sl.idx, cells, sizeof(int) * (size_t)n);
+  std::memcpy(sl.val, values, sizeof(double) * (size_t)n);
+  CK(cudaMemcpyAsync(x->d_cells, sl.idx, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->d_cellv, sl.val, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaEventRecord(sl.done, x->stream));
+  sl.pending = true;
+  return SW2G_OK;
+}
+
+void tracer_from_list(sw2g_ctx* x, int which, const double* values, int n) {
+  if (which != 3 || x->tracer_active) return;
+  for (int k = 0; k < n; k++)
+    if (values[k] != 0.0 || std::signbit(values[k])) {
+      x->tracer_active = true;
+      return;
+    }
+}
+}  // namespace
+
+sw2g_status sw2g_add_cells(sw2g_ctx* x, int which, const int* cells, const double* values, int n, double scale) {
+  sw2g_status st = force_ready(x, which);
+  if (st != SW2G_OK) return st;
+  if ((st = stage_cells(x, cells, values, n)) != SW2G_OK) return st;
+  // every interior cell gets field += scale * delta, as the reference's loop
+  // over the whole grid does (perturbs.c:308), with delta zero off the list
+  fp64_scatter_cells(x->d_delta, x->d_cells, x->d_cellv, n, x->stream);
+  fp64_add_scaled(x->b.f[which], x->d_delta, scale, x->s.nx, x->s.ny, x->stream);
+  fp64_scatter_cells(x->d_delta, x->d_cells, nullptr, n, x->stream);
+  CK(cudaGetLastError());
+  tracer_from_list(x, which, values, n);
+  return SW2G_OK;
+}
+
+sw2g_status sw2g_set_cells(sw2g_ctx* x, int which, const int* cells, const double* values, int n) {
+  sw2g_status st = force_ready(x, which);
+  if (st != SW2G_OK) return st;
+  if ((st = stage_cells(x, cells, values, n)) != SW2G_OK) return st;
+  fp64_scatter_cells(x->b.f[which], x->d_cells, x->d_cellv, n, x->stream);
+  halo_wrap(x->b.f[which], x->s.nx, x->s.ny, x->stream);
+  CK(cudaGetLastError());
+  tracer_from_list(x, which, values, n);
+  return SW2G_OK;
+}
+
 sw2g_status sw2g_apply_channel(sw2g_ctx* x) {
   sw2g_status st = force_ready(x, 0);
   if (st != SW2G_OK) return st;
@@ -1119,6 +1222,13 @@ void sw2g_destroy(sw2g_ctx* x) {
   if (x->d_bad) cudaFree(x->d_bad);
   if (x->d_strips) cudaFree(x->d_strips);
   if (x->d_mask) cudaFree(x->d_mask);
+  if (x->d_cells) cudaFree(x->d_cells);
+  if (x->d_cellv) cudaFree(x->d_cellv);
+  for (auto& sl : x->cell_slot) {
+    if (sl.idx) cudaFreeHost(sl.idx);
+    if (sl.val) cudaFreeHost(sl.val);
+    if (sl.done) cudaEventDestroy(sl.done);
+  }
   if (x->h_chk) cudaFreeHost(x->h_chk);
   x->timers.release();
   x->run32.release();

@@ -1443,6 +1443,10 @@ __global__ void k_set_where(int nx, int ny, double* f, const double* val, const 
     if (mask[q]) f[q] = val[q];
   }
 }
+__global__ void k_scatter_cells(double* f, const int* __restrict__ cells, const double* __restrict__ values, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    f[cells[t]] = values ? values[t] : 0.0;
+}
 }  // namespace
 
 void fp64_add_scaled(double* f, const double* d, double scale, int nx, int ny, cudaStream_t st) {
@@ -1455,6 +1459,12 @@ void fp64_set_where(double* f, const double* val, const unsigned char* mask, int
   const int n = nx * ny, blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
   k_set_where<<<blocks, 256, 0, st>>>(nx, ny, f, val, mask);
   halo_wrap(f, nx, ny, st);
+}
+
+void fp64_scatter_cells(double* f, const int* cells, const double* values, int n, cudaStream_t st) {
+  if (n <= 0) return;
+  const int blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+  k_scatter_cells<<<blocks, 256, 0, st>>>(f, cells, values, n);
 }
 
 void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, cudaStream_t st) {

@@ -142,6 +142,8 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
 void fp64_add_scaled(double* f, const double* d, double scale, int nx, int ny, cudaStream_t st);
 void fp64_set_where(double* f, const double* val, const unsigned char* mask, int nx, int ny, cudaStream_t st);
 void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, cudaStream_t st);
+// f[cells[k]] = values[k] (values NULL: 0.0) for k < n; the cells are distinct.
+void fp64_scatter_cells(double* f, const int* cells, const double* values, int n, cudaStream_t st);
 // Compares the step's division by a row metric (div_rcp) with IEEE division
 // on `samples` random numerators per divisor; returns the mismatch count in
 // *bad (device pointer) once the stream is done.

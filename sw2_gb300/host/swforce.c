@@ -68,7 +68,18 @@ int swforce_init(swforce *w, int nx, int ny) {
   w->deta = (double *)calloc(S, sizeof(double));
   w->du = (double *)calloc(S, sizeof(double));
   w->dv = (double *)calloc(S, sizeof(double));
-  if (!w->pert || !w->tracer || !w->mask || !w->perturbs || !w->deta || !w->du || !w->dv) {
+  const size_t N = (size_t)nx * ny;
+  w->cells = (int *)calloc(N, sizeof(int));
+  w->cell_pert = (double *)calloc(N, sizeof(double));
+  w->cell_tracer = (double *)calloc(N, sizeof(double));
+  w->row_pl = (double *)calloc((size_t)ny + 2, sizeof(double));
+  w->row_sin = (double *)calloc((size_t)ny + 2, sizeof(double));
+  w->row_cos = (double *)calloc((size_t)ny + 2, sizeof(double));
+  w->row_surf = (double *)calloc((size_t)ny + 2, sizeof(double));
+  w->col_lonc = (double *)calloc((size_t)nx + 2, sizeof(double));
+  if (!w->pert || !w->tracer || !w->mask || !w->perturbs || !w->deta || !w->du || !w->dv || !w->cells ||
+      !w->cell_pert || !w->cell_tracer || !w->row_pl || !w->row_sin || !w->row_cos || !w->row_surf ||
+      !w->col_lonc) {
     swforce_free(w);
     return -1;
   }
@@ -83,24 +94,84 @@ void swforce_free(swforce *w) {
   free(w->deta);
   free(w->du);
   free(w->dv);
+  free(w->cells);
+  free(w->cell_pert);
+  free(w->cell_tracer);
+  free(w->row_pl);
+  free(w->row_sin);
+  free(w->row_cos);
+  free(w->row_surf);
+  free(w->col_lonc);
   memset(w, 0, sizeof *w);
 }
 
+/* Per-case tables of the values the Gaussian loops use per row and column:
+ * the same functions of the same arguments as the reference evaluates per
+ * cell, so the cached numbers are its numbers. */
+static void tables(const swcase *c, swforce *w) {
+  if (w->tables_ready) return;
+  for (int j = 1; j <= c->ny; j++) {
+    const double pl = swf_lat2pclat(c, swf_latc(c, j));
+    w->row_pl[j] = pl;
+    w->row_sin[j] = sin(pl);
+    w->row_cos[j] = cos(pl);
+    w->row_surf[j] = swf_DXC(c, j) * swf_DYC(c, j);
+  }
+  for (int i = 1; i <= c->nx; i++) w->col_lonc[i] = swf_lonc(c, i);
+  w->tables_ready = 1;
+}
+
+static int cmp_int(const void *a, const void *b) {
+  const int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+/* Margin (radians of central angle) of the test that skips cells outside
+ * the radius. The reference's computed distance differs from the exact
+ * central angle of its inputs by far less than this (about 1e-15 / sin of
+ * the angle: a few 1e-9 at angles of 1e-6), so a cell whose exact angle
+ * exceeds radius/R + kSkipMargin is one where the reference finds
+ * r >= radius and changes nothing. */
+#define kSkipMargin 1e-6
+
 /* get_Gaussian_field, fill mode 1 (perturbs.c:333-364): every interior cell
  * whose great-circle distance (tools.c:104-119, on the mean radius, between
- * planetocentric latitudes) is below the radius. */
+ * planetocentric latitudes) is below the radius. Cells that cannot be inside
+ * are skipped before that expression is evaluated: the central angle to the
+ * centre is at least the difference of latitudes, and in a row at latitude
+ * pl it exceeds th = radius/R + margin wherever the longitude difference
+ * (mod 2 pi, as the cosine in the distance sees it) exceeds
+ * acos((cos th - sin(plat) sin(pl)) / (cos(plat) cos(pl))). */
 static void gaussian_field(const swcase *c, double lon, double lat, double amp, double sigma, double radius,
                            double inject, swforce *w) {
   const double R = (c->rE + c->rP) / 2.0;
   const double plat = swf_lat2pclat(c, lat);
+  const double sp = sin(plat), cp = cos(plat);
+  const double th = radius / R + kSkipMargin;
+  const double two_pi = 8.0 * atan(1.0);
+  const int skip = (th < 3.0);  /* otherwise every cell can be inside (or radius is not a number) */
+  const double cth = cos(th);
   for (int j = 1; j <= c->ny; j++) {
-    const double pl = swf_lat2pclat(c, swf_latc(c, j));
+    const double pl = w->row_pl[j];
+    double dl = 4.0;  /* largest longitude difference that can be inside; >= pi: all */
+    if (skip) {
+      if (fabs(pl - plat) > th) continue;
+      const double cmin = (cth - sp * w->row_sin[j]) / (cp * w->row_cos[j]);
+      if (cmin > 1.0) continue;
+      if (cmin > -1.0) dl = acos(cmin) + kSkipMargin;
+    }
     for (int i = 1; i <= c->nx; i++) {
-      const double r = (R)*acos(sin(plat) * sin(pl) + cos(plat) * cos(pl) * cos(swf_lonc(c, i) - lon));
+      if (dl < 3.14) {
+        double d = w->col_lonc[i] - lon;
+        d -= two_pi * nearbyint(d / two_pi);
+        if (fabs(d) > dl) continue;
+      }
+      const double r = (R)*acos(sin(plat) * w->row_sin[j] + cos(plat) * w->row_cos[j] * cos(w->col_lonc[i] - lon));
       if (r < radius) {
         const size_t q = IXP(c->nx, i, j);
         w->pert[q] += amp * exp(-sq(r) / (2.0 * sq(sigma)));
         w->tracer[q] = (inject)*exp(-sq(r) / (2.0 * sq(sigma)));
+        if (!w->mask[q]) w->cells[w->ncells++] = (int)q;
         w->mask[q] = 1;
         w->perturbs[q] = 1.0;
       }
@@ -158,20 +229,30 @@ int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, do
   while (lon < c->lon0) lon += (c->lon1 - c->lon0);
   while (lon > c->lon1) lon -= (c->lon1 - c->lon0);
   const double amp = volume / (2.0 * PI_() * sq(sigma) * (1.0 - exp(-sq(radius) / (2.0 * sq(sigma)))));
-  const size_t S = (size_t)(c->nx + 4) * (c->ny + 4);
-  memset(w->pert, 0, S * sizeof(double));
-  memset(w->mask, 0, S);
+  tables(c, w);
+  /* the previous injection's cells back to zero (the reference starts from a
+   * zeroed perturb_field, perturbs.c:237-238) */
+  for (int k = 0; k < w->ncells; k++) {
+    w->pert[w->cells[k]] = 0.0;
+    w->mask[w->cells[k]] = 0;
+  }
+  w->ncells = 0;
   gaussian_field(c, lon, lat, amp, sigma, radius, inject, w);
   const double lonRight = lon + (c->lon1 - c->lon0);
   const double lonLeft = lon - (c->lon1 - c->lon0);
   if ((lon + radius / swf_rZ(c, lat)) >= c->lon1) gaussian_field(c, lonLeft, lat, amp, sigma, radius, inject, w);
   if ((lon - radius / swf_rZ(c, lat)) <= c->lon0) gaussian_field(c, lonRight, lat, amp, sigma, radius, inject, w);
-  /* injected volume, summed in the reference's loop order (j outer, i inner) */
-  double V = 0.0;
-  for (int j = 1; j <= c->ny; j++) {
-    const double s = swf_DXC(c, j) * swf_DYC(c, j);
-    for (int i = 1; i <= c->nx; i++) V += w->pert[IXP(c->nx, i, j)] * s;
+  /* padded index order is the reference's loop order (j outer, i inner) */
+  qsort(w->cells, (size_t)w->ncells, sizeof(int), cmp_int);
+  const int W = c->nx + 4;
+  for (int k = 0; k < w->ncells; k++) {
+    w->cell_pert[k] = w->pert[w->cells[k]];
+    w->cell_tracer[k] = w->tracer[w->cells[k]];
   }
+  /* injected volume, summed in the reference's loop order; the cells off the
+   * list add +0.0, which changes no sum that starts at +0.0 */
+  double V = 0.0;
+  for (int k = 0; k < w->ncells; k++) V += w->cell_pert[k] * w->row_surf[w->cells[k] / W - 1];
   if (fabs(volume) > 1e-7) {
     if (V == 0.0) {
       set_err(err, errlen, "Gaussian %d: total injected volume is 0", g);
@@ -180,10 +261,7 @@ int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, do
     const double rf = (volume / V);
     /* the reference's own check of the rescaled volume (perturbs.c:310-326) */
     double Vc = 0.0;
-    for (int j = 1; j <= c->ny; j++) {
-      const double s = swf_DXC(c, j) * swf_DYC(c, j);
-      for (int i = 1; i <= c->nx; i++) Vc += (rf * w->pert[IXP(c->nx, i, j)]) * s;
-    }
+    for (int k = 0; k < w->ncells; k++) Vc += (rf * w->cell_pert[k]) * w->row_surf[w->cells[k] / W - 1];
     if (fabs(Vc - volume) / volume > 1e-1) {
       set_err(err, errlen, "Gaussian %d: injected volume %e does not match %e", g, Vc, volume);
       return -1;

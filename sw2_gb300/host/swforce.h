@@ -26,6 +26,17 @@ typedef struct {
   unsigned char *mask; /* cells inside the radius (where TRACER and PERTURBS are set) */
   double *perturbs;    /* the reference's PERTURBS field (1 inside any radius this step) */
   double *deta, *du, *dv;  /* one vortex: increments of eta, u, v */
+  /* The cells inside the radius of the last injection: ncells padded
+   * indices, increasing, with their Gaussian (cell_pert) and tracer
+   * (cell_tracer) values, the same numbers as pert/tracer hold there. */
+  int *cells;
+  int ncells;
+  double *cell_pert, *cell_tracer;
+  /* per-case tables, filled on first use: planetocentric latitude of row j
+   * and its sine and cosine, area element DXC*DYC of row j, longitude of
+   * column i (index j or i, 0..n+1) */
+  double *row_pl, *row_sin, *row_cos, *row_surf, *col_lonc;
+  int tables_ready;
 } swforce;
 
 int swforce_init(swforce *w, int nx, int ny);
@@ -45,9 +56,12 @@ double swf_DYC(const swcase *c, int j);
 
 /* One Gaussian injection that is active at time t (t0 <= t <= t1 of row g):
  * fills w->pert (zeroed first), sets w->tracer/w->mask for the cells inside
- * the radius (mask zeroed first), sets w->perturbs to 1 there, and returns in
- * *scale the rescale factor volume/V (perturbs.c:303-309), or 0 when the
- * volume is below the reference's 1e-7 threshold (no eta change).
+ * the radius (mask zeroed first), sets w->perturbs to 1 there, lists those
+ * cells in w->cells/cell_pert/cell_tracer, and returns in *scale the rescale
+ * factor volume/V (perturbs.c:303-309), or 0 when the volume is below the
+ * reference's 1e-7 threshold (no eta change). Only cells that can lie inside
+ * the radius are evaluated (see swforce.c); the others keep zero, as the
+ * reference's evaluation of them gives.
  * Returns 0, 1 if row g is not active at t, or -1 on an error of the case
  * (message in err). */
 int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, double *scale, char *err,

@@ -246,21 +246,57 @@ static int ck(sw2g_status st, const char *what) {
   return -1;
 }
 
+/* The cells of the PERTURBS field (w->perturbs) set to 1 since it was last
+ * cleared, so that clearing it (core.c:94, 292) touches those cells only;
+ * `all` when its content came from elsewhere (a loaded frame). */
+typedef struct {
+  int *idx;
+  size_t n, cap;
+  int all;
+} marks;
+
+static int marks_add(marks *m, const int *idx, int n) {
+  if (m->n + (size_t)n > m->cap) {
+    size_t cap = m->cap ? m->cap : 1024;
+    while (cap < m->n + (size_t)n) cap *= 2;
+    int *p = (int *)realloc(m->idx, cap * sizeof(int));
+    if (!p) return -1;
+    m->idx = p;
+    m->cap = cap;
+  }
+  memcpy(m->idx + m->n, idx, (size_t)n * sizeof(int));
+  m->n += (size_t)n;
+  return 0;
+}
+
+static void perturbs_clear(swforce *w, marks *m) {
+  if (m->all) memset(w->perturbs, 0, (size_t)(w->nx + 4) * (w->ny + 4) * sizeof(double));
+  else
+    for (size_t k = 0; k < m->n; k++) w->perturbs[m->idx[k]] = 0.0;
+  m->n = 0;
+  m->all = 0;
+}
+
 /* The forcing of the step that ends at time t (core.c:292-302, perturbs.c):
  * Gaussians, then vortices. During the run it is applied between
  * sw2g_step_open and sw2g_step_close, where the reference applies it (after
  * the velocity halos, before do_channel); at t0 it is followed by
- * sw2g_apply_channel (core.c:96-101). */
-static int apply_forcing(const swcase *c, sw2g_ctx *g, swforce *w, double Dt, double t, char *err, size_t errlen) {
-  const size_t S = (size_t)(c->nx + 4) * (c->ny + 4);
-  memset(w->perturbs, 0, S * sizeof(double));
+ * sw2g_apply_channel (core.c:96-101). A Gaussian sends only the cells inside
+ * its radius to the GPU (sw2g_set_cells, sw2g_add_cells). */
+static int apply_forcing(const swcase *c, sw2g_ctx *g, swforce *w, marks *pm, double Dt, double t, char *err,
+                         size_t errlen) {
+  perturbs_clear(w, pm);
   for (int k = 0; k < c->num_gaussians; k++) {
     double rf = 0;
     const int rc = swforce_gaussian(c, k, Dt, t, w, &rf, err, errlen);
     if (rc < 0) return -1;
     if (rc == 1) continue;
-    if (ck(sw2g_set_field_where(g, 3, w->tracer, w->mask), "tracer")) return -1;
-    if (rf != 0.0 && ck(sw2g_add_field(g, 0, w->pert, rf), "eta")) return -1;
+    if (marks_add(pm, w->cells, w->ncells)) {
+      snprintf(err, errlen, "out of host memory");
+      return -1;
+    }
+    if (ck(sw2g_set_cells(g, 3, w->cells, w->cell_tracer, w->ncells), "tracer")) return -1;
+    if (rf != 0.0 && ck(sw2g_add_cells(g, 0, w->cells, w->cell_pert, w->ncells, rf), "eta")) return -1;
   }
   for (int k = 0; k < c->num_vortices; k++) {
     if (!swforce_vortex_due(c, k, Dt, t)) continue;
@@ -301,6 +337,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
   int rc = 1;
   sw2g_ctx *g = NULL;
   swforce w = {0};
+  marks pm = {0};
   double *f[5] = {NULL, NULL, NULL, NULL, NULL}, *windx = NULL, *windy = NULL, *zero = NULL;
   double *f2[5] = {NULL, NULL, NULL, NULL, NULL};
   frame_writer wr;
@@ -371,7 +408,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
   double t = c.t0;
   /* forcing at t0 and the wall fixes (core.c:96-101) */
   if (!fp32 && resume < 0) {
-    if (apply_forcing(&c, g, &w, Dt, t, err, sizeof err)) {
+    if (apply_forcing(&c, g, &w, &pm, Dt, t, err, sizeof err)) {
       if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
       goto done;
     }
@@ -391,6 +428,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
     }
     nstart = ns;
     memcpy(w.perturbs, f[4], S * sizeof(double));
+    pm.all = 1;
     if (ck(sw2g_upload(g, f[0], f[1], f[2], f[3], windx, windy, zero, SW2G_UPLOAD_FRAME), "load")) goto done;
   } else {
     if (ck(sw2g_download(g, f[0], f[1], f[2], f[3]), "download")) goto done;
@@ -420,7 +458,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
     if (st == SW2G_OK && forced) {
       st = sw2g_step_open(g);
       if (st == SW2G_OK) {
-        if (apply_forcing(&c, g, &w, Dt, tk, err, sizeof err)) {
+        if (apply_forcing(&c, g, &w, &pm, Dt, tk, err, sizeof err)) {
           if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
           goto done;
         }
@@ -439,7 +477,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
     for (int q = 0; q < k; q++) t += Dt;  /* core.c:145 */
     n += k;
     const int m = n - 1;  /* the step just finished */
-    if (!forced) memset(w.perturbs, 0, S * sizeof(double));  /* core.c:292 */
+    if (!forced) perturbs_clear(&w, &pm);  /* core.c:292 */
     if (m % c.saveEvery == 0) {  /* core.c:315-320 */
       /* the writer holds at most the other set: submitting it waited for this one */
       double *const *fs = set ? f2 : f;
@@ -459,6 +497,7 @@ done:
   if (writer_stop(&wr) && rc == 0) rc = 1;
   if (g) sw2g_destroy(g);
   swforce_free(&w);
+  free(pm.idx);
   for (int k = 0; k < 5; k++) free(f[k]);
   for (int k = 0; k < 5; k++) free(f2[k]);
   free(windx);

@@ -35,7 +35,11 @@ class SwCase(ctypes.Structure):
 
 class SwForce(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("pert", _P), ("tracer", _P),
-                ("mask", ctypes.POINTER(ctypes.c_ubyte)), ("perturbs", _P), ("deta", _P), ("du", _P), ("dv", _P)]
+                ("mask", ctypes.POINTER(ctypes.c_ubyte)), ("perturbs", _P), ("deta", _P), ("du", _P), ("dv", _P),
+                ("cells", ctypes.POINTER(ctypes.c_int)), ("ncells", ctypes.c_int),
+                ("cell_pert", _P), ("cell_tracer", _P),
+                ("row_pl", _P), ("row_sin", _P), ("row_cos", _P), ("row_surf", _P), ("col_lonc", _P),
+                ("tables_ready", ctypes.c_int)]
 
 
 _lib = None
@@ -158,6 +162,14 @@ class Forcing:
         return (rc, rf.value, self._arr(self.w.pert), self._arr(self.w.tracer),
                 np.ctypeslib.as_array(self.w.mask, (self.shape[0] * self.shape[1],)).reshape(self.shape).copy(),
                 self._arr(self.w.perturbs))
+
+    def cells(self):
+        """The last injection's cell list: (padded indices, Gaussian values, tracer values)."""
+        n = self.w.ncells
+        if n == 0:
+            return np.zeros(0, np.int32), np.zeros(0), np.zeros(0)
+        return (np.ctypeslib.as_array(self.w.cells, (n,)).copy(), np.ctypeslib.as_array(self.w.cell_pert, (n,)).copy(),
+                np.ctypeslib.as_array(self.w.cell_tracer, (n,)).copy())
 
     def vortex(self, row: int):
         load().swforce_vortex(ctypes.byref(self.case.c), row, ctypes.byref(self.w))

@@ -294,6 +294,27 @@ class Solver:
         self._check(L.sw2g_set_field_where(self.h, int(which), _ptr(v), m.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))),
                     "sw2g_set_field_where")
 
+    def add_cells(self, which: int, cells, values, scale: float = 1.0):
+        """sw2g_add_cells: field += scale * value on listed interior cells
+        (increasing padded indices), += scale * 0 elsewhere."""
+        L = load()
+        L.sw2g_add_cells.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_double]
+        c = np.ascontiguousarray(cells, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        return L.sw2g_add_cells(self.h, int(which), c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(v),
+                                int(c.size), float(scale))
+
+    def set_cells(self, which: int, cells, values):
+        """sw2g_set_cells: field = value on listed interior cells."""
+        L = load()
+        L.sw2g_set_cells.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+        c = np.ascontiguousarray(cells, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        return L.sw2g_set_cells(self.h, int(which), c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(v),
+                                int(c.size))
+
     def apply_channel(self):
         L = load()
         L.sw2g_apply_channel.argtypes = [ctypes.c_void_p]

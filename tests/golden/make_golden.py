@@ -107,6 +107,15 @@ def _f05(p):
     _f04(p)
 
 
+def _f06(p):
+    # three injections on a 1024 x 512 band for the whole run: a ramped static
+    # one, a moving one across the periodic seam with tracer, one against the
+    # northern wall moving in degrees per second
+    p.gaussians = [[0.0, 40 * p.Dt, 2 * p.Dt, 100.0, 10.0, 0, 0.0, 2.0e13 / p.Dt, 1, 2.0, 6.0, 0.0],
+                   [0.0, 40 * p.Dt, 0.0, 2.0, -20.0, 0, -60.0, 1.5e13 / p.Dt, 1, 1.5, 5.0, 1.0],
+                   [0.0, 40 * p.Dt, 3 * p.Dt, 250.0, 50.0, 1, 0.01, 1.0e13 / p.Dt, 1, 3.0, 9.0, 0.5]]
+
+
 FORCING_CASES = {
     "f01_gauss_static": (dict(nx=48, ny=24, sch=2, seed=31, jet="none", bumps=0, lat0=-60.0, lat1=60.0),
                          60, 20, 10, _f01),
@@ -119,8 +128,12 @@ FORCING_CASES = {
     # kept as the ENERGY lines and SHA-256 digests of the last frame
     "f05_jupiter_example": (dict(nx=50, ny=50, sch=1, seed=34, jet="none", bumps=0, hyper=False, lon0=0.0,
                                  lon1=90.0, lat0=-35.0, lat1=-10.0, Dt=50.0, h0=1000.0), 34560, 864, 100, _f05),
+    # injections every step on a grid large enough for the forcing's cost to
+    # matter; kept as the ENERGY lines and SHA-256 digests of the last frame
+    "f06_gauss_1024": (dict(nx=1024, ny=512, sch=2, seed=36, jet="none", bumps=0, lat0=-60.0, lat1=60.0),
+                       30, 10, 10, _f06),
 }
-HASH_ONLY = {"f05_jupiter_example"}
+HASH_ONLY = {"f05_jupiter_example", "f06_gauss_1024"}
 
 
 def polar_wind_table(amp=30.0, k=6.0):
@@ -287,7 +300,19 @@ def main():
     if not os.path.exists(REF_BIN):
         raise SystemExit("reference not built (sources absent?)")
     only_forcing = "--forcing" in sys.argv  # regenerate the forcing and polar cases only
+    # --only NAME: run the reference on that one forcing case and update its entry
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     manifest = {}
+    if only:
+        with open(os.path.join(OUT, "manifest.json")) as fh:
+            manifest = json.load(fh)
+        CRASH_CASES.clear()
+        CASES.clear()
+        HASH_CASES.clear()
+        POLAR_CASES.clear()
+        for k in list(FORCING_CASES):
+            if k != only:
+                del FORCING_CASES[k]
     if only_forcing:
         with open(os.path.join(OUT, "manifest.json")) as fh:
             manifest = {k: v for k, v in json.load(fh).items() if not v.get("forcing") and not v.get("polar")}
@@ -382,7 +407,7 @@ def main():
     # examples/JupiterEnergyTest run (an older version of the code), which
     # f04_jupiter_box mirrors; kept for its first 1e5 s
     kat = os.path.join(REF_DIR, "examples", "JupiterEnergyTest", "enou.txt")
-    if os.path.exists(kat):
+    if os.path.exists(kat) and not only:
         with open(kat) as fh:
             lines = [ln.split(None, 1)[1].strip() for ln in fh if ln.startswith("ENERGY")]
         manifest["kat_enou"] = {"source": "examples/JupiterEnergyTest/enou.txt",

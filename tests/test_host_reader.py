@@ -146,3 +146,71 @@ def test_vortex_fields(tmp_path):
     assert np.all(np.isfinite(deta)) and np.abs(deta[inner]).max() > 1.0
     assert np.abs(du[inner]).max() > 0 and np.abs(dv[inner]).max() > 0
     assert np.all(deta[0:2] == 0) and np.all(du[:, 0:2] == 0)  # halos untouched (the step wraps them)
+
+
+def _brute_gaussian_mask(c, f, G, Dt, t):
+    """The cells inside the radius by the reference's expression evaluated at
+    every interior cell (perturbs.c:22-364, polar 0), with the per-row and
+    per-column values the C code tabulates."""
+    w = f.w
+    nx, ny = c.c.nx, c.c.ny
+    R = (c.c.rE + c.c.rP) / 2.0
+    pi = 4.0 * math.atan(1.0)
+    deg = lambda a: a * (pi / 180.0)
+    t0 = G[0]
+    lon, lat = deg(G[3]), deg(G[4])
+    rZ = lambda la: c.c.rE / math.sqrt(1.0 + (math.tan(la) * math.tan(la)) / c.c.epsilon2)
+    om = G[6] / rZ(lat) if int(G[5]) == 0 else deg(G[6])
+    lon = lon + om * (t - t0)
+    radius = G[10]
+    if int(G[8]) == 1:
+        radius = radius / 360.0 * 2 * pi * (c.c.rE + c.c.rP) / 2.0
+    while lon < c.c.lon0:
+        lon += (c.c.lon1 - c.c.lon0)
+    while lon > c.c.lon1:
+        lon -= (c.c.lon1 - c.c.lon0)
+    centres = [lon]
+    if (lon + radius / rZ(lat)) >= c.c.lon1:
+        centres.append(lon - (c.c.lon1 - c.c.lon0))
+    if (lon - radius / rZ(lat)) <= c.c.lon0:
+        centres.append(lon + (c.c.lon1 - c.c.lon0))
+    plat = math.atan(1.0 / c.c.epsilon2 * math.tan(lat))
+    mask = np.zeros((ny + 4, nx + 4), np.uint8)
+    for lc in centres:
+        for j in range(1, ny + 1):
+            sj, cj = w.row_sin[j], w.row_cos[j]
+            for i in range(1, nx + 1):
+                x = math.sin(plat) * sj + math.cos(plat) * cj * math.cos(w.col_lonc[i] - lc)
+                r = R * math.acos(x) if -1.0 <= x <= 1.0 else float("nan")
+                if r < radius:
+                    mask[j + 1, i + 1] = 1
+    return mask
+
+
+@pytest.mark.parametrize("lon,lat,sigma,radius", [
+    (100.0, 10.0, 2.0, 5.0),      # interior
+    (1.0, -5.0, 3.0, 8.0),        # across the periodic seam (west)
+    (358.5, 20.0, 3.0, 12.0),     # across the seam (east)
+    (200.0, 55.0, 4.0, 15.0),     # against the northern wall
+    (60.0, 0.0, 20.0, 200.0),     # radius beyond the planet: every cell
+    (33.75, -27.5, 0.5, 1.0),     # small: one cell
+])
+def test_gaussian_skips_only_cells_outside_the_radius(tmp_path, lon, lat, sigma, radius):
+    """The Gaussian evaluation skips cells that cannot lie inside the radius;
+    its cells must be exactly those where the reference's distance, evaluated
+    at every cell, is below the radius, and its list must match its fields."""
+    p = gc.forcing_params("f01_gauss_static")
+    p.gaussians = [[0.0, 20 * p.Dt, 0.0, lon, lat, 0, 0.0, 2.5e13 / p.Dt, 1, sigma, radius, 1.0]]
+    path = tmp_path / "c.sw"
+    formats.write_sw(str(path), p)
+    c = hostlib.Case(str(path))
+    f = hostlib.Forcing(c)
+    for t in (3 * p.Dt, 4 * p.Dt):  # twice: the second call must clear the first's cells
+        rc, rf, pert, tracer, mask, _ = f.gaussian(0, p.Dt, t)
+        assert rc == 0 and rf > 0
+        ref = _brute_gaussian_mask(c, f, p.gaussians[0], p.Dt, t)
+        assert np.array_equal(mask, ref)
+        assert np.all(pert[mask == 0] == 0.0)
+        idx, cp, ct = f.cells()
+        assert np.array_equal(idx, np.sort(np.nonzero(mask.ravel())[0]))
+        assert np.array_equal(cp, pert.ravel()[idx]) and np.array_equal(ct, tracer.ravel()[idx])

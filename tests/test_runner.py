@@ -71,12 +71,20 @@ def test_forcing_cases_match_the_reference(tmp_path, name):
 
 @pytest.mark.parametrize("name", HASHED)
 def test_reference_example_run(tmp_path, name):
-    """The reference's examples/JupiterEnergyTest case, all 34,560 steps:
-    every ENERGY line and the last frame must be the reference's."""
+    """Runs kept as hashes: the reference's examples/JupiterEnergyTest case,
+    all 34,560 steps (every ENERGY line as printed), and a 1024x512 band with
+    three Gaussians injected every step, whose cells inside the radii reach the
+    GPU as lists (ENERGY lines to their printed digits: sums over 0.5 M cells
+    in another order). The last frame must be the reference's bit for bit."""
     entry = gc.manifest()[name]
     formats.write_sw(str(tmp_path / f"{name}.sw"), gc.forcing_params(name))
     energy, frames = run(tmp_path, name)
-    assert energy == entry["energy_printed"]
+    if name == "f05_jupiter_example":
+        assert energy == entry["energy_printed"]
+    else:
+        assert len(energy) == len(entry["energy_printed"])
+        for a, b in zip(energy, entry["energy_printed"]):
+            assert same_energy(a, b), (a, b)
     assert len(frames) == entry["frames"]
     nstep, t, nx, ny, fl = frames[max(frames)]
     assert t == entry["last_frame"]["t"]
