@@ -312,12 +312,46 @@ def parity_fp64(lib, case, nsteps, local):
     return out
 
 
+def forcing_leg(n_short: int, n_long: int):
+    """Per-step time of the case-file runner (sw2g-run: case reader, host
+    forcing, GPU step) on a 1024x512 band with three Gaussians injected in
+    every step (cases.forcing_band), whose cells inside the radii reach the GPU
+    as lists. Two runs of n_short and n_long steps from the same start, each
+    writing only its first and last frame; the difference of their wall times
+    over the difference of steps is the time of a forced step."""
+    import tempfile
+
+    from sw2_gb300 import cases, formats, hostlib
+
+    times = {}
+    with tempfile.TemporaryDirectory() as wd:
+        for n in (n_short, n_long):
+            p = cases.forcing_band(n)
+            name = f"forced{n}"
+            formats.write_sw(os.path.join(wd, name + ".sw"), p)
+            os.makedirs(os.path.join(wd, "out"), exist_ok=True)
+            t0 = time.perf_counter()
+            r = subprocess.run([hostlib.RUNNER, "--quiet", "1", "1", name, "out"], cwd=wd, capture_output=True,
+                               text=True, timeout=600)
+            times[n] = time.perf_counter() - t0
+            if r.returncode != 0:
+                return {"error": r.stderr[-500:]}
+    per_step = (times[n_long] - times[n_short]) / (n_long - n_short)
+    p = cases.forcing_band(n_long)
+    return {"workload": f"{p.nx}x{p.ny} band, 3 Gaussians injected every step (ramped static, moving across "
+                        f"the seam with tracer, against the wall), minmod, nu4, FP64",
+            "ms_per_forced_step": 1e3 * per_step, "cell_updates_per_s": p.nx * p.ny / per_step,
+            "runs_s": {str(k): v for k, v in times.items()},
+            "path": "sw2g-run: host evaluation of the cells inside each radius, sw2g_set_cells + sw2g_add_cells "
+                    "between sw2g_step_open and sw2g_step_close"}
+
+
 def ensemble(lib, nsteps, tune_steps, acc_steps, local, seed=7):
     """The 64-member ensemble on uneven grids (16 x 512x256, 24 x 1024x512,
     24 x 2048x1024; Van Leer, FP32 form) stepped as one batch: one launch per
-    phase over all members, one-step CUDA graph replays, sweep schedule chosen
-    by the tuner. Worst-member h error against the FP64 step is measured on one
-    member of each grid size."""
+    phase over all members, one-step CUDA graph replays, tile shape and sweep
+    schedule chosen by the tuner. Worst-member h error against the FP64 step
+    over all members."""
     from sw2_gb300 import cases
 
     specs = cases.ensemble_members(seed)
@@ -339,7 +373,8 @@ def ensemble(lib, nsteps, tune_steps, acc_steps, local, seed=7):
     out = {"members": len(cs), "grids": "16 x 512x256, 24 x 1024x512, 24 x 2048x1024",
            "cells_per_step": cells, "steps": nsteps, "value": cells * nsteps / (ms * 1e-3), "unit": UNIT,
            "ms_per_step": ms / nsteps, "launches_per_step": b.last_launches() / nsteps,
-           "schedule": b.schedule(), "tune_ms_per_step": tune, "limiter": "Van Leer (r <= 0 -> 0)"}
+           "schedule": f"32x{b.tile_rows()}/{b.schedule()}", "tune_ms_per_step": tune,
+           "tune_spread": max(tune.values()) / min(tune.values()), "limiter": "Van Leer (r <= 0 -> 0)"}
     b.close()
     if acc_steps > 0:
         # every member from its initial state, acc_steps steps as one batch,
@@ -385,6 +420,8 @@ def main():
                     help="steps of the FP64 step against the oracle on the headline workload (0 skips)")
     ap.add_argument("--large-config", default="band8192", help="workload of the large case run in both forms")
     ap.add_argument("--large-steps", type=int, default=1000, help="steps of the large case (0 skips it)")
+    ap.add_argument("--no-forcing", dest="forcing", action="store_false",
+                    help="skip the per-step time of the forced 1024x512 case through the case-file runner")
     ap.add_argument("--cpu-steps", type=int, default=None, help="oracle steps for the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
@@ -473,6 +510,7 @@ def main():
         accl["workload"] = args.large_config
         large = (cl.params.nx * cl.params.ny, descl, ml64, ml32, accl)
         del cl
+    forced = forcing_leg(20, 220) if args.forcing and rank == 0 else None
     # the FP64 step against the oracle at the drop-in configuration's length
     par = None
     if args.parity_steps > 0 and rank == 0:
@@ -548,6 +586,7 @@ def main():
         "fp32_over_fp64_large": m32b["value"] / m64b["value"],
         "accuracy_fp32_vs_fp64": acc,
         "parity_fp64_vs_oracle": par,
+        "forcing_runner": forced,
         "ensemble_fp32_batched": ens,
         "fp32_batched_over_fp64": (ens["value"] / m64["value"]) if ens else None,
     }

@@ -258,14 +258,22 @@ int sw2g_batch_error_step(const sw2g_batch *b);
 double sw2g_batch_last_step_ms(const sw2g_batch *b);
 long long sw2g_batch_last_launches(const sw2g_batch *b);
 
-/* Sweep-schedule autotuner. The order in which the tiles of all members are
- * assigned to blocks changes no result, so candidates are timed on the live
- * run: each of the SW2G_SCHEDULES orders advances the batch
- * steps_per_candidate steps (ms_per_step[s] receives its time per step, may
- * be NULL), and the fastest is kept. */
+/* Autotuner of the batch's launch shape. Neither the tile shape (32 cells
+ * wide, 4, 8 or 16 rows high: SW2G_TILE_SHAPES shapes) nor the order in which
+ * the tiles of all members are assigned to blocks (SW2G_SCHEDULES orders:
+ * rows, columns, members interleaved, bands of 8 tile columns) changes any
+ * result, so the candidates are timed on the live run: each of the
+ * SW2G_TILE_SHAPES x SW2G_SCHEDULES pairs advances the batch
+ * steps_per_candidate steps (after one untimed step per shape, which captures
+ * its graph); ms_per_step[shape * SW2G_SCHEDULES + schedule] receives its time
+ * per step (may be NULL), and the fastest pair is kept.
+ * sw2g_batch_set_schedule picks a pair by hand (tile_rows 4, 8 or 16). */
 #define SW2G_SCHEDULES 4
+#define SW2G_TILE_SHAPES 3
 sw2g_status sw2g_batch_tune(sw2g_batch *b, int steps_per_candidate, double *ms_per_step);
+sw2g_status sw2g_batch_set_schedule(sw2g_batch *b, int tile_rows, int schedule);
 int sw2g_batch_schedule(const sw2g_batch *b);
+int sw2g_batch_tile_rows(const sw2g_batch *b);
 void sw2g_batch_destroy(sw2g_batch *b);
 
 /* Self-check of the FP64 step's division by a row metric factor (it uses

@@ -382,3 +382,19 @@ def ensemble_members(seed: int = 7):
         out.append((nx, ny, dict(planet="jupiter", jet="cos6", sch=3, nsteps=1000, bumps=1,
                                  amp=(0.01, 0.08), sigma_km=(1000.0, 3000.0), seed=seed * 1000 + m)))
     return out
+
+
+def forcing_band(nsteps: int = 30, nx: int = 1024, ny: int = 512) -> CaseParams:
+    """A band with Gaussian mass injections in every step (add_Gaussians,
+    perturbs.c:22-195), run from the reference's own initial state (LoadFrom
+    0: zero fields, forcing at t0): a ramped static injection, a moving one
+    across the periodic seam that injects tracer, and one against the northern
+    wall moving in degrees per second; sizes in degrees. Table rows are the
+    reference's 12 Gaussian columns (t0, t1, tau, lon, lat, isdegvel, vel, Q,
+    isdegsize, sigma, radius, inject_tracer)."""
+    p = make_case(nx, ny, sch=2, seed=36, jet="none", bumps=0, lat0=-60.0, lat1=60.0, nsteps=nsteps).params
+    p.nsteps, p.SaveEvery, p.IteInfo, p.LoadFrom = nsteps, nsteps, nsteps, 0
+    p.gaussians = [[0.0, 40 * p.Dt, 2 * p.Dt, 100.0, 10.0, 0, 0.0, 2.0e13 / p.Dt, 1, 2.0, 6.0, 0.0],
+                   [0.0, 40 * p.Dt, 0.0, 2.0, -20.0, 0, -60.0, 1.5e13 / p.Dt, 1, 1.5, 5.0, 1.0],
+                   [0.0, 40 * p.Dt, 3 * p.Dt, 250.0, 50.0, 1, 0.01, 1.0e13 / p.Dt, 1, 3.0, 9.0, 0.5]]
+    return p

@@ -21,6 +21,7 @@ constexpr int kChunk = kCheckSlots;  // steps per check read-back
 struct BatchExec {
   int4* d_tiles = nullptr;
   int ntiles = 0, nbx = 0, nby = 0;  // nbx x nby: the grid of a single member
+  int th = kTileRowsSolo;            // tile height of the kernels
   int* d_counter = nullptr;
   int n_dev = 0;                     // device counter: steps since cap was taken
   std::vector<MemberDesc> cap;
@@ -59,6 +60,17 @@ struct BatchExec {
     n_dev = 0;
     return cudaMemsetAsync(d_counter, 0, sizeof(int), st);
   }
+  // Another tile shape: the captured graph (its grid size and kernels) no longer applies.
+  void set_shape(int tile_rows, int n_tiles, int nbx1, int nby1) {
+    if (tile_rows != th || n_tiles != ntiles) {
+      if (exec) cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+    th = tile_rows;
+    ntiles = n_tiles;
+    nbx = nbx1;
+    nby = nby1;
+  }
   // Check slot of the next step, and the steps left before the slots wrap.
   int slot() const { return n_dev & (kCheckSlots - 1); }
   int room() const { return kCheckSlots - slot(); }
@@ -68,7 +80,7 @@ struct BatchExec {
     const int M = (int)cap.size();
     if (tm && tm->on) {
       for (int s = 0; s < n; s++)
-        launches += fp32_batch_step(sch, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, tm);
+        launches += fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, tm);
       n_dev += n;
       return cudaGetLastError();
     }
@@ -76,7 +88,7 @@ struct BatchExec {
       cudaGraph_t g = nullptr;
       cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
-      fp32_batch_step(sch, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, nullptr);
+      fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, nullptr);
       e = cudaStreamEndCapture(st, &g);
       if (e != cudaSuccess) return e;
       e = cudaGraphInstantiate(&exec, g, 0);
@@ -585,7 +597,7 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     c32.wx = x->d_aux32[0];
     c32.wy = x->d_aux32[1];
     c32.hb = x->d_aux32[2];
-    fp32_tiles(c->nx, c->ny, &x->run32.nbx, &x->run32.nby);
+    fp32_tiles(c->nx, c->ny, x->run32.th, &x->run32.nbx, &x->run32.nby);
     if ((st = cuda_fail(x->run32.alloc(0), "batch")) != SW2G_OK) return fail(st);
     x->run32.sch = c32.sch;
   }
@@ -1331,8 +1343,9 @@ struct sw2g_batch {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   BatchExec run;
-  std::vector<int2> nb;
+  std::vector<int2> dims;  // members' nx, ny
   int sched = SCHED_ROWS;
+  int th = kTileRowsSolo;
   double last_ms = 0;
   long long last_launches = 0;
   int err_member = -1, err_step = -1;
@@ -1340,10 +1353,22 @@ struct sw2g_batch {
 
 namespace {
 
-sw2g_status batch_set_schedule(sw2g_batch* b, int sched) {
-  const std::vector<int4> t = tile_table(b->nb, sched);
+// Tile shape th rows high and sweep schedule sched: the tile table of the
+// members' tiles in that order (the device table holds room for the
+// smallest tiles).
+sw2g_status batch_set_schedule(sw2g_batch* b, int th, int sched) {
+  std::vector<int2> nb;
+  for (const int2 d : b->dims) {
+    int nbx = 0, nby = 0;
+    fp32_tiles(d.x, d.y, th, &nbx, &nby);
+    nb.push_back(make_int2(nbx, nby));
+  }
+  const std::vector<int4> t = tile_table(nb, sched);
+  CK(cudaStreamSynchronize(b->stream));  // no queued step reads the table being replaced
   CK(cudaMemcpy(b->run.d_tiles, t.data(), t.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  b->run.set_shape(th, (int)t.size(), nb[0].x, nb[0].y);
   b->sched = sched;
+  b->th = th;
   return SW2G_OK;
 }
 
@@ -1376,18 +1401,16 @@ sw2g_status sw2g_batch_create(sw2g_ctx* const* members, int n, sw2g_batch** out)
     return fail(st);
   for (int e = 0; e < 2; e++)
     if ((st = cuda_fail(cudaEventCreate(&b->ev[e]), "event")) != SW2G_OK) return fail(st);
-  int ntiles = 0;
+  int ntiles = 0;  // for the smallest tiles, the most of them
   for (sw2g_ctx* x : b->mem) {
     int nbx = 0, nby = 0;
-    fp32_tiles(x->c32.nx, x->c32.ny, &nbx, &nby);
-    b->nb.push_back(make_int2(nbx, nby));
+    fp32_tiles(x->c32.nx, x->c32.ny, kTileRows[0], &nbx, &nby);
+    b->dims.push_back(make_int2(x->c32.nx, x->c32.ny));
     ntiles += nbx * nby;
   }
   if ((st = cuda_fail(b->run.alloc(ntiles), "batch")) != SW2G_OK) return fail(st);
   b->run.sch = members[0]->c32.sch;
-  b->run.nbx = b->nb[0].x;
-  b->run.nby = b->nb[0].y;
-  if ((st = batch_set_schedule(b, SCHED_ROWS)) != SW2G_OK) return fail(st);
+  if ((st = batch_set_schedule(b, kTileRowsSolo, SCHED_ROWS)) != SW2G_OK) return fail(st);
   *out = b;
   return SW2G_OK;
 }
@@ -1461,24 +1484,40 @@ sw2g_status sw2g_batch_step(sw2g_batch* b, int nsteps) {
 
 sw2g_status sw2g_batch_tune(sw2g_batch* b, int steps_per_candidate, double* ms_per_step) {
   if (!b || steps_per_candidate < 1) return SW2G_ERR_BAD_ARG;
+  static_assert(SW2G_TILE_SHAPES == kTileShapes && SW2G_SCHEDULES == SCHED_COUNT, "candidates of the header");
   double best = 0;
-  int best_s = SCHED_ROWS;
-  for (int s = 0; s < SCHED_COUNT; s++) {
-    sw2g_status st = batch_set_schedule(b, s);
-    if (st != SW2G_OK) return st;
-    st = sw2g_batch_step(b, steps_per_candidate);
-    if (st != SW2G_OK) return st;
-    const double ms = b->last_ms / steps_per_candidate;
-    if (ms_per_step) ms_per_step[s] = ms;
-    if (s == 0 || ms < best) {
-      best = ms;
-      best_s = s;
+  int best_th = kTileRowsSolo, best_s = SCHED_ROWS;
+  for (int shape = 0; shape < kTileShapes; shape++) {
+    for (int s = 0; s < SCHED_COUNT; s++) {
+      sw2g_status st = batch_set_schedule(b, kTileRows[shape], s);
+      if (st != SW2G_OK) return st;
+      // the first steps of a shape capture its graph: one untimed step first
+      if (s == 0 && (st = sw2g_batch_step(b, 1)) != SW2G_OK) return st;
+      st = sw2g_batch_step(b, steps_per_candidate);
+      if (st != SW2G_OK) return st;
+      const double ms = b->last_ms / steps_per_candidate;
+      if (ms_per_step) ms_per_step[shape * SCHED_COUNT + s] = ms;
+      if ((shape == 0 && s == 0) || ms < best) {
+        best = ms;
+        best_th = kTileRows[shape];
+        best_s = s;
+      }
     }
   }
-  return batch_set_schedule(b, best_s);
+  return batch_set_schedule(b, best_th, best_s);
+}
+
+sw2g_status sw2g_batch_set_schedule(sw2g_batch* b, int tile_rows, int schedule) {
+  if (!b || schedule < 0 || schedule >= SCHED_COUNT) return SW2G_ERR_BAD_ARG;
+  bool known = false;
+  for (int k = 0; k < kTileShapes; k++) known = known || (kTileRows[k] == tile_rows);
+  if (!known) return SW2G_ERR_BAD_ARG;
+  CK(cudaSetDevice(b->device));
+  return batch_set_schedule(b, tile_rows, schedule);
 }
 
 int sw2g_batch_schedule(const sw2g_batch* b) { return b ? b->sched : -1; }
+int sw2g_batch_tile_rows(const sw2g_batch* b) { return b ? b->th : -1; }
 int sw2g_batch_error_member(const sw2g_batch* b) { return b ? b->err_member : -1; }
 int sw2g_batch_error_step(const sw2g_batch* b) { return b ? b->err_step : -1; }
 double sw2g_batch_last_step_ms(const sw2g_batch* b) { return b ? b->last_ms : 0.0; }

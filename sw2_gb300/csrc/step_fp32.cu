@@ -31,8 +31,14 @@
 namespace sw2g {
 namespace f32 {
 
-constexpr int TW = 32, TH = 8, NT = TW * TH;
+// Tiles are TW = 32 cells wide (a warp per tile row) and TH rows high, TH a
+// template parameter in {4, 8, 16} (the tile shapes the batch tuner picks
+// from); a block has one thread per tile cell.
+constexpr int TW = 32;
 constexpr int NONE = INT_MIN;
+static_assert(kTileRowsMax == 16, "the FP32 layout pads rows for tiles up to 16 rows high");
+template <int TH>
+__host__ __device__ constexpr int nthreads() { return TW * TH; }
 
 __device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1) * W; }
 
@@ -47,14 +53,16 @@ struct KP {
 
 // Per-row constants of the rows a block touches (j0-2 .. j0+TH+2), staged in
 // shared memory once per block from the row-major table p.q[(j+1)*Q_NUM + t].
-typedef float RowCache[TH + 5][Q_NUM];
+template <int TH>
+using RowCache = float[TH + 5][Q_NUM];
 struct Rows {
   const float (*r)[Q_NUM];
   int j0;
 };
 __device__ __forceinline__ float Q(const Rows& c, int t, int j) { return c.r[j - c.j0 + 2][t]; }
-__device__ __forceinline__ void fill_rows(const KP& p, int j0, RowCache& sq) {
-  for (int t = threadIdx.x; t < (TH + 5) * Q_NUM; t += TW * TH) {
+template <int TH>
+__device__ __forceinline__ void fill_rows(const KP& p, int j0, RowCache<TH>& sq) {
+  for (int t = threadIdx.x; t < (TH + 5) * Q_NUM; t += nthreads<TH>()) {
     const int r = t / Q_NUM, c = t - r * Q_NUM;
     const int row = min(j0 - 2 + r, p.ny + 2);
     sq[r][c] = p.q[(size_t)(row + 1) * Q_NUM + c];
@@ -225,15 +233,17 @@ __device__ __forceinline__ void put(T* f, int W, int nx, int ny, int i, int j, T
 // padding rows and columns that the ring-2 window of any tile is in bounds.
 // The window [i0-2, i0+TW+1] x [j0-2, j0+TH+1] starts on a 16-byte boundary
 // (padded column i0-1 = TW*bx), so it is read with 16-byte loads.
-typedef float Tile[TH + 4][TW + 4];
+template <int TH>
+using Tile = float[TH + 4][TW + 4];
 
 __device__ __forceinline__ int IX32(int P, int i, int j) { return (i + 1) + (j + 1) * P; }
 
 // Window loads by the threads: 16-byte loads of each row, spread over the block.
-__device__ __forceinline__ void load_tile(const float* __restrict__ f, int P, int i0, int j0, Tile& t) {
+template <int TH>
+__device__ __forceinline__ void load_tile(const float* __restrict__ f, int P, int i0, int j0, Tile<TH>& t) {
   constexpr int C4 = (TW + 4) / 4;
   const float* base = f + (size_t)(j0 - 1) * P + (i0 - 1);
-  for (int q = threadIdx.x; q < (TH + 4) * C4; q += NT) {
+  for (int q = threadIdx.x; q < (TH + 4) * C4; q += nthreads<TH>()) {
     const int r = q / C4, c = q - r * C4;
     const float4 v = __ldg(reinterpret_cast<const float4*>(base + (size_t)r * P) + c);
     *reinterpret_cast<float4*>(&t[r][4 * c]) = v;
@@ -249,7 +259,7 @@ __device__ __forceinline__ void load_tile(const float* __restrict__ f, int P, in
 // barrier's first phase with an iteration limit. A wait that runs out sets
 // CHECK_TIMEOUT in the step's check word (SW2G_ERR_TIMEOUT on the host) and
 // the whole block returns without computing.
-constexpr int TILE_ROWS = TH + 4, TILE_ROW_BYTES = (TW + 4) * 4;
+constexpr int TILE_ROW_BYTES = (TW + 4) * 4;
 // Each wait suspends the thread for at most TILE_WAIT_HINT_NS, so the limit
 // bounds a wait to about 1.3 s.
 constexpr int TILE_WAIT_LIMIT = 1 << 16;
@@ -269,8 +279,9 @@ __device__ __forceinline__ void tiles_init(unsigned long long* bar, int copies) 
 }
 
 // Row r of the window of field f (pitch P) at tile (i0, j0) into t[r].
-__device__ __forceinline__ void tile_row_copy(unsigned long long* bar, const float* f, int P, int i0, int j0, Tile& t,
-                                              int r) {
+template <int TH>
+__device__ __forceinline__ void tile_row_copy(unsigned long long* bar, const float* f, int P, int i0, int j0,
+                                              Tile<TH>& t, int r) {
   const float* src = f + (size_t)(j0 - 1 + r) * P + (i0 - 1);
   unsigned long long g;
   asm("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(src));
@@ -315,11 +326,12 @@ __device__ __forceinline__ bool tiles_wait(unsigned long long* bar, int* bad, in
 // following laplacian.c:59-81: ZE(i,0) = 0 and DI(i,ny+1) fixed at the walls;
 // ZE(0,j) and DI(nx+1,j) are the wrapped values ZE(nx,j) and DI(1,j),
 // evaluated at their source column from the global arrays gU, gV.
-__device__ __forceinline__ void zeta_div(const KP& p, const Rows& rc, int i0, int j0, const Tile& su, const Tile& sv,
-                                         const float* gU, const float* gV, float (*ze)[TW + 1],
+template <int TH>
+__device__ __forceinline__ void zeta_div(const KP& p, const Rows& rc, int i0, int j0, const Tile<TH>& su,
+                                         const Tile<TH>& sv, const float* gU, const float* gV, float (*ze)[TW + 1],
                                          float (*di)[TW + 1]) {
   const int P = p.P, nx = p.nx, ny = p.ny;
-  for (int t = threadIdx.x; t < (TW + 1) * (TH + 1); t += NT) {
+  for (int t = threadIdx.x; t < (TW + 1) * (TH + 1); t += nthreads<TH>()) {
     const int a = t % (TW + 1), b = t / (TW + 1);
     {  // ZE at (i, j) = (i0 - 1 + a, j0 - 1 + b)
       const int i = i0 - 1 + a, j = j0 - 1 + b;
@@ -364,18 +376,19 @@ __device__ __forceinline__ void lap_out(const Rows& rc, int j, int a, int b, con
 }
 
 // ------------------------------------------------------------------ kernels
+template <int TH>
 __device__ __forceinline__ void d_lap1(const KP& p, int bx, int by, const float* __restrict__ u,
                                        const float* __restrict__ v, float* Lu, float* Lv) {
-  __shared__ __align__(16) Tile su, sv;
+  __shared__ __align__(16) Tile<TH> su, sv;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
-  __shared__ RowCache sq;
+  __shared__ RowCache<TH> sq;
   const int i0 = bx * TW + 1, j0 = by * TH + 1;
-  fill_rows(p, j0, sq);
+  fill_rows<TH>(p, j0, sq);
   const Rows rc{sq, j0};
-  load_tile(u, p.P, i0, j0, su);
-  load_tile(v, p.P, i0, j0, sv);
+  load_tile<TH>(u, p.P, i0, j0, su);
+  load_tile<TH>(v, p.P, i0, j0, sv);
   __syncthreads();
-  zeta_div(p, rc, i0, j0, su, sv, u, v, ze, di);
+  zeta_div<TH>(p, rc, i0, j0, su, sv, u, v, ze, di);
   __syncthreads();
   const int a = threadIdx.x % TW, b = threadIdx.x / TW;
   const int i = i0 + a, j = j0 + b;
@@ -402,41 +415,43 @@ struct Main1Io {
 // row B; global (i0-2+A, j0-2+B)). An x face lies west of column A and is
 // shared whole by its two cells (their Courant numbers use the same row
 // metric); a y face lies north of row B and shares its limited slopes.
-template <int SCH>
-__device__ __forceinline__ float mass_xface(const Tile& se, const Tile& su, float kx, int A, int B) {
+template <int SCH, int TH>
+__device__ __forceinline__ float mass_xface(const Tile<TH>& se, const Tile<TH>& su, float kx, int A, int B) {
   return face1<SCH>(se[B][A - 2], se[B][A - 1], se[B][A], se[B][A + 1], su[B][A - 1] * kx);
 }
-template <int SCH>
-__device__ __forceinline__ float u_xface(const Tile& su, float kc, int A, int B) {
+template <int SCH, int TH>
+__device__ __forceinline__ float u_xface(const Tile<TH>& su, float kc, int A, int B) {
   const float uw = su[B][A - 1], ue = su[B][A];
   return face2<SCH>(su[B][A - 2], uw, ue, su[B][A + 1], cpos2(uw, ue, kc), cneg2(uw, ue, kc));
 }
-template <int SCH>
-__device__ __forceinline__ float v_xface(const Tile& sv, const Tile& su, float kxv, int A, int B) {
+template <int SCH, int TH>
+__device__ __forceinline__ float v_xface(const Tile<TH>& sv, const Tile<TH>& su, float kxv, int A, int B) {
   const float u1 = su[B + 1][A - 1], u0 = su[B][A - 1];
   return face2<SCH>(sv[B][A - 2], sv[B][A - 1], sv[B][A], sv[B][A + 1], cpos2(u1, u0, kxv), cneg2(u1, u0, kxv));
 }
 // Heights relative to the reference of row B (global row j).
-template <int SCH>
-__device__ __forceinline__ float2 mass_yface(const Tile& se, const Tile& sv, const Rows& rc, int A, int B, int j) {
+template <int SCH, int TH>
+__device__ __forceinline__ float2 mass_yface(const Tile<TH>& se, const Tile<TH>& sv, const Rows& rc, int A, int B,
+                                             int j) {
   return face1_shared<SCH>(se[B - 1][A] + Q(rc, Q_DHBM1, j), se[B][A], se[B + 1][A] + Q(rc, Q_DHBP1, j),
                            se[B + 2][A] + Q(rc, Q_DHBP2, j), sv[B][A] > 0.f);
 }
-template <int SCH>
-__device__ __forceinline__ float2 mom_yface(const Tile& t, int A, int B) {
+template <int SCH, int TH>
+__device__ __forceinline__ float2 mom_yface(const Tile<TH>& t, int A, int B) {
   return face2_shared<SCH>(t[B - 1][A], t[B][A], t[B + 1][A], t[B + 2][A]);
 }
 
-template <int SCH>
+template <int SCH, int TH>
 __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1Io& o) {
-  __shared__ __align__(16) Tile se, su, sv, sl, sm;
+  constexpr int NT = nthreads<TH>();
+  __shared__ __align__(16) Tile<TH> se, su, sv, sl, sm;
   __shared__ float ze[TH + 1][TW + 1], di[TH + 1][TW + 1];
   // x faces [b][a]: west of tile column a (a = 0..TW); y faces [b][a]: south of
   // tile row b (b = 0..TH)
   __shared__ float xm[TH][TW + 1], xu[TH][TW + 1], xv[TH][TW + 1];
   __shared__ float2 ym[TH + 1][TW], yu[TH + 1][TW], yv[TH + 1][TW];
   __shared__ float red[2][NT / 32];
-  __shared__ RowCache sq;
+  __shared__ RowCache<TH> sq;
   const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
   const int i0 = bx * TW + 1, j0 = by * TH + 1;
   // this thread's own cell: issue its global loads before the tile traffic
@@ -448,13 +463,13 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
   const double eta_old = o.eta[q];
   const float h1v = (p.k >= 1) ? o.h1[q32] : 0.f, h2v = (p.k >= 2) ? o.h2[q32] : 0.f;
   const float e_raw = p.extra ? o.es[q32] : 0.f;  // eta without the bottom, for the damping
-  fill_rows(p, j0, sq);
+  fill_rows<TH>(p, j0, sq);
   const Rows rc{sq, j0};
-  load_tile(o.es, P, i0, j0, se);
-  load_tile(o.us, P, i0, j0, su);
-  load_tile(o.vs, P, i0, j0, sv);
-  load_tile(o.Lu, P, i0, j0, sl);
-  load_tile(o.Lv, P, i0, j0, sm);
+  load_tile<TH>(o.es, P, i0, j0, se);
+  load_tile<TH>(o.us, P, i0, j0, su);
+  load_tile<TH>(o.vs, P, i0, j0, sv);
+  load_tile<TH>(o.Lu, P, i0, j0, sl);
+  load_tile<TH>(o.Lv, P, i0, j0, sm);
   __syncthreads();
   if (p.extra) {  // UWINDX, VWINDY (sw.h:216-217) and H = eta + depth - hB (sw.h:213)
     for (int t = threadIdx.x; t < (TH + 4) * (TW + 4); t += NT) {
@@ -466,25 +481,26 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
     }
     __syncthreads();
   }
-  zeta_div(p, rc, i0, j0, sl, sm, o.Lu, o.Lv, ze, di);
+  zeta_div<TH>(p, rc, i0, j0, sl, sm, o.Lu, o.Lv, ze, di);
   {  // faces: each thread the x faces west of its cell and the y faces north of it
-    xm[tb][ta] = mass_xface<SCH>(se, su, Q(rc, Q_KXE, j), a, b);
-    xu[tb][ta] = u_xface<SCH>(su, Q(rc, Q_KXC, j), a, b);
-    xv[tb][ta] = v_xface<SCH>(sv, su, Q(rc, Q_KXV, j), a, b);
-    ym[tb + 1][ta] = mass_yface<SCH>(se, sv, rc, a, b, j);
-    yu[tb + 1][ta] = mom_yface<SCH>(su, a, b);
-    yv[tb + 1][ta] = mom_yface<SCH>(sv, a, b);
-    // and the tile's south row and east column of faces, on the last warps
-    // (the first ones carry the extra items of zeta_div)
-    const int w = tb, l = ta;
-    if (w == TH - 4) ym[0][l] = mass_yface<SCH>(se, sv, rc, l + 2, 1, j0 - 1);
-    else if (w == TH - 3) yu[0][l] = mom_yface<SCH>(su, l + 2, 1);
-    else if (w == TH - 2) yv[0][l] = mom_yface<SCH>(sv, l + 2, 1);
-    else if (w == TH - 1 && l < 3 * TH) {
-      const int r = l % TH, B = r + 2, jr = j0 + r;
-      if (l < TH) xm[r][TW] = mass_xface<SCH>(se, su, Q(rc, Q_KXE, jr), TW + 2, B);
-      else if (l < 2 * TH) xu[r][TW] = u_xface<SCH>(su, Q(rc, Q_KXC, jr), TW + 2, B);
-      else xv[r][TW] = v_xface<SCH>(sv, su, Q(rc, Q_KXV, jr), TW + 2, B);
+    xm[tb][ta] = mass_xface<SCH, TH>(se, su, Q(rc, Q_KXE, j), a, b);
+    xu[tb][ta] = u_xface<SCH, TH>(su, Q(rc, Q_KXC, j), a, b);
+    xv[tb][ta] = v_xface<SCH, TH>(sv, su, Q(rc, Q_KXV, j), a, b);
+    ym[tb + 1][ta] = mass_yface<SCH, TH>(se, sv, rc, a, b, j);
+    yu[tb + 1][ta] = mom_yface<SCH, TH>(su, a, b);
+    yv[tb + 1][ta] = mom_yface<SCH, TH>(sv, a, b);
+    // and the tile's south row (3 x TW faces) and east column (3 x TH) of
+    // faces, counted from the last warp backwards (the first warps carry the
+    // extra items of zeta_div); the south-row items fill whole warps
+    const int e = (NT / 32 - 1 - tb) * 32 + ta;
+    if (e < TW) ym[0][e] = mass_yface<SCH, TH>(se, sv, rc, e + 2, 1, j0 - 1);
+    else if (e < 2 * TW) yu[0][e - TW] = mom_yface<SCH, TH>(su, e - TW + 2, 1);
+    else if (e < 3 * TW) yv[0][e - 2 * TW] = mom_yface<SCH, TH>(sv, e - 2 * TW + 2, 1);
+    else if (e < 3 * TW + 3 * TH) {
+      const int l = e - 3 * TW, r = l % TH, B = r + 2, jr = j0 + r;
+      if (l < TH) xm[r][TW] = mass_xface<SCH, TH>(se, su, Q(rc, Q_KXE, jr), TW + 2, B);
+      else if (l < 2 * TH) xu[r][TW] = u_xface<SCH, TH>(su, Q(rc, Q_KXC, jr), TW + 2, B);
+      else xv[r][TW] = v_xface<SCH, TH>(sv, su, Q(rc, Q_KXV, jr), TW + 2, B);
     }
   }
   __syncthreads();
@@ -574,10 +590,12 @@ struct Main2Io {
 };
 
 // Pressure (calc.c:500-540), AB, Coriolis u then v (calc.c:542-598).
+template <int TH>
 __device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2Io& io, int tile_test) {
-  __shared__ __align__(16) Tile se, su, sv;  // ring-2 windows, ring 1 used
+  constexpr int NT = nthreads<TH>(), TILE_ROWS = TH + 4;
+  __shared__ __align__(16) Tile<TH> se, su, sv;  // ring-2 windows, ring 1 used
   __shared__ float un[TH + 1][TW + 1];       // new u at (i0-1+a, j0+b)
-  __shared__ RowCache sq;
+  __shared__ RowCache<TH> sq;
   const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
   const int i0 = bx * TW + 1, j0 = by * TH + 1;
   // own cell of the v update: issue its global loads first
@@ -591,6 +609,7 @@ __device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2
   // the (at most two) positions of the new-u region this thread updates:
   // their global operands are loaded now as well
   constexpr int NU = (TW + 1) * (TH + 1);
+  static_assert(2 * NT >= NU, "two items of the new-u region per thread");
   float pre_dup[2], pre_h1[2], pre_h2[2];
   double pre_u[2];
 #pragma unroll
@@ -607,14 +626,15 @@ __device__ __forceinline__ void d_main2(const KP& p, int bx, int by, const Main2
     pre_u[s2] = own ? io.u[IX(W, i, j)] : 0.0;
   }
   __shared__ __align__(8) unsigned long long tbar;
+  static_assert(3 * TILE_ROWS <= NT, "one thread per row copy");
   tiles_init(&tbar, 3 * TILE_ROWS);
   if (threadIdx.x < 3 * TILE_ROWS) {  // Coriolis uses U and V without the winds
     const int t = threadIdx.x / TILE_ROWS, r = threadIdx.x - t * TILE_ROWS;
-    if (t == 0) tile_row_copy(&tbar, io.es, P, i0, j0, se, r);
-    else if (t == 1) tile_row_copy(&tbar, io.us, P, i0, j0, su, r);
-    else tile_row_copy(&tbar, io.vs, P, i0, j0, sv, r);
+    if (t == 0) tile_row_copy<TH>(&tbar, io.es, P, i0, j0, se, r);
+    else if (t == 1) tile_row_copy<TH>(&tbar, io.us, P, i0, j0, su, r);
+    else tile_row_copy<TH>(&tbar, io.vs, P, i0, j0, sv, r);
   }
-  fill_rows(p, j0, sq);
+  fill_rows<TH>(p, j0, sq);
   const Rows rc{sq, j0};
   if (!tiles_wait(&tbar, io.bad, tile_test)) return;
   // new u on [i0-1, i0+TW-1] x [j0, j0+TH]: interior cells recomputed, the
@@ -731,19 +751,19 @@ __device__ __forceinline__ int4 tile_of(const int4* __restrict__ tiles) {
 // Resident blocks per SM the register allocation must allow (measured:
 // kb_lap1 at 8 and kb_main2 at 6 are 9-15 % faster than at their natural 6
 // and 5; kb_main1 gains nothing beyond 6).
-template <int N>
-__global__ void __launch_bounds__(NT, 8) kb_lap1(const __grid_constant__ DescSet<N> ds,
-                                              const int4* __restrict__ tiles, const int* __restrict__ counter) {
+template <int TH, int N>
+__global__ void __launch_bounds__(nthreads<TH>(), 2048 / nthreads<TH>())
+    kb_lap1(const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, const int* __restrict__ counter) {
   const int4 t = tile_of<N>(tiles);
   const int n = *counter;
   const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
   const View v = view_of(d, n);
-  d_lap1(kp_of(d, v.k), t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
+  d_lap1<TH>(kp_of(d, v.k), t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
 }
 
-template <int SCH, int N>
-__global__ void __launch_bounds__(NT) kb_main1(const __grid_constant__ DescSet<N> ds,
-                                               const int4* __restrict__ tiles, const int* __restrict__ counter) {
+template <int SCH, int TH, int N>
+__global__ void __launch_bounds__(nthreads<TH>())
+    kb_main1(const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, const int* __restrict__ counter) {
   const int4 t = tile_of<N>(tiles);
   const int n = *counter;
   const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
@@ -751,12 +771,12 @@ __global__ void __launch_bounds__(NT) kb_main1(const __grid_constant__ DescSet<N
   const Main1Io o{d.eta[v.cur], d.es[v.cur], d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv, d.heta[v.h1], d.heta[v.h2],
                   d.eta[1 - v.cur], d.es[1 - v.cur], d.heta[v.w], d.dup, d.dvp, d.cfl + 2 * v.slot,
                   d.bad + v.slot};
-  d_main1<SCH>(kp_of(d, v.k), t.y, t.z, o);
+  d_main1<SCH, TH>(kp_of(d, v.k), t.y, t.z, o);
 }
 
-template <int N>
-__global__ void __launch_bounds__(NT, 6) kb_main2(const __grid_constant__ DescSet<N> ds,
-                                               const int4* __restrict__ tiles, const int* __restrict__ counter) {
+template <int TH, int N>
+__global__ void __launch_bounds__(nthreads<TH>(), 1536 / nthreads<TH>())
+    kb_main2(const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, const int* __restrict__ counter) {
   const int4 t = tile_of<N>(tiles);
   const int n = *counter;
   const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
@@ -764,7 +784,7 @@ __global__ void __launch_bounds__(NT, 6) kb_main2(const __grid_constant__ DescSe
   const Main2Io io{d.es[1 - v.cur], d.u[v.cur], d.v[v.cur], d.us[v.cur], d.vs[v.cur], d.u[1 - v.cur],
                    d.v[1 - v.cur], d.us[1 - v.cur], d.vs[1 - v.cur], d.dup, d.dvp, d.hu[v.h1], d.hu[v.h2],
                    d.hv[v.h1], d.hv[v.h2], d.hu[v.w], d.hv[v.w], d.bad + v.slot};
-  d_main2(kp_of(d, v.k), t.y, t.z, io, d.tile_test);
+  d_main2<TH>(kp_of(d, v.k), t.y, t.z, io, d.tile_test);
 }
 
 __global__ void kb_advance(int* counter) { *counter += 1; }
@@ -790,12 +810,12 @@ void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStrea
 
 void fp32_geometry(int nx, int ny, int* P, int* R) {
   *P = TW * ((nx + TW - 1) / TW) + 4;
-  *R = TH * ((ny + TH - 1) / TH) + 4;
+  *R = kTileRowsMax * ((ny + kTileRowsMax - 1) / kTileRowsMax) + 4;  // in bounds for every tile height
 }
 
-void fp32_tiles(int nx, int ny, int* nbx, int* nby) {
+void fp32_tiles(int nx, int ny, int th, int* nbx, int* nby) {
   *nbx = (nx + TW - 1) / TW;
-  *nby = (ny + TH - 1) / TH;
+  *nby = (ny + th - 1) / th;
 }
 
 MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
@@ -837,10 +857,11 @@ void Fp32Engine::advance_host(long long nsteps) {
 
 namespace {
 
-template <int N>
+template <int TH, int N>
 int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
                  int* counter, cudaStream_t st, Timers* tm) {
   static_assert(sizeof(DescSet<N>) + 3 * sizeof(void*) <= 32760, "launch parameters are limited to 32 KB");
+  constexpr int NT = nthreads<TH>();
   std::vector<DescSet<N>> hold(1);  // heap: up to ~28 KB
   DescSet<N>& ds = hold[0];
   std::memset(&ds, 0, sizeof ds);
@@ -854,8 +875,8 @@ int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, i
     if (tm && tm->on) tm->end(st);              \
     nl++;                                       \
   } while (0)
-#define MAIN1(S) LAUNCH("f32_main1", (kb_main1<S, N><<<g, NT, 0, st>>>(ds, tiles, counter)))
-  LAUNCH("f32_lap1", kb_lap1<N><<<g, NT, 0, st>>>(ds, tiles, counter));
+#define MAIN1(S) LAUNCH("f32_main1", (kb_main1<S, TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)))
+  LAUNCH("f32_lap1", (kb_lap1<TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)));
   switch (sch) {
     case 0: MAIN1(0); break;
     case 1: MAIN1(1); break;
@@ -869,7 +890,7 @@ int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, i
     case 9: MAIN1(9); break;
     default: MAIN1(kVanLeerSafe); break;
   }
-  LAUNCH("f32_main2", kb_main2<N><<<g, NT, 0, st>>>(ds, tiles, counter));
+  LAUNCH("f32_main2", (kb_main2<TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)));
   kb_advance<<<1, 1, 0, st>>>(counter);
   nl++;
 #undef MAIN1
@@ -877,13 +898,21 @@ int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, i
   return nl;
 }
 
+template <int TH>
+int batch_step_th(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
+                  int* counter, cudaStream_t st, Timers* tm) {
+  if (nmem == 1) return batch_step_n<TH, 1>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+  if (nmem <= 16) return batch_step_n<TH, 16>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+  return batch_step_n<TH, kMaxBatch>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+}
+
 }  // namespace
 
-int fp32_batch_step(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
-                    int* counter, cudaStream_t st, Timers* tm) {
-  if (nmem == 1) return batch_step_n<1>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
-  if (nmem <= 16) return batch_step_n<16>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
-  return batch_step_n<kMaxBatch>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+int fp32_batch_step(int sch, int th, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx,
+                    int nby, int* counter, cudaStream_t st, Timers* tm) {
+  if (th == 4) return batch_step_th<4>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+  if (th == 16) return batch_step_th<16>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
+  return batch_step_th<8>(sch, desc, nmem, tiles, ntiles, nbx, nby, counter, st, tm);
 }
 
 }  // namespace sw2g

@@ -236,12 +236,19 @@ constexpr int kMaxBatch = 96;
 MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k);
 // The same descriptor seen n steps after it was taken (what the kernels derive).
 MemberDesc fp32_desc_after(const MemberDesc& d, int n);
-void fp32_tiles(int nx, int ny, int* nbx, int* nby);
+// Tile shapes of the FP32 kernels: 32 cells wide, kTileRows[s] rows high.
+constexpr int kTileShapes = 3;
+constexpr int kTileRows[kTileShapes] = {4, 8, 16};
+constexpr int kTileRowsMax = 16;
+// Tile height of a single context's steps (measured fastest for one member).
+constexpr int kTileRowsSolo = 8;
+// Tiles of a grid for tiles th rows high.
+void fp32_tiles(int nx, int ny, int th, int* nbx, int* nby);
 // Enqueues one step of a batch of nmem members (host descriptors, passed by
-// value); tiles is the device tile table (unused for one member, whose grid
-// is nbx x nby). Returns the number of kernel launches.
-int fp32_batch_step(int sch, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx, int nby,
-                    int* counter, cudaStream_t st, Timers* tm);
+// value) with tiles th rows high; tiles is the device tile table (unused for
+// one member, whose grid is nbx x nby). Returns the number of kernel launches.
+int fp32_batch_step(int sch, int th, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx,
+                    int nby, int* counter, cudaStream_t st, Timers* tm);
 
 // FP32 shadow (pitch P) of an FP64 padded field (pitch nx+4), all padded cells.
 void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStream_t st);

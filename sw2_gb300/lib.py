@@ -332,6 +332,7 @@ class Batch:
     per phase over all members' tiles, time loop replayed as a CUDA graph."""
 
     SCHEDULES = ("rows", "columns", "interleaved", "bands")
+    TILE_ROWS = (4, 8, 16)  # tile shapes: 32 cells wide, this many rows high
 
     def __init__(self, solvers):
         L = load()
@@ -379,11 +380,28 @@ class Batch:
         return load().sw2g_batch_last_launches(self.h)
 
     def tune(self, steps_per_candidate: int):
-        ms = (ctypes.c_double * 4)()
+        """Times every (tile shape, schedule) pair and keeps the fastest;
+        returns {"32xTH/schedule": ms per step}."""
+        nc = len(self.TILE_ROWS) * len(self.SCHEDULES)
+        ms = (ctypes.c_double * nc)()
         rc = load().sw2g_batch_tune(self.h, int(steps_per_candidate), ms)
         if rc != OK:
             raise SW2GError(rc, "sw2g_batch_tune")
-        return {self.SCHEDULES[i]: ms[i] for i in range(4)}
+        ns = len(self.SCHEDULES)
+        return {f"32x{th}/{self.SCHEDULES[k]}": ms[i * ns + k] for i, th in enumerate(self.TILE_ROWS)
+                for k in range(ns)}
+
+    def set_schedule(self, tile_rows: int, schedule: str):
+        L = load()
+        L.sw2g_batch_set_schedule.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        rc = L.sw2g_batch_set_schedule(self.h, int(tile_rows), self.SCHEDULES.index(schedule))
+        if rc != OK:
+            raise SW2GError(rc, "sw2g_batch_set_schedule")
 
     def schedule(self) -> str:
         return self.SCHEDULES[load().sw2g_batch_schedule(self.h)]
+
+    def tile_rows(self) -> int:
+        L = load()
+        L.sw2g_batch_tile_rows.argtypes = [ctypes.c_void_p]
+        return L.sw2g_batch_tile_rows(self.h)

@@ -108,12 +108,9 @@ def _f05(p):
 
 
 def _f06(p):
-    # three injections on a 1024 x 512 band for the whole run: a ramped static
-    # one, a moving one across the periodic seam with tracer, one against the
-    # northern wall moving in degrees per second
-    p.gaussians = [[0.0, 40 * p.Dt, 2 * p.Dt, 100.0, 10.0, 0, 0.0, 2.0e13 / p.Dt, 1, 2.0, 6.0, 0.0],
-                   [0.0, 40 * p.Dt, 0.0, 2.0, -20.0, 0, -60.0, 1.5e13 / p.Dt, 1, 1.5, 5.0, 1.0],
-                   [0.0, 40 * p.Dt, 3 * p.Dt, 250.0, 50.0, 1, 0.01, 1.0e13 / p.Dt, 1, 3.0, 9.0, 0.5]]
+    # three injections on a 1024 x 512 band for the whole run (the bench's
+    # forcing workload, cases.forcing_band)
+    p.gaussians = cases.forcing_band(p.nsteps, p.nx, p.ny).gaussians
 
 
 FORCING_CASES = {

@@ -57,11 +57,36 @@ def test_tuning_changes_no_result():
         ss.append(s)
     b = lib.Batch(ss)
     times = b.tune(3)
-    assert set(times) == set(lib.Batch.SCHEDULES) and all(t > 0 for t in times.values())
-    assert b.schedule() in lib.Batch.SCHEDULES
+    assert len(times) == len(lib.Batch.TILE_ROWS) * len(lib.Batch.SCHEDULES)
+    assert all(t > 0 for t in times.values())
+    assert b.schedule() in lib.Batch.SCHEDULES and b.tile_rows() in lib.Batch.TILE_ROWS
     assert b.step(4) == lib.OK
+    # 12 candidates x 3 steps, one untimed step per shape, and 4 more
+    n = 12 * 3 + 3 + 4
     for c, s in zip(cs, ss):
-        got, ref = s.download(), solo(c, 4 * 3 + 4)
+        got, ref = s.download(), solo(c, n)
+        for k in ("eta", "u", "v"):
+            assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("tile_rows", lib.Batch.TILE_ROWS)
+def test_every_tile_shape_gives_the_same_bits(tile_rows):
+    """Each face is computed by the tile that needs it with the same
+    operations whatever the tile's height, so every shape and schedule, also
+    changed between steps, ends where the member stepped alone ends."""
+    cs = members(seed=9)
+    ss = []
+    for c in cs:
+        s = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
+        s.upload(*c.fields())
+        ss.append(s)
+    b = lib.Batch(ss)
+    b.set_schedule(tile_rows, "columns")
+    assert b.step(5) == lib.OK
+    b.set_schedule(lib.Batch.TILE_ROWS[(lib.Batch.TILE_ROWS.index(tile_rows) + 1) % 3], "interleaved")
+    assert b.step(6) == lib.OK
+    for c, s in zip(cs, ss):
+        got, ref = s.download(), solo(c, 11)
         for k in ("eta", "u", "v"):
             assert np.array_equal(got[k], ref[k]), k
 
