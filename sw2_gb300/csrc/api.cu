@@ -187,17 +187,18 @@ struct sw2g_ctx {
   // forcing between steps (FP64 form): staging of one padded field and a mask
   double* d_force = nullptr;
   void* d_mask = nullptr;
-  // forcing on listed cells: two pinned staging slots for the caller's index
-  // and value lists (used in turn, each free again once its event has
-  // completed), the lists on the device, and a padded field that is zero
-  // outside the cells of the call in progress
+  // forcing on listed cells: a ring of pinned staging slots for the caller's
+  // index and value lists (used in turn, each free again once its event has
+  // completed: with 8 slots the calls of one forced step do not wait for the
+  // step), the lists on the device, and a padded field that is zero outside
+  // the cells of the call in progress
   struct CellSlot {
     int* idx = nullptr;
     double* val = nullptr;
     size_t cap = 0;
     cudaEvent_t done = nullptr;
     bool pending = false;
-  } cell_slot[2];
+  } cell_slot[8];
   int cell_next = 0;
   int* d_cells = nullptr;
   double* d_cellv = nullptr;
@@ -1144,7 +1145,7 @@ sw2g_status stage_cells(sw2g_ctx* x, const int* cells, const double* values, int
     x->d_cell_cap = (size_t)n;
   }
   auto& sl = x->cell_slot[x->cell_next];
-  x->cell_next ^= 1;
+  x->cell_next = (x->cell_next + 1) % 8;
   if (!sl.done) CK(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
   if (sl.pending) CK(cudaEventSynchronize(sl.done));  // the copy that last used this slot
   sl.pending = false;
