@@ -312,6 +312,23 @@ def parity_fp64(lib, case, nsteps, local):
     return out
 
 
+def metric_divisors(case):
+    """The row metric factors the FP64 step divides by (DXE, DXV, DYN, DYC,
+    DXE+DXE, rZ at centres and faces), every row including halos."""
+    from sw2_gb300 import cases
+
+    p = case.params
+    g = cases.Grid(p)
+    dlon = (g.lon1 - g.lon0) / float(p.nx)
+    dlat = (g.lat1 - g.lat0) / float(p.ny)
+    out = []
+    for j in range(-1, p.ny + 3):
+        lc, ln, ln1 = g.latc(j), g.latn(j), g.latn(j - 1)
+        dxe = dlon * g.rZ(lc)
+        out += [dxe, dlon * g.rZ(ln), dlat * g.rM(lc), dlat * g.rM(ln1), dxe + dxe, g.rZ(lc), g.rZ(ln)]
+    return np.array(out)
+
+
 def forcing_leg(n_short: int, n_long: int):
     """Per-step time of the case-file runner (sw2g-run: case reader, host
     forcing, GPU step) on a 1024x512 band with three Gaussians injected in
@@ -511,6 +528,14 @@ def main():
         large = (cl.params.nx * cl.params.ny, descl, ml64, ml32, accl)
         del cl
     forced = forcing_leg(20, 220) if args.forcing and rank == 0 else None
+    # the FP64 step's division by row metrics (one Markstein correction)
+    # against IEEE division: 1e10 random and near-midpoint numerators over the
+    # metric factors of the headline workload, and each factor against the
+    # 1024 numerators within 512 ulps below +-2
+    divs = metric_divisors(case)
+    per = int(1e10) // len(divs) + 1
+    div_check = {"divisors": len(divs), "samples": per * len(divs), "grid_pairs": 1024 * len(divs),
+                 "mismatches": lib.selfcheck_division(divs, samples=per, seed=2026 + rank, device=local)}
     # the FP64 step against the oracle at the drop-in configuration's length
     par = None
     if args.parity_steps > 0 and rank == 0:
@@ -586,6 +611,7 @@ def main():
         "fp32_over_fp64_large": m32b["value"] / m64b["value"],
         "accuracy_fp32_vs_fp64": acc,
         "parity_fp64_vs_oracle": par,
+        "division_selfcheck": div_check,
         "forcing_runner": forced,
         "ensemble_fp32_batched": ens,
         "fp32_batched_over_fp64": (ens["value"] / m64["value"]) if ens else None,

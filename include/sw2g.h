@@ -276,12 +276,13 @@ int sw2g_batch_schedule(const sw2g_batch *b);
 int sw2g_batch_tile_rows(const sw2g_batch *b);
 void sw2g_batch_destroy(sw2g_batch *b);
 
-/* Self-check of the FP64 step's division by a row metric factor (it uses
- * multiplications and fused multiply-adds with the metric's correctly rounded
- * reciprocal; results must equal IEEE division bit for bit). For each of the
- * n divisors (positive, normal) draws `samples` numerators, random and near
- * rounding midpoints, on CUDA device `device`, and returns in *mismatches how
- * many quotients differ from IEEE a/b. No counterpart in the reference. */
+/* Self-check of the FP64 step's division by a row metric factor (one
+ * multiplication and two fused multiply-adds with the metric's correctly
+ * rounded reciprocal; results must equal IEEE division bit for bit). For each
+ * of the n divisors (positive, normal) draws `samples` numerators, random and
+ * near rounding midpoints, and also takes the 1024 numerators within 512 ulps
+ * below +-2, on CUDA device `device`; returns in *mismatches how many
+ * quotients differ from IEEE a/b. No counterpart in the reference. */
 sw2g_status sw2g_selfcheck_division(const double *divisors, int n, long long samples, unsigned long long seed,
                                     int device, long long *mismatches);
 

@@ -22,6 +22,7 @@ struct BatchExec {
   int4* d_tiles = nullptr;
   int ntiles = 0, nbx = 0, nby = 0;  // nbx x nby: the grid of a single member
   int th = kTileRowsSolo;            // tile height of the kernels
+  int per_step = 0;                  // launches per step of the captured graph
   int* d_counter = nullptr;
   int n_dev = 0;                     // device counter: steps since cap was taken
   std::vector<MemberDesc> cap;
@@ -88,7 +89,7 @@ struct BatchExec {
       cudaGraph_t g = nullptr;
       cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
-      fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, nullptr);
+      per_step = fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, nullptr);
       e = cudaStreamEndCapture(st, &g);
       if (e != cudaSuccess) return e;
       e = cudaGraphInstantiate(&exec, g, 0);
@@ -100,7 +101,7 @@ struct BatchExec {
       if (e != cudaSuccess) return e;
     }
     n_dev += n;
-    launches += 4LL * n;
+    launches += (long long)per_step * n;
     return cudaSuccess;
   }
 };
@@ -290,6 +291,10 @@ sw2g_status alloc_fp32(sw2g_ctx* x) {
   if ((st = dalloc32(x, &e.Lu, S32)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.Lv, S32)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.dup, S32)) != SW2G_OK) return st;
+  if (x->s.nu6 != 0) {
+    if ((st = dalloc32(x, &e.LLu, S32)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.LLv, S32)) != SW2G_OK) return st;
+  }
   if ((st = dalloc32(x, &e.dvp, S32)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.cfl, 2 * (size_t)kChunk)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.bad, (size_t)kChunk)) != SW2G_OK) return st;
@@ -517,8 +522,8 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   if (!out) return SW2G_ERR_BAD_ARG;
   *out = nullptr;
   if (!case_ok(c) || (precision != SW2G_FP64 && precision != SW2G_FP32)) return SW2G_ERR_BAD_ARG;
-  // the FP32 form covers nabla^2 and nabla^4 hyperviscosity (the configurations' operators)
-  if (precision == SW2G_FP32 && (c->hypernu[2] != 0 || c->polar != 0 || (c->flags & SW2G_FLAG_LAPE_ETA)))
+  // the FP32 form covers the band (no polar caps) and the reference's u source of the eta Laplacian
+  if (precision == SW2G_FP32 && (c->polar != 0 || (c->flags & SW2G_FLAG_LAPE_ETA)))
     return SW2G_ERR_BAD_ARG;
   sw2g_ctx* x = new (std::nothrow) sw2g_ctx();
   if (!x) return SW2G_ERR_NOMEM;
@@ -595,6 +600,7 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     c32.sigdt = (float)(s.sigma * c->Dt);
     c32.nu2dt = (float)(s.nu2 * c->Dt);
     c32.nu4dt = (float)(s.nu4 * c->Dt);
+    c32.nu6dt = (float)(s.nu6 * c->Dt);
     c32.wx = x->d_aux32[0];
     c32.wy = x->d_aux32[1];
     c32.hb = x->d_aux32[2];

@@ -45,7 +45,7 @@ __device__ __forceinline__ int IX(int W, int i, int j) { return (i + 1) + (j + 1
 struct KP {
   int nx, ny, W, H, P;
   const float* q;  // Q_NUM x H per-row FP32 table
-  float sig2dt, sigdt, nu2dt, nu4dt;
+  float sig2dt, sigdt, nu2dt, nu4dt, nu6dt;
   int k;           // Adams-Bashforth index
   int extra;       // winds / bottom present
   const float* wx; const float* wy; const float* hb;  // FP32 copies (pitch P) when extra
@@ -376,7 +376,10 @@ __device__ __forceinline__ void lap_out(const Rows& rc, int j, int a, int b, con
 }
 
 // ------------------------------------------------------------------ kernels
-template <int TH>
+// ACC = false: the first Laplacian level L of (u, v), written with its halo
+// images. ACC = true: the Laplacian of the second level LL, i.e. the third
+// level LLL, added as nu6*Dt*LLL to the partial tendencies Lu, Lv (core.c:233-268).
+template <int TH, bool ACC = false>
 __device__ __forceinline__ void d_lap1(const KP& p, int bx, int by, const float* __restrict__ u,
                                        const float* __restrict__ v, float* Lu, float* Lv) {
   __shared__ __align__(16) Tile<TH> su, sv;
@@ -395,8 +398,14 @@ __device__ __forceinline__ void d_lap1(const KP& p, int bx, int by, const float*
   if (i > p.nx || j > p.ny) return;
   float lu, lv;
   lap_out(rc, j, a, b, ze, di, lu, lv);
-  put<IMG_LU>(Lu, p.P, p.nx, p.ny, i, j, lu);
-  put<IMG_LV>(Lv, p.P, p.nx, p.ny, i, j, lv);
+  if constexpr (ACC) {
+    const int q32 = IX32(p.P, i, j);
+    Lu[q32] += p.nu6dt * lu;
+    Lv[q32] += p.nu6dt * lv;
+  } else {
+    put<IMG_LU>(Lu, p.P, p.nx, p.ny, i, j, lu);
+    put<IMG_LV>(Lv, p.P, p.nx, p.ny, i, j, lv);
+  }
 }
 
 struct Main1Io {
@@ -407,6 +416,7 @@ struct Main1Io {
   double* eta_next; float* es_next;
   float* hist_eta;          // slot for Deta_n
   float* dup; float* dvp;
+  float* LLu; float* LLv;   // second Laplacian level, written only when nu6 != 0
   unsigned* cfl;            // 2 floats as bits (max |u|/dx, max |v|/dy)
   int* bad;
 };
@@ -531,6 +541,10 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
     // ---- second Laplacian of (u, v) from L (laplacian.c:83-89)
     float llu, llv;
     lap_out(rc, j, ta, tb, ze, di, llu, llv);
+    if (p.nu6dt != 0.f) {  // kept with its halo images for the third level
+      put<IMG_LU>(o.LLu, P, nx, ny, i, j, llu);
+      put<IMG_LV>(o.LLv, P, nx, ny, i, j, llv);
+    }
 
     // ---- BODYU (calc.c:168-200)
     {
@@ -735,7 +749,7 @@ __device__ __forceinline__ KP kp_of(const MemberDesc& d, int k) {
   KP p;
   p.nx = d.nx; p.ny = d.ny; p.W = d.nx + 4; p.H = d.ny + 4; p.P = d.P;
   p.q = d.q;
-  p.sig2dt = d.sig2dt; p.sigdt = d.sigdt; p.nu2dt = d.nu2dt; p.nu4dt = d.nu4dt;
+  p.sig2dt = d.sig2dt; p.sigdt = d.sigdt; p.nu2dt = d.nu2dt; p.nu4dt = d.nu4dt; p.nu6dt = d.nu6dt;
   p.k = k;
   p.extra = d.extra;
   p.wx = d.wx; p.wy = d.wy; p.hb = d.hb;
@@ -761,6 +775,18 @@ __global__ void __launch_bounds__(nthreads<TH>(), 2048 / nthreads<TH>())
   d_lap1<TH>(kp_of(d, v.k), t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
 }
 
+// Third Laplacian level (nu6): members without it return at once.
+template <int TH, int N>
+__global__ void __launch_bounds__(nthreads<TH>(), 2048 / nthreads<TH>())
+    kb_lap3(const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, const int* __restrict__ counter) {
+  const int4 t = tile_of<N>(tiles);
+  const int n = *counter;
+  const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
+  if (d.nu6dt == 0.f) return;
+  const View v = view_of(d, n);
+  d_lap1<TH, true>(kp_of(d, v.k), t.y, t.z, d.LLu, d.LLv, d.dup, d.dvp);
+}
+
 template <int SCH, int TH, int N>
 __global__ void __launch_bounds__(nthreads<TH>())
     kb_main1(const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, const int* __restrict__ counter) {
@@ -769,8 +795,8 @@ __global__ void __launch_bounds__(nthreads<TH>())
   const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
   const View v = view_of(d, n);
   const Main1Io o{d.eta[v.cur], d.es[v.cur], d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv, d.heta[v.h1], d.heta[v.h2],
-                  d.eta[1 - v.cur], d.es[1 - v.cur], d.heta[v.w], d.dup, d.dvp, d.cfl + 2 * v.slot,
-                  d.bad + v.slot};
+                  d.eta[1 - v.cur], d.es[1 - v.cur], d.heta[v.w], d.dup, d.dvp, d.LLu, d.LLv,
+                  d.cfl + 2 * v.slot, d.bad + v.slot};
   d_main1<SCH, TH>(kp_of(d, v.k), t.y, t.z, o);
 }
 
@@ -823,7 +849,7 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
   std::memset(&d, 0, sizeof d);  // padding included, so descriptors compare with memcmp
   d.nx = c.nx; d.ny = c.ny; d.P = c.P;
   d.extra = c.extra;
-  d.sig2dt = c.sig2dt; d.sigdt = c.sigdt; d.nu2dt = c.nu2dt; d.nu4dt = c.nu4dt;
+  d.sig2dt = c.sig2dt; d.sigdt = c.sigdt; d.nu2dt = c.nu2dt; d.nu4dt = c.nu4dt; d.nu6dt = c.nu6dt;
   d.q = c.q;
   d.wx = c.wx; d.wy = c.wy; d.hb = c.hb;
   for (int q = 0; q < 2; q++) {
@@ -834,6 +860,7 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
     d.heta[q] = e.heta[q]; d.hu[q] = e.hu[q]; d.hv[q] = e.hv[q];
   }
   d.Lu = e.Lu; d.Lv = e.Lv; d.dup = e.dup; d.dvp = e.dvp;
+  d.LLu = e.LLu; d.LLv = e.LLv;
   d.cfl = e.cfl; d.bad = e.bad;
   d.cur0 = e.cur;
   d.w0 = e.w;
@@ -890,6 +917,9 @@ int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, i
     case 9: MAIN1(9); break;
     default: MAIN1(kVanLeerSafe); break;
   }
+  bool nu6 = false;
+  for (int m = 0; m < nmem; m++) nu6 = nu6 || (desc[m].nu6dt != 0.f);
+  if (nu6) LAUNCH("f32_lap3", (kb_lap3<TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)));
   LAUNCH("f32_main2", (kb_main2<TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)));
   kb_advance<<<1, 1, 0, st>>>(counter);
   nl++;

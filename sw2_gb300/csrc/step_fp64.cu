@@ -56,10 +56,15 @@ __device__ __forceinline__ double mul_pow2(double x, int k, double p) {
 #define TWICE(x) mul_pow2((x), 1, 2.0)
 
 // Correctly rounded a/b given y = RN(1/b), b a positive normal number, with
-// multiplications and fused multiply-adds (Markstein's method: P. Markstein,
-// IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook of
-// Floating-Point Arithmetic, ch. "division with an FMA"): q1 is within one
-// ulp of a/b, so r1 = a - b*q1 is exact and RN(q1 + r1*y) = RN(a/b).
+// one multiplication and two fused multiply-adds (Markstein's method:
+// P. Markstein, IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al., Handbook
+// of Floating-Point Arithmetic, ch. "division with an FMA"): q0 = RN(a*y),
+// r0 = a - b*q0 (exact), RN(q0 + r0*y) = RN(a/b). Markstein's theorem covers
+// q0 within one ulp of a/b; RN(a*y) can be up to 1.5 ulps off, and the one
+// correction still rounds correctly there by the case analysis of a/b in
+// [1/2, 1) scaled (a wrong rounding would need a and b both within a few
+// ulps of a power of two, a set the self-check walks exhaustively, with
+// random and near-midpoint numerators on top: fp64_check_division).
 // A zero numerator gives itself (+-0 / b = +-0 for b > 0); other numerators
 // outside [2^-900, 2^776] (subnormals: remainders could underflow; inf, NaN)
 // use the IEEE division. The row tables hold y = 1.0/b computed by IEEE
@@ -70,9 +75,7 @@ __device__ __forceinline__ double div_rcp(double a, double b, double y) {
   if ((unsigned)(dexp(a) - 123) > 1799u - 123u) return a / b;
   const double q0 = __dmul_rn(a, y);
   const double r0 = __fma_rn(-b, q0, a);
-  const double q1 = __fma_rn(r0, y, q0);
-  const double r1 = __fma_rn(-b, q1, a);
-  return __fma_rn(r1, y, q1);
+  return __fma_rn(r0, y, q0);
 }
 
 // a + b rounded to nearest, ties to even, computed on the integer pipe (the
@@ -761,6 +764,20 @@ __global__ void k_check_division(const double* div, int n, long long samples, un
       const double h = __longlong_as_double((long long)(((e - 53) << 52))) * (double)(((r2 >> 10) & 7) + 1) * 0.5;
       a = __dmul_rn(b, q + h);
     }
+    const double want = a / b, got = div_rcp(a, b, y);
+    if (dbits(want) != dbits(got)) miss++;
+  }
+  // every divisor against the numerators +-(2 - k ulp), k = 1..512: with the
+  // divisor's significand also within a few ulps of 2 these are the pairs
+  // where RN(a*y) strays more than one ulp from a/b and a wrong rounding is
+  // not excluded by the case analysis alone
+  const long long grid = (long long)n * 1024;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < grid;
+       t += (long long)gridDim.x * blockDim.x) {
+    const double b = div[t >> 10];
+    const double y = 1.0 / b;
+    const unsigned long long k = (unsigned long long)(t & 511), neg = (unsigned long long)((t >> 9) & 1);
+    const double a = __longlong_as_double((long long)((0x3FFFFFFFFFFFFFFFULL - k) | (neg << 63)));
     const double want = a / b, got = div_rcp(a, b, y);
     if (dbits(want) != dbits(got)) miss++;
   }

@@ -173,7 +173,7 @@ struct Fp32Ctx {
   int nx, ny, sch, extra;
   int P, R;  // FP32 arrays: row pitch and rows (padded so tile windows stay in bounds)
   const float* q;
-  float sig2dt, sigdt, nu2dt, nu4dt;
+  float sig2dt, sigdt, nu2dt, nu4dt, nu6dt;
   const float* wx; const float* wy; const float* hb;
   // Test of the failure path (sw2g_test_tile_timeout): > 0 makes the tile
   // loads of the next steps also wait for a barrier phase that never
@@ -196,6 +196,7 @@ struct Fp32Engine {
   float* hv[3] = {nullptr, nullptr, nullptr};
   int w = 0;
   float* Lu = nullptr; float* Lv = nullptr;
+  float* LLu = nullptr; float* LLv = nullptr;  // second Laplacian level (only with nu6)
   float* dup = nullptr; float* dvp = nullptr;
   unsigned* cfl = nullptr;  // 2 per step (float bits)
   int* bad = nullptr;       // 1 per step
@@ -217,13 +218,14 @@ constexpr int kCheckTimeout = 2;
 struct MemberDesc {
   int nx, ny, P;
   int extra;
-  float sig2dt, sigdt, nu2dt, nu4dt;
+  float sig2dt, sigdt, nu2dt, nu4dt, nu6dt;
   const float* q;
   const float* wx; const float* wy; const float* hb;
   double* eta[2]; double* u[2]; double* v[2];
   float* es[2]; float* us[2]; float* vs[2];
   float* heta[3]; float* hu[3]; float* hv[3];
   float* Lu; float* Lv; float* dup; float* dvp;
+  float* LLu; float* LLv;
   unsigned* cfl; int* bad;
   int cur0, w0, k0, tile_test;
 };

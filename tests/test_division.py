@@ -38,6 +38,19 @@ def test_random_divisors_match_ieee():
     assert lib.selfcheck_division(d, samples=5_000, seed=12) == 0
 
 
+def test_divisors_near_powers_of_two_match_ieee():
+    """The one-correction quotient RN(q0 + (a - b q0) y), q0 = RN(a y), can
+    start more than one ulp off only when a's and b's significands are both
+    within a few ulps of 2: every divisor within 512 ulps below 2 (and just
+    above 1, and scaled by powers of two) against every numerator within 512
+    ulps below 2 of either sign (the self-check's grid), plus random and
+    near-midpoint numerators."""
+    below2 = np.arange(0x3FFFFFFFFFFFFFFF - 511, 0x3FFFFFFFFFFFFFFF + 1, dtype=np.uint64).view(np.float64)
+    above1 = np.arange(0x3FF0000000000000, 0x3FF0000000000000 + 512, dtype=np.uint64).view(np.float64)
+    d = np.concatenate([below2, above1, np.ldexp(below2, -20), np.ldexp(below2, 37), np.ldexp(above1, 11)])
+    assert lib.selfcheck_division(d, samples=2_000, seed=13) == 0
+
+
 def test_integer_pipe_addition_matches_the_fp64_unit():
     """The step's additions on the integer pipe (sadd, ssub) against the FP64
     unit: 2^27 operand pairs per seed over the adder's edge cases."""

@@ -76,9 +76,30 @@ def test_fp32_winds_and_nu2():
     assert np.max(np.abs(a["u"] - b["u"])) <= 2e-5 * np.max(np.abs(b["u"]))
 
 
+def test_fp32_nu2_nu4_nu6():
+    """All three hyperviscosity orders (laplacian_vels applied three times,
+    core.c:233-268): the third level is the Laplacian of the second, with the
+    same halo images and wall fixes, added to the partial tendencies."""
+    case = cases.make_case(nx=96, ny=48, sch=1, seed=12)
+    nu4 = case.params.hypernu[1]  # grid-scale e-folding time 10 Dt
+    # nu6 with a grid-scale e-folding time of 20 Dt, so that it matters
+    nu6 = 0.5 * nu4 ** 1.5 * (10.0 * case.params.Dt) ** 0.5
+    case.params.hypernu = (2.0e-3 * nu4 ** 0.5, 0.5 * nu4, nu6)
+    _, a = run(case, lib.FP32, 6)
+    _, b = run(case, lib.FP64, 6)
+    assert np.max(np.abs(a["eta"] - b["eta"])) <= 2e-6 * case.params.depth
+    assert np.max(np.abs(a["u"] - b["u"])) <= 2e-5 * np.max(np.abs(b["u"]))
+    assert np.max(np.abs(a["v"] - b["v"])) <= 2e-5 * max(1.0, np.max(np.abs(b["v"])))
+    # and it matters: without nu6 the FP64 step ends elsewhere
+    case.params.hypernu = (2.0e-3 * nu4 ** 0.5, 0.5 * nu4, 0.0)
+    _, c = run(case, lib.FP64, 6)
+    assert np.max(np.abs(c["u"] - b["u"])) > 10 * np.max(np.abs(a["u"] - b["u"]))
+
+
 def test_fp32_rejects_what_it_does_not_cover():
     case = cases.make_case(nx=16, ny=8, sch=2, seed=1)
-    case.params.hypernu = (0.0, 1.0, 1.0)
+    case.params.polar, case.params.angleSim = 1, 20.0
+    case.params.nx = case.params.ny = 16
     with pytest.raises(lib.SW2GError):
         lib.Solver(case.params, precision=lib.FP32)
     case = cases.make_case(nx=16, ny=8, sch=2, seed=1, tracer=True)

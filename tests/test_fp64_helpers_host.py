@@ -175,6 +175,19 @@ int main(int argc, char** argv) {
     if (!same(x * 0.25, mul_pow2(x, -2, 0.25))) bad_pow++;
     if (!same(x * 2.0, mul_pow2(x, 1, 2.0))) bad_pow++;
   }
+  // every divisor within 512 ulps below 2 or just above 1 against every
+  // numerator within 512 ulps below +-2: the pairs where RN(a*y) can stray
+  // more than one ulp from a/b
+  for (int j = 0; j < 1024; j++) {
+    const double b = j < 512 ? __longlong_as_double(0x3FFFFFFFFFFFFFFFLL - j)
+                             : __longlong_as_double(0x3FF0000000000000LL + (j - 512));
+    const double y = 1.0 / b;
+    for (int k = 0; k < 1024; k++) {
+      const double a = __longlong_as_double((long long)((0x3FFFFFFFFFFFFFFFULL - (uint64_t)(k & 511)) |
+                                                        ((uint64_t)(k >> 9) << 63)));
+      if (!same(a / b, div_rcp(a, b, y))) bad_div++;
+    }
+  }
   printf("%%lld %%lld\n", bad_div, bad_pow);
   return 0;
 }
