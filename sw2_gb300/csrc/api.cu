@@ -354,15 +354,53 @@ bool all_zero(const double* a, size_t n) {
 
 // Upload for the FP32 form: eta is stored as eta - eta_ref(j), with eta_ref
 // the zonal mean of the uploaded interior (halo rows take the wrapped rows).
+// Buffers of the FP32 form's tracer, made on the first upload of a nonzero
+// tracer: FP64 state and FP32 shadow (double-buffered), the history ring and
+// the device descriptor the tracer kernel reads.
+sw2g_status tracer_fp32(sw2g_ctx* x) {
+  Fp32Engine& e = x->e32;
+  if (e.d_trd) return SW2G_OK;
+  const size_t S = (size_t)x->s.W * x->s.H, S32 = (size_t)x->c32.P * x->c32.R;
+  sw2g_status st;
+  for (int q = 0; q < 2; q++) {
+    if ((st = dalloc(x, &e.tr[q], S)) != SW2G_OK) return st;
+    if ((st = dalloc32(x, &e.ts[q], S32)) != SW2G_OK) return st;
+  }
+  for (int q = 0; q < 3; q++)
+    if ((st = dalloc32(x, &e.htr[q], S32)) != SW2G_OK) return st;
+  TracerDesc td;
+  for (int q = 0; q < 2; q++) {
+    td.tr[q] = e.tr[q];
+    td.ts[q] = e.ts[q];
+  }
+  for (int q = 0; q < 3; q++) td.h[q] = e.htr[q];
+  td.sig2dt = (float)(2.0 * x->c.Dt * x->c.tracer_dis);  // calc.c:162
+  TracerDesc* d = nullptr;
+  if ((st = dalloc32(x, &d, 1)) != SW2G_OK) return st;
+  CK(cudaMemcpyAsync(d, &td, sizeof td, cudaMemcpyHostToDevice, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  e.d_trd = d;
+  return SW2G_OK;
+}
+
 sw2g_status upload_fp32(sw2g_ctx* x, const double* eta, const double* u, const double* v, const double* tracer,
                         const double* windx, const double* windy, const double* hB, int mode) {
   const DevState& s = x->s;
   const int W = s.W, H = s.H, nx = s.nx, ny = s.ny;
   const size_t S = (size_t)W * H, bytes = S * sizeof(double);
   const bool cont = (mode == SW2G_UPLOAD_CONTINUE);
-  if (tracer && !all_zero(tracer, S)) {
-    fprintf(stderr, "sw2g: the FP32 form does not advect a tracer; upload an all-zero tracer or NULL\n");
-    return SW2G_ERR_BAD_ARG;
+  Fp32Engine& e = x->e32;
+  // the tracer is advected once any padded cell of it can be nonzero (a tracer
+  // that is +0.0 everywhere stays so: its step then changes nothing)
+  if (tracer && (e.tracer || !all_zero(tracer, S))) {
+    sw2g_status st = tracer_fp32(x);
+    if (st != SW2G_OK) return st;
+    CK(cudaMemcpyAsync(e.tr[e.cur], tracer, bytes, cudaMemcpyHostToDevice, x->stream));
+    if (mode == SW2G_UPLOAD_FRAME) halo_wrap(e.tr[e.cur], nx, ny, x->stream);
+    fp32_shadow(e.ts[e.cur], e.tr[e.cur], nx, ny, x->c32.P, x->stream);
+    e.tracer = true;
+  } else if (!cont) {
+    e.tracer = false;
   }
   if (!cont) {
     x->ref.assign(H, 0.0);
@@ -385,7 +423,6 @@ sw2g_status upload_fp32(sw2g_ctx* x, const double* eta, const double* u, const d
     CK(cudaMemcpyAsync(x->d_q32, q.data(), q.size() * sizeof(float), cudaMemcpyHostToDevice, x->stream));
     CK(cudaStreamSynchronize(x->stream));
   }
-  Fp32Engine& e = x->e32;
   std::vector<double> ep(S);
   for (int j = -1; j <= ny + 2; j++)
     for (int i = -1; i <= nx + 2; i++) {
@@ -940,8 +977,11 @@ sw2g_status sw2g_download(sw2g_ctx* x, double* eta, double* u, double* v, double
     }
     if (u) CK(cudaMemcpyAsync(u, e.u[e.cur], bytes, cudaMemcpyDeviceToHost, x->stream));
     if (v) CK(cudaMemcpyAsync(v, e.v[e.cur], bytes, cudaMemcpyDeviceToHost, x->stream));
+    if (tracer) {
+      if (e.tracer) CK(cudaMemcpyAsync(tracer, e.tr[e.cur], bytes, cudaMemcpyDeviceToHost, x->stream));
+      else std::memset(tracer, 0, bytes);
+    }
     CK(cudaStreamSynchronize(x->stream));
-    if (tracer) std::memset(tracer, 0, bytes);
     return SW2G_OK;
   }
   for (int q = 0; q < 4; q++)
@@ -1223,8 +1263,9 @@ void* sw2g_device_field(sw2g_ctx* x, int which) {
   if (!x || which < 0 || which > 3) return nullptr;
   if (x->precision == SW2G_FP32) {
     const Fp32Engine& e = x->e32;
-    // eta is held as eta - eta_ref(j) in this form; the tracer is not held
-    return which == 0 ? (void*)e.eta[e.cur] : which == 1 ? (void*)e.u[e.cur] : which == 2 ? (void*)e.v[e.cur] : nullptr;
+    // eta is held as eta - eta_ref(j) in this form; the tracer only while advected
+    return which == 0 ? (void*)e.eta[e.cur] : which == 1 ? (void*)e.u[e.cur] : which == 2 ? (void*)e.v[e.cur]
+                                                                            : (e.tracer ? (void*)e.tr[e.cur] : nullptr);
   }
   return x->b.f[which];
 }

@@ -591,6 +591,59 @@ __device__ __forceinline__ void d_main1(const KP& p, int bx, int by, const Main1
   }
 }
 
+// BODYTRACER (calc.c:117-163): TVD fluxes of the tracer on the four faces,
+// each with both split Courant numbers of its face velocity (winds
+// included), the compression term and the damping -2*Dt*TracerDis*T; then the
+// Adams-Bashforth combination (calc.c:651-699) and the update with the
+// single-rank halo wrap (core.c:161-182). One cell per thread, faces per cell.
+template <int SCH, int TH>
+__device__ __forceinline__ void d_tracer(const KP& p, int bx, int by, const TracerDesc& td, int cur, int w, int h1,
+                                         int h2, const float* __restrict__ us, const float* __restrict__ vs,
+                                         int* bad) {
+  __shared__ __align__(16) Tile<TH> st, su, sv;
+  __shared__ RowCache<TH> sq;
+  const int W = p.W, P = p.P, nx = p.nx, ny = p.ny;
+  const int i0 = bx * TW + 1, j0 = by * TH + 1;
+  fill_rows<TH>(p, j0, sq);
+  const Rows rc{sq, j0};
+  load_tile<TH>(td.ts[cur], P, i0, j0, st);
+  load_tile<TH>(us, P, i0, j0, su);
+  load_tile<TH>(vs, P, i0, j0, sv);
+  __syncthreads();
+  if (p.extra) {  // UWINDX, VWINDY (sw.h:216-217)
+    for (int t = threadIdx.x; t < (TH + 4) * (TW + 4); t += nthreads<TH>()) {
+      const int c = t % (TW + 4), r = t / (TW + 4);
+      const int qq = IX32(P, i0 - 2 + c, j0 - 2 + r);
+      su[r][c] += p.wx[qq];
+      sv[r][c] += p.wy[qq];
+    }
+    __syncthreads();
+  }
+  const int ta = threadIdx.x % TW, tb = threadIdx.x / TW;
+  const int a = ta + 2, b = tb + 2, i = i0 + ta, j = j0 + tb;
+  if (i > nx || j > ny) return;
+  const float kx = Q(rc, Q_KXE, j), ky = Q(rc, Q_KYN, j);
+  const float uw = su[b][a - 1], ue = su[b][a], vsb = sv[b - 1][a], vn = sv[b][a];
+  const float T = st[b][a];
+  const float fw = face2<SCH>(st[b][a - 2], st[b][a - 1], T, st[b][a + 1], fmaxf(uw, 0.f) * kx, fminf(uw, 0.f) * kx);
+  const float fe = face2<SCH>(st[b][a - 1], T, st[b][a + 1], st[b][a + 2], fmaxf(ue, 0.f) * kx, fminf(ue, 0.f) * kx);
+  const float fs = face2<SCH>(st[b - 2][a], st[b - 1][a], T, st[b + 1][a], fmaxf(vsb, 0.f) * ky, fminf(vsb, 0.f) * ky);
+  const float fn = face2<SCH>(st[b - 1][a], T, st[b + 1][a], st[b + 2][a], fmaxf(vn, 0.f) * ky, fminf(vn, 0.f) * ky);
+  float dtr = (fw - fe) + (fs - fn);
+  dtr += T * ((ue - uw) * kx + (vn - vsb) * ky);
+  dtr -= td.sig2dt * T;
+  const int q32 = IX32(P, i, j);
+  float ab;
+  if (p.k == 0) ab = dtr;
+  else if (p.k == 1) ab = 1.5f * dtr - 0.5f * td.h[h1][q32];
+  else ab = (23.f / 12.f) * dtr - (4.f / 3.f) * td.h[h1][q32] + (5.f / 12.f) * td.h[h2][q32];
+  td.h[w][q32] = dtr;
+  const double tn = td.tr[cur][IX(W, i, j)] + f2d(ab);
+  put<IMG_ETA>(td.tr[1 - cur], W, nx, ny, i, j, tn);
+  put<IMG_ETA>(td.ts[1 - cur], P, nx, ny, i, j, d2f(tn));
+  if (!in_range(tn)) atomicOr(bad, 1);
+}
+
 struct Main2Io {
   const float* es;                        // new eta shadow
   const double* u; const double* v;       // FP64 state at step start (pitch W)
@@ -775,6 +828,19 @@ __global__ void __launch_bounds__(nthreads<TH>(), 2048 / nthreads<TH>())
   d_lap1<TH>(kp_of(d, v.k), t.y, t.z, d.us[v.cur], d.vs[v.cur], d.Lu, d.Lv);
 }
 
+// Tracer advection: members without an active tracer return at once.
+template <int SCH, int TH, int N>
+__global__ void __launch_bounds__(nthreads<TH>())
+    kb_tracer(const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, const int* __restrict__ counter) {
+  const int4 t = tile_of<N>(tiles);
+  const int n = *counter;
+  const MemberDesc& d = ds.m[N == 1 ? 0 : t.x];
+  if (!d.trd) return;
+  const View v = view_of(d, n);
+  d_tracer<SCH, TH>(kp_of(d, v.k), t.y, t.z, *d.trd, v.cur, v.w, v.h1, v.h2, d.us[v.cur], d.vs[v.cur],
+                    d.bad + v.slot);
+}
+
 // Third Laplacian level (nu6): members without it return at once.
 template <int TH, int N>
 __global__ void __launch_bounds__(nthreads<TH>(), 2048 / nthreads<TH>())
@@ -861,6 +927,7 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
   }
   d.Lu = e.Lu; d.Lv = e.Lv; d.dup = e.dup; d.dvp = e.dvp;
   d.LLu = e.LLu; d.LLv = e.LLv;
+  d.trd = e.tracer ? e.d_trd : nullptr;
   d.cfl = e.cfl; d.bad = e.bad;
   d.cur0 = e.cur;
   d.w0 = e.w;
@@ -903,6 +970,23 @@ int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, i
     nl++;                                       \
   } while (0)
 #define MAIN1(S) LAUNCH("f32_main1", (kb_main1<S, TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)))
+#define TRACER(S) LAUNCH("f32_tracer", (kb_tracer<S, TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)))
+  bool tracer = false;
+  for (int m = 0; m < nmem; m++) tracer = tracer || (desc[m].trd != nullptr);
+  if (tracer) {  // reads the step's old u, v and tracer only (core.c:161-182)
+    switch (sch) {
+      case 0: TRACER(0); break;
+      case 1: TRACER(1); break;
+      case 2: TRACER(2); break;
+      case 4: TRACER(4); break;
+      case 5: TRACER(5); break;
+      case 6: TRACER(6); break;
+      case 7: TRACER(7); break;
+      case 8: TRACER(8); break;
+      case 9: TRACER(9); break;
+      default: TRACER(kVanLeerSafe); break;
+    }
+  }
   LAUNCH("f32_lap1", (kb_lap1<TH, N><<<g, NT, 0, st>>>(ds, tiles, counter)));
   switch (sch) {
     case 0: MAIN1(0); break;
@@ -924,6 +1008,7 @@ int batch_step_n(int sch, const MemberDesc* desc, int nmem, const int4* tiles, i
   kb_advance<<<1, 1, 0, st>>>(counter);
   nl++;
 #undef MAIN1
+#undef TRACER
 #undef LAUNCH
   return nl;
 }

@@ -169,6 +169,16 @@ enum Q32 {
   Q_NUM
 };
 
+// Tracer of an FP32-form member (device-resident, one per context with an
+// active tracer): FP64 state and FP32 shadow (double-buffered like eta), the
+// three-slot history ring of its tendency, and 2*Dt*TracerDis.
+struct TracerDesc {
+  double* tr[2];
+  float* ts[2];
+  float* h[3];
+  float sig2dt;
+};
+
 struct Fp32Ctx {
   int nx, ny, sch, extra;
   int P, R;  // FP32 arrays: row pitch and rows (padded so tile windows stay in bounds)
@@ -197,6 +207,12 @@ struct Fp32Engine {
   int w = 0;
   float* Lu = nullptr; float* Lv = nullptr;
   float* LLu = nullptr; float* LLv = nullptr;  // second Laplacian level (only with nu6)
+  // tracer (allocated when a nonzero tracer is uploaded; advected while active)
+  double* tr[2] = {nullptr, nullptr};
+  float* ts[2] = {nullptr, nullptr};
+  float* htr[3] = {nullptr, nullptr, nullptr};
+  TracerDesc* d_trd = nullptr;
+  bool tracer = false;
   float* dup = nullptr; float* dvp = nullptr;
   unsigned* cfl = nullptr;  // 2 per step (float bits)
   int* bad = nullptr;       // 1 per step
@@ -226,6 +242,7 @@ struct MemberDesc {
   float* heta[3]; float* hu[3]; float* hv[3];
   float* Lu; float* Lv; float* dup; float* dvp;
   float* LLu; float* LLv;
+  const TracerDesc* trd;  // nullptr: no tracer advected
   unsigned* cfl; int* bad;
   int cur0, w0, k0, tile_test;
 };

@@ -96,16 +96,32 @@ def test_fp32_nu2_nu4_nu6():
     assert np.max(np.abs(c["u"] - b["u"])) > 10 * np.max(np.abs(a["u"] - b["u"]))
 
 
+@pytest.mark.parametrize("sch", [1, 2, 3])
+def test_fp32_tracer_with_winds(sch):
+    """The tracer (BODYTRACER, calc.c:117-163; AB and update, core.c:161-182)
+    advected by the flow plus a zonal wind, with its dissipation: FP64 state,
+    FP32 fluxes, within the tolerance of the other fields."""
+    wind = np.stack([np.arange(-180.0, 181.0), 25 * np.cos(np.deg2rad(np.arange(-180.0, 181.0)) * 3)], axis=1)
+    case = cases.make_case(nx=64, ny=32, sch=sch, seed=21, wind=wind, tracer=True, TracerDis=2.0e-6)
+    flags = lib.FLAG_VANLEER_SAFE if sch == 3 else 0
+    _, a = run(case, lib.FP32, 8, flags=flags)
+    _, b = run(case, lib.FP64, 8, flags=flags)
+    assert np.max(np.abs(b["tracer"])) > 0.1
+    assert np.max(np.abs(a["tracer"] - b["tracer"])) <= 2e-5 * np.max(np.abs(b["tracer"]))
+    assert np.max(np.abs(a["eta"] - b["eta"])) <= 2e-6 * case.params.depth
+    # the tracer moved: it differs from its initial field
+    assert np.max(np.abs(b["tracer"] - case.tracer)) > 1e-3 * np.max(np.abs(b["tracer"]))
+
+
 def test_fp32_rejects_what_it_does_not_cover():
     case = cases.make_case(nx=16, ny=8, sch=2, seed=1)
     case.params.polar, case.params.angleSim = 1, 20.0
     case.params.nx = case.params.ny = 16
     with pytest.raises(lib.SW2GError):
         lib.Solver(case.params, precision=lib.FP32)
-    case = cases.make_case(nx=16, ny=8, sch=2, seed=1, tracer=True)
-    s = lib.Solver(case.params, precision=lib.FP32)
+    case = cases.make_case(nx=16, ny=8, sch=2, seed=1)
     with pytest.raises(lib.SW2GError):
-        s.upload(*case.fields())
+        lib.Solver(case.params, precision=lib.FP32, flags=lib.FLAG_LAPE_ETA)
 
 
 @pytest.mark.slow
