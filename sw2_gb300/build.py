@@ -31,13 +31,16 @@ HOST_C = ["gcc", "-std=gnu11", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-m
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST = "-fPIC,-ffp-contract=off,-O2"
 
-# (source, extra nvcc flags)
+# (source, extra nvcc flags, object name); the FP32 form's limiter kernels are
+# one source compiled once per limiter group
 UNITS = [
-    ("api.cu", []),
-    ("step_fp64.cu", ["-fmad=false"]),
-    ("noalloc.cu", ["-fmad=false"]),
-    ("step_fp32.cu", []),
-    ("geometry.cpp", None),  # plain host C++
+    ("api.cu", [], "api.o"),
+    ("step_fp64.cu", ["-fmad=false"], "step_fp64.o"),
+    ("noalloc.cu", ["-fmad=false"], "noalloc.o"),
+    ("step_fp32.cu", ["-fmad=false"], "step_fp32.o"),
+    *[("step_fp32_limiters.cu", ["-fmad=false", f"-DSW2G_LIMITER_GROUP={g}"], f"step_fp32_limiters{g}.o")
+      for g in range(4)],
+    ("geometry.cpp", None, "geometry.o"),  # plain host C++
 ]
 
 
@@ -46,8 +49,8 @@ def nvcc() -> str:
     return p
 
 
-def _compile(src: str, extra) -> str:
-    obj = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, extra, objname: str) -> str:
+    obj = os.path.join(OUT, objname)
     path = os.path.join(CSRC, src)
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
     if extra is None:
@@ -97,7 +100,7 @@ def build(force: bool = False) -> str:
     if not force and not _stale():
         return LIB
     os.makedirs(OUT, exist_ok=True)
-    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), UNITS))
     tmp = LIB + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-Xcompiler", "-fPIC"]

@@ -24,6 +24,7 @@ struct BatchExec {
   int th = kTileRowsSolo;            // tile height of the kernels
   int per_step = 0;                  // launches per step of the captured graph
   int* d_counter = nullptr;
+  unsigned* d_queue = nullptr;       // the kernels' strip queue (2 words, zero between launches)
   int n_dev = 0;                     // device counter: steps since cap was taken
   std::vector<MemberDesc> cap;
   cudaGraphExec_t exec = nullptr;
@@ -32,6 +33,8 @@ struct BatchExec {
   cudaError_t alloc(int ntile) {
     ntiles = ntile;
     cudaError_t e = cudaMalloc((void**)&d_counter, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_queue, 2 * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(d_queue, 0, 2 * sizeof(unsigned));
     if (e == cudaSuccess && ntile > 0) e = cudaMalloc((void**)&d_tiles, sizeof(int4) * ntile);
     return e;
   }
@@ -39,9 +42,11 @@ struct BatchExec {
     if (exec) cudaGraphExecDestroy(exec);
     if (d_tiles) cudaFree(d_tiles);
     if (d_counter) cudaFree(d_counter);
+    if (d_queue) cudaFree(d_queue);
     exec = nullptr;
     d_tiles = nullptr;
     d_counter = nullptr;
+    d_queue = nullptr;
     cap.clear();
   }
   // Brings the launch state in line with the members' descriptors at their
@@ -81,7 +86,7 @@ struct BatchExec {
     const int M = (int)cap.size();
     if (tm && tm->on) {
       for (int s = 0; s < n; s++)
-        launches += fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, tm);
+        launches += fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, d_queue, st, tm);
       n_dev += n;
       return cudaGetLastError();
     }
@@ -89,7 +94,7 @@ struct BatchExec {
       cudaGraph_t g = nullptr;
       cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
       if (e != cudaSuccess) return e;
-      per_step = fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, st, nullptr);
+      per_step = fp32_batch_step(sch, th, cap.data(), M, d_tiles, ntiles, nbx, nby, d_counter, d_queue, st, nullptr);
       e = cudaStreamEndCapture(st, &g);
       if (e != cudaSuccess) return e;
       e = cudaGraphInstantiate(&exec, g, 0);
@@ -291,6 +296,11 @@ sw2g_status alloc_fp32(sw2g_ctx* x) {
   if ((st = dalloc32(x, &e.Lu, S32)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.Lv, S32)) != SW2G_OK) return st;
   if ((st = dalloc32(x, &e.dup, S32)) != SW2G_OK) return st;
+  {
+    unsigned char* maps = nullptr;
+    if ((st = dalloc32(x, &maps, fp32_map_bytes())) != SW2G_OK) return st;
+    e.maps = maps;
+  }
   if (x->s.nu6 != 0) {
     if ((st = dalloc32(x, &e.LLu, S32)) != SW2G_OK) return st;
     if ((st = dalloc32(x, &e.LLv, S32)) != SW2G_OK) return st;
@@ -380,6 +390,10 @@ sw2g_status tracer_fp32(sw2g_ctx* x) {
   CK(cudaMemcpyAsync(d, &td, sizeof td, cudaMemcpyHostToDevice, x->stream));
   CK(cudaStreamSynchronize(x->stream));
   e.d_trd = d;
+  if (!fp32_write_maps(e.maps, x->c32, e, x->stream)) {  // now with the tracer shadows
+    fprintf(stderr, "sw2g: tensor maps of the FP32 fields could not be made\n");
+    return SW2G_ERR_CUDA;
+  }
   return SW2G_OK;
 }
 
@@ -644,6 +658,12 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     fp32_tiles(c->nx, c->ny, x->run32.th, &x->run32.nbx, &x->run32.nby);
     if ((st = cuda_fail(x->run32.alloc(0), "batch")) != SW2G_OK) return fail(st);
     x->run32.sch = c32.sch;
+    fp32_prepare();
+    if ((st = cuda_fail(cudaStreamSynchronize(x->stream), "alloc")) != SW2G_OK) return fail(st);
+    if (!fp32_write_maps(x->e32.maps, c32, x->e32, x->stream)) {
+      fprintf(stderr, "sw2g: tensor maps of the FP32 fields could not be made\n");
+      return fail(SW2G_ERR_CUDA);
+    }
   }
   if ((st = cuda_fail(cudaMalloc((void**)&x->d_cfl, sizeof(unsigned long long) * 2 * kChunk), "cfl")) != SW2G_OK)
     return fail(st);

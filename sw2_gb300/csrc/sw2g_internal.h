@@ -1,6 +1,7 @@
 // Internal declarations shared by the sw2g translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -216,8 +217,17 @@ struct Fp32Engine {
   float* dup = nullptr; float* dvp = nullptr;
   unsigned* cfl = nullptr;  // 2 per step (float bits)
   int* bad = nullptr;       // 1 per step
+  void* maps = nullptr;     // TM_NUM tensor maps (device memory) of the FP32 fields, see Fp32Map
   // host view after nsteps more steps: state buffer and history ring position
   void advance_host(long long nsteps);
+};
+
+// Tensor maps of a member's FP32 fields (rows of a strip, for the TMA
+// engine), by field: the two buffers of the eta, u, v and tracer shadows, the
+// Laplacian levels, the winds and the bottom height.
+enum Fp32Map {
+  TM_ES = 0, TM_US = 2, TM_VS = 4, TM_LU = 6, TM_LV = 7, TM_LLU = 8, TM_LLV = 9, TM_TS = 10,
+  TM_WX = 12, TM_WY = 13, TM_HB = 14, TM_NUM = 15
 };
 
 // Steps whose checks are kept on the device before the host reads them back.
@@ -243,6 +253,7 @@ struct MemberDesc {
   float* Lu; float* Lv; float* dup; float* dvp;
   float* LLu; float* LLv;
   const TracerDesc* trd;  // nullptr: no tracer advected
+  const CUtensorMap* tm;  // TM_NUM tensor maps of this member's FP32 fields
   unsigned* cfl; int* bad;
   int cur0, w0, k0, tile_test;
 };
@@ -255,19 +266,30 @@ constexpr int kMaxBatch = 96;
 MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k);
 // The same descriptor seen n steps after it was taken (what the kernels derive).
 MemberDesc fp32_desc_after(const MemberDesc& d, int n);
-// Tile shapes of the FP32 kernels: 32 cells wide, kTileRows[s] rows high.
+// Strips of the FP32 kernels: kStripWidth cells wide (a warp, four cells per
+// lane), kTileRows[s] rows high (the shapes the batch tuner picks from).
+constexpr int kStripWidth = 128;
 constexpr int kTileShapes = 3;
-constexpr int kTileRows[kTileShapes] = {4, 8, 16};
-constexpr int kTileRowsMax = 16;
-// Tile height of a single context's steps (measured fastest for one member).
-constexpr int kTileRowsSolo = 8;
-// Tiles of a grid for tiles th rows high.
+constexpr int kTileRows[kTileShapes] = {16, 32, 64};
+// Strip height of a single context's steps.
+constexpr int kTileRowsSolo = 32;
+// Strips of a grid for strips th rows high.
 void fp32_tiles(int nx, int ny, int th, int* nbx, int* nby);
 // Enqueues one step of a batch of nmem members (host descriptors, passed by
-// value) with tiles th rows high; tiles is the device tile table (unused for
-// one member, whose grid is nbx x nby). Returns the number of kernel launches.
+// value) with strips th rows high; tiles is the device strip table (unused
+// for one member, whose strips are nbx x nby in row order); queue is the
+// launches' strip queue (2 words, zero between launches). Returns the number
+// of kernel launches.
 int fp32_batch_step(int sch, int th, const MemberDesc* desc, int nmem, const int4* tiles, int ntiles, int nbx,
-                    int nby, int* counter, cudaStream_t st, Timers* tm);
+                    int nby, int* counter, unsigned* queue, cudaStream_t st, Timers* tm);
+// Shared-memory limits and occupancy of every FP32 kernel on the current
+// device; called before any step can be captured into a graph.
+void fp32_prepare();
+// Bytes of a member's tensor-map table, and writing it (after the buffers
+// exist; rewritten when the tracer buffers are made). False if the driver
+// does not provide the tensor-map encoder or refuses a map.
+size_t fp32_map_bytes();
+bool fp32_write_maps(void* d_maps, const Fp32Ctx& c, const Fp32Engine& e, cudaStream_t st);
 
 // FP32 shadow (pitch P) of an FP64 padded field (pitch nx+4), all padded cells.
 void fp32_shadow(float* dst, const double* src, int nx, int ny, int P, cudaStream_t st);

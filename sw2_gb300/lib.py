@@ -329,10 +329,10 @@ class Solver:
 
 class Batch:
     """Several SW2G_FP32 solvers stepped together (sw2g_batch_*): one launch
-    per phase over all members' tiles, time loop replayed as a CUDA graph."""
+    per phase over all members' strips, time loop replayed as a CUDA graph."""
 
     SCHEDULES = ("rows", "columns", "interleaved", "bands")
-    TILE_ROWS = (4, 8, 16)  # tile shapes: 32 cells wide, this many rows high
+    TILE_ROWS = (16, 32, 64)  # strip shapes: 128 cells wide, this many rows high
 
     def __init__(self, solvers):
         L = load()

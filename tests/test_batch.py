@@ -71,9 +71,10 @@ def test_tuning_changes_no_result():
 
 @pytest.mark.parametrize("tile_rows", lib.Batch.TILE_ROWS)
 def test_every_tile_shape_gives_the_same_bits(tile_rows):
-    """Each face is computed by the tile that needs it with the same
-    operations whatever the tile's height, so every shape and schedule, also
-    changed between steps, ends where the member stepped alone ends."""
+    """Each face is computed with the same operations wherever it is
+    evaluated (carried down a strip or recomputed at a strip's first row), so
+    every strip height and schedule, also changed between steps, ends where
+    the member stepped alone ends."""
     cs = members(seed=9)
     ss = []
     for c in cs:
