@@ -243,6 +243,15 @@ __device__ __forceinline__ void put1(T* f, int pitch, int nx, int ny, int i, int
   }
 }
 
+// The lane's cells near an edge, with their images.
+template <Img M, int OFF, typename T>
+__device__ __forceinline__ void put4_edge(T* f, int pitch, int nx, int ny, int i, int j, T v0, T v1, T v2, T v3) {
+  if (i <= nx) put1<M, OFF>(f, pitch, nx, ny, i, j, v0);
+  if (i + 1 <= nx) put1<M, OFF>(f, pitch, nx, ny, i + 1, j, v1);
+  if (i + 2 <= nx) put1<M, OFF>(f, pitch, nx, ny, i + 2, j, v2);
+  if (i + 3 <= nx) put1<M, OFF>(f, pitch, nx, ny, i + 3, j, v3);
+}
+
 // The four cells (i..i+3, j) of a lane with their images; cells beyond nx
 // are not written. Cells with no images are stored with vector stores.
 template <Img M, int OFF, typename T>
@@ -261,9 +270,7 @@ __device__ __forceinline__ void put4(T* f, int pitch, int nx, int ny, int i, int
     }
     return;
   }
-#pragma unroll
-  for (int c = 0; c < 4; c++)
-    if (i + c <= nx) put1<M, OFF>(f, pitch, nx, ny, i + c, j, v[c]);
+  put4_edge<M, OFF, T>(f, pitch, nx, ny, i, j, v[0], v[1], v[2], v[3]);
 }
 
 // FP64 values of the lane's four cells (pitch W); cells beyond nx read 0.
@@ -379,14 +386,20 @@ struct Ring {
 template <int D>
 __host__ __device__ constexpr int bar_bytes() { return (NWARP * D * 8 + 127) / 128 * 128; }
 
-// Carves the warp's ring out of the block's dynamic shared memory and
-// initialises its barriers (one arrival each: the expect_tx of lane 0).
+// The block's dynamic shared memory from its first 128-byte boundary.
+__device__ __forceinline__ unsigned char* smem_base(unsigned char* sm) {
+  return sm + ((128u - (smem_u32(sm) & 127u)) & 127u);
+}
+
+// Carves the warp's ring out of the block's dynamic shared memory (the
+// blocks' barriers of this ring at bar_off, their rows at row_off, both
+// byte offsets from smem_base) and initialises its barriers (one arrival
+// each: the expect_tx of lane 0).
 template <int NF, int D>
-__device__ __forceinline__ void ring_init(unsigned char* sm, Ring<NF, D>& r) {
+__device__ __forceinline__ void ring_init_at(unsigned char* a, int bar_off, int row_off, Ring<NF, D>& r) {
   const int w = threadIdx.x >> 5;
-  unsigned char* a = sm + ((128u - (smem_u32(sm) & 127u)) & 127u);
-  r.bar = reinterpret_cast<unsigned long long*>(a) + w * D;
-  r.buf = reinterpret_cast<float*>(a + bar_bytes<D>()) + w * D * NF * RS;
+  r.bar = reinterpret_cast<unsigned long long*>(a + bar_off) + w * D;
+  r.buf = reinterpret_cast<float*>(a + row_off) + w * D * NF * RS;
   r.base = 0;
   r.issued = 0;
   if (lane_id() == 0) {
@@ -395,6 +408,10 @@ __device__ __forceinline__ void ring_init(unsigned char* sm, Ring<NF, D>& r) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncwarp();
+}
+template <int NF, int D>
+__device__ __forceinline__ void ring_init(unsigned char* sm, Ring<NF, D>& r) {
+  ring_init_at(smem_base(sm), 0, bar_bytes<D>(), r);
 }
 
 // Starts a strip: the first min(D, T) rows. The slots were last read with
@@ -447,6 +464,34 @@ __device__ __forceinline__ void ring_end(Ring<NF, D>& r) {
   r.base += r.T;
 }
 
+// ------------------------------------------------ own-cell staging (cp.async)
+// The own-cell inputs of a row (FP64 state, FP32 histories) are copied by
+// each lane into a per-warp double-buffered staging area with cp.async one
+// row ahead, and each lane waits for its own copies a row later
+// (cp.async.wait_group): the loads are issued a full row before their use
+// without holding registers.
+__device__ __forceinline__ void cpa16(unsigned dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+// 8 bytes, or 8 zero bytes (nothing read) when !ok
+__device__ __forceinline__ void cpa8(unsigned dst, const void* src, bool ok) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(ok ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cpa4(unsigned dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cpa_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// The lane's four FP64 cells of row j (pitch W), cells beyond nx as zeros.
+__device__ __forceinline__ void cpa_d4(unsigned dst, const double* f, int W, int nx, int i, int j) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const bool ok = (i + c <= nx);
+    cpa8(dst + 8 * c, ok ? f + IX(W, i + c, j) : f, ok);
+  }
+}
+
 // ------------------------------------------------------------ strip queue
 // Warps take strips in the order of the launch's strip table until none is
 // left; the last warp of the launch to find the queue empty resets it
@@ -467,6 +512,15 @@ __device__ __forceinline__ void warp_done(unsigned* queue) {
 }
 
 // ------------------------------------------- Laplacian pieces (laplacian.c)
+// Operands of the wrapped ZE(0, j) = ZE(nx, j) and DI(nx+1, j) = DI(1, j) at
+// their source columns (only the strips at the seam need them).
+__device__ __forceinline__ float4 ze_source(const float* gU, const float* gV, int P, int nx, int j) {
+  return make_float4(gV[IX32(P, nx + 1, j)], gV[IX32(P, nx, j)], gU[IX32(P, nx, j + 1)], gU[IX32(P, nx, j)]);
+}
+__device__ __forceinline__ float4 di_source(const float* gU, const float* gV, int P, int j) {
+  return make_float4(gU[IX32(P, 1, j)], gU[IX32(P, 0, j)], gV[IX32(P, 1, j)], gV[IX32(P, 1, j - 1)]);
+}
+
 // ZE(i, j) at columns ib-1+k, k = 0..4 (laplacian.c:77-79): zero outside rows
 // 1..ny and beyond column nx; ZE(0, j) is the wrapped ZE(nx, j), evaluated at
 // its source column from the global arrays gU, gV (pitch P). ua, ub: u rows j,
@@ -482,8 +536,8 @@ __device__ __forceinline__ void ze5(const float* q, int nx, int ny, int P, int i
     const int i = ib - 1 + k;
     float v1 = va[k + 2], v0 = va[k + 1], u1 = ub[k + 1], u0 = ua[k + 1];
     if (i == 0) {
-      v1 = gV[IX32(P, nx + 1, j)]; v0 = gV[IX32(P, nx, j)];
-      u1 = gU[IX32(P, nx, j + 1)]; u0 = gU[IX32(P, nx, j)];
+      const float4 g = ze_source(gU, gV, P, nx, j);
+      v1 = g.x; v0 = g.y; u1 = g.z; u0 = g.w;
     }
     const float z = idxv * ((v1 - v0) - idyc * (dxc1 * u1 - dxc0 * u0));
     ze[k] = (rowok && i <= nx) ? z : 0.f;
@@ -504,8 +558,8 @@ __device__ __forceinline__ void di5(const float* q, int nx, int ny, int P, int i
     const int i = ib + k;
     float uc = uj[k + 2], uw = uj[k + 1], vc = vj[k + 2], vs = vjm[k + 2];
     if (i == nx + 1) {
-      uc = gU[IX32(P, 1, jd)]; uw = gU[IX32(P, 0, jd)];
-      vc = gV[IX32(P, 1, jd)]; vs = gV[IX32(P, 1, jd - 1)];
+      const float4 g = di_source(gU, gV, P, jd);
+      uc = g.x; uw = g.y; vc = g.z; vs = g.w;
     }
     const float dv = idxe * ((uc - uw) + idyn * (dxv1 * vc - dxv0 * vs));
     const float dw = (ujm[k + 2] - ujm[k + 1]) * idxew;
@@ -649,13 +703,39 @@ __device__ __forceinline__ bool strip_lap(const MemberDesc& d, const View& vw, i
 }
 
 // ---------------------------------------------------------------- kb_main1
-// Staged rows j0-2 .. j1+2 (ring row t <-> j0-2+t) of: eta shadow, u, v
-// shadows, Lu, Lv, and with EXTRA the winds and the bottom height
-// (UWINDX, VWINDY of sw.h:216-217 and H = eta + depth - hB, sw.h:213).
+// Two rings per warp: rows j0-2 .. j1+2 (ring row t <-> j0-2+t) of the eta,
+// u and v shadows, and with EXTRA the winds and the bottom height (UWINDX,
+// VWINDY of sw.h:216-217 and H = eta + depth - hB, sw.h:213); and rows
+// j0-1 .. j1+1 (ring row t <-> j0-1+t) of the first Laplacian level Lu, Lv,
+// of which row j needs only j and j+1.
+constexpr int kDLapIn = 3;  // depth of the Laplacian-level ring of kb_main1
+template <bool EXTRA>
+__host__ __device__ constexpr int main1_fields() { return EXTRA ? 6 : 3; }
+template <bool EXTRA>
+__host__ __device__ constexpr int main1_bars() {
+  return (NWARP * (kDMain1 + kDLapIn) * 8 + 127) / 128 * 128;
+}
+template <bool EXTRA>
+__host__ __device__ constexpr int main1_lrows() {
+  return main1_bars<EXTRA>() + NWARP * kDMain1 * main1_fields<EXTRA>() * RS * 4;
+}
+// own-cell staging of a warp: two rows of [eta (32 lanes x 4 doubles), h1, h2 (32 x 4 floats)]
+constexpr int kStageMain1 = 2 * 2048;
+template <bool EXTRA>
+__host__ __device__ constexpr int main1_stage() {
+  return main1_lrows<EXTRA>() + NWARP * kDLapIn * 2 * RS * 4;
+}
+
+// Sections of a row are separated by a compiler fence, so that windows are
+// read again from shared memory where a section needs them instead of being
+// held in registers across the row.
+__device__ __forceinline__ void section() { asm volatile("" ::: "memory"); }
+
 template <int SCH, bool EXTRA>
 __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw, int sx, int sy, int SR,
-                                            Ring<EXTRA ? 8 : 5, kDMain1>& rg, bool test) {
-  enum { FE, FU, FV, FLU, FLV, FWX, FWY, FHB };
+                                            Ring<main1_fields<EXTRA>(), kDMain1>& rg, Ring<2, kDLapIn>& rl,
+                                            unsigned stg, bool test) {
+  enum { FE, FU, FV, FWX, FWY, FHB };
   const int nx = d.nx, ny = d.ny, P = d.P, W = nx + 4;
   const float* q = d.q;
   const int i0 = sx * SW + 1, j0 = sy * SR + 1, j1 = min(j0 + SR - 1, ny);
@@ -664,8 +744,6 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
   rg.map[FE] = map_of(d, TM_ES + vw.cur);
   rg.map[FU] = map_of(d, TM_US + vw.cur);
   rg.map[FV] = map_of(d, TM_VS + vw.cur);
-  rg.map[FLU] = map_of(d, TM_LU);
-  rg.map[FLV] = map_of(d, TM_LV);
   if constexpr (EXTRA) {
     rg.map[FWX] = map_of(d, TM_WX);
     rg.map[FWY] = map_of(d, TM_WY);
@@ -674,9 +752,16 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
   rg.x = sx * SW;
   rg.y0 = j0 - 1;  // tensor row of j0 - 2
   rg.T = j1 - j0 + 5;
+  rl.map[0] = map_of(d, TM_LU);
+  rl.map[1] = map_of(d, TM_LV);
+  rl.x = sx * SW;
+  rl.y0 = j0;  // tensor row of j0 - 1
+  rl.T = j1 - j0 + 3;
   ring_begin(rg);
+  ring_begin(rl);
   for (int t = 0; t < 4; t++)
     if (!ring_wait(rg, t, bad)) return false;
+  if (!ring_wait(rl, 0, bad) || !ring_wait(rl, 1, bad)) return false;
   if (test && !ring_test(rg, d.tile_test, bad)) return false;
 
   // windows of the stencil fields, with the winds added to u, v and the
@@ -726,8 +811,8 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
 #pragma unroll
     for (int c = 0; c < 4; c++) ysv[c] = face2_shared<SCH>(a[c], vb[c], cc[c], dd[c]);
     float la[8], lb[8], ma[8], mb[8], zt[5];
-    win8(rg.row(1, FLU), la); win8(rg.row(2, FLU), lb);
-    win8(rg.row(1, FLV), ma); win8(rg.row(2, FLV), mb);
+    win8(rl.row(0, 0), la); win8(rl.row(1, 0), lb);
+    win8(rl.row(0, 1), ma); win8(rl.row(1, 1), mb);
     ze5(q, nx, ny, P, ib, jm, la, lb, ma, d.Lu, d.Lv, zt);
 #pragma unroll
     for (int c = 0; c < 4; c++) zm[c] = zt[c + 1];
@@ -745,36 +830,44 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
   const int kab = vw.k;
   float mxu = 0.f, mxv = 0.f;
   bool oor = false;
-  // own-cell inputs of the next row, loaded a row ahead
-  double eo[4];
-  float4 g1 = make_float4(0.f, 0.f, 0.f, 0.f), g2 = g1;
-  ld4d(eta_in, W, nx, ib, j0, eo);
-  if (kab >= 1) g1 = ld4f(h1p, P, ib, j0);
-  if (kab >= 2) g2 = ld4f(h2p, P, ib, j0);
+  // own-cell inputs of a row, staged a row ahead (slot k & 1 of the row j0 + k)
+  const int l = lane_id();
+  auto stage = [&](int jr, int slot) {
+    const unsigned b = stg + slot * 2048;
+    cpa_d4(b + l * 32, eta_in, W, nx, ib, jr);
+    if (kab >= 1) cpa16(b + 1024 + l * 16, h1p + IX32(P, ib, jr));
+    if (kab >= 2) cpa16(b + 1536 + l * 16, h2p + IX32(P, ib, jr));
+  };
+  stage(j0, 0);
+  cpa_commit();
 
   for (int j = j0; j <= j1; j++) {
-    const int k = j - j0, t = k + 2;  // ring row of j
+    const int k = j - j0, t = k + 2;  // ring row of j (the Laplacian ring: k + 1)
     ring_refill(rg, k);
-    if (!ring_wait(rg, t + 2, bad)) return false;
-    float h1[4], h2[4];
-    double ec[4];
-    arr(g1, h1); arr(g2, h2);
-#pragma unroll
-    for (int c = 0; c < 4; c++) ec[c] = eo[c];
-    if (j < j1) {
-      ld4d(eta_in, W, nx, ib, j + 1, eo);
-      if (kab >= 1) g1 = ld4f(h1p, P, ib, j + 1);
-      if (kab >= 2) g2 = ld4f(h2p, P, ib, j + 1);
+    ring_refill(rl, k);
+    if (j < j1) stage(j + 1, (k + 1) & 1);
+    cpa_commit();
+    if (!ring_wait(rg, t + 2, bad) || !ring_wait(rl, k + 2, bad)) {
+      cpa_wait0();
+      return false;
     }
-    bool valid[4];
+    cpa_wait1();  // this lane's copies of row j
+    float h1[4] = {0.f, 0.f, 0.f, 0.f}, h2[4] = {0.f, 0.f, 0.f, 0.f};
+    double ec[4];
+    {
+      const unsigned b = stg + (k & 1) * 2048;
 #pragma unroll
-    for (int c = 0; c < 4; c++) valid[c] = (ib + c <= nx);
+      for (int c = 0; c < 4; c++) {
+        asm volatile("ld.shared.f64 %0, [%1];" : "=d"(ec[c]) : "r"(b + l * 32 + 8 * c) : "memory");
+      }
+      if (kab >= 1) asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(h1[0]), "=f"(h1[1]), "=f"(h1[2]), "=f"(h1[3]) : "r"(b + 1024 + l * 16) : "memory");
+      if (kab >= 2) asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(h2[0]), "=f"(h2[1]), "=f"(h2[2]), "=f"(h2[3]) : "r"(b + 1536 + l * 16) : "memory");
+    }
 
     // ---- mass (BODYH, calc.c:70-113), H relative to the row reference Hb(j)
-    float e0[8], u0[8], vm[8], v0[8];
-    E8(t, e0); U8(t, u0); V8(t - 1, vm); V8(t, v0);
     {
-      float em[4], e1[4], e2[4];
+      float e0[8], u0[8], vm[4], v0[4], em[4], e1[4], e2[4];
+      E8(t, e0); U8(t, u0); V4(t - 1, vm); V4(t, v0);
       E4(t - 1, em); E4(t + 1, e1); E4(t + 2, e2);
       const float kx = Qr(q, Q_KXE, j), ky = Qr(q, Q_KYN, j), hb = Qr(q, Q_HB, j), eref = Qr(q, Q_EREF, j);
       const float geo = Qr(q, Q_GEO, j), dm1 = Qr(q, Q_DHBM1, j), dp1 = Qr(q, Q_DHBP1, j), dp2 = Qr(q, Q_DHBP2, j);
@@ -789,36 +882,42 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
       for (int c = 0; c < 4; c++) {
         float2 fs = ysm[c];
         fs.y += dm1;  // the south face's upwind value relative to Hb(j)
-        const float2 fn = face1_shared<SCH>(em[c] + dm1, e0[c + 2], e1[c] + dp1, e2[c] + dp2, v0[c + 2] > 0.f);
+        const float2 fn = face1_shared<SCH>(em[c] + dm1, e0[c + 2], e1[c] + dp1, e2[c] + dp2, v0[c] > 0.f);
         ysm[c] = fn;
-        const float cw = u0[c + 1] * kx, ce = u0[c + 2] * kx, cs = vm[c + 2] * ky, cn = v0[c + 2] * ky;
+        const float cw = u0[c + 1] * kx, ce = u0[c + 2] * kx, cs = vm[c] * ky, cn = v0[c] * ky;
         float de = (fx[c] - fx[c + 1]) + (face1_term(fs, cs) - face1_term(fn, cn));
         de = fmaf(hb, (cw - ce) + (cs - cn), de);
         de = fmaf(-sig2dt, eref + (EXTRA ? eraw[c] : e0[c + 2]), de);
         // Adams-Bashforth (calc.c:651-699) then the geofactor (calc.c:403-422)
         float ab = ab3(kab, de, h1[c], h2[c]);
-        ab = fmaf(-(geo * (hb + e0[c + 2])), 0.5f * (v0[c + 2] + vm[c + 2]), ab);
+        ab = fmaf(-(geo * (hb + e0[c + 2])), 0.5f * (v0[c] + vm[c]), ab);
         hist[c] = de;
         en[c] = ec[c] + f2d(ab);
         esn[c] = d2f(en[c]);
-        oor = oor || (valid[c] && !in_range(en[c]));
+        oor = oor || ((ib + c <= nx) && !in_range(en[c]));
       }
       st4f(hw, P, ib, j, hist);
       put4<IMG_ETA, 1>(eta_out, W, nx, ny, ib, j, en);
       put4<IMG_ETA, 3>(es_out, P, nx, ny, ib, j, esn);
     }
+    section();
 
-    // ---- second Laplacian level of (u, v) from L (laplacian.c:51-111)
-    float llu[4], llv[4], lc[4], mc[4];
+    // ---- second Laplacian level of (u, v) from L (laplacian.c:51-111),
+    // and the hyperviscosity terms nu2*Dt*L + nu4*Dt*LL of both tendencies
+    float visu[4], visv[4];
     {
-      float la[8], lb[8], ma[8], mb[8], zj[5], dn[5];
-      win8(rg.row(t, FLU), la); win8(rg.row(t + 1, FLU), lb);
-      win8(rg.row(t, FLV), ma); win8(rg.row(t + 1, FLV), mb);
+      float la[8], lb[8], ma[8], mb[8], zj[5], dn[5], llu[4], llv[4];
+      win8(rl.row(k + 1, 0), la); win8(rl.row(k + 2, 0), lb);
+      win8(rl.row(k + 1, 1), ma); win8(rl.row(k + 2, 1), mb);
       ze5(q, nx, ny, P, ib, j, la, lb, ma, d.Lu, d.Lv, zj);
       di5(q, nx, ny, P, ib, j + 1, lb, mb, ma, la, d.Lu, d.Lv, dn);
       lap_out4(q, j, zj, zm, dj, dn, llu, llv);
 #pragma unroll
-      for (int c = 0; c < 4; c++) { zm[c] = zj[c + 1]; lc[c] = la[c + 2]; mc[c] = ma[c + 2]; }
+      for (int c = 0; c < 4; c++) {
+        zm[c] = zj[c + 1];
+        visu[c] = fmaf(nu4dt, llu[c], nu2dt * la[c + 2]);
+        visv[c] = fmaf(nu4dt, llv[c], nu2dt * ma[c + 2]);
+      }
 #pragma unroll
       for (int c = 0; c < 5; c++) dj[c] = dn[c];
       if (keep_ll) {  // with its halo images, for the third level
@@ -826,13 +925,12 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
         put4<IMG_LV, 3>(d.LLv, P, nx, ny, ib, j, llv);
       }
     }
+    section();
 
-    float u1[8];
-    U8(t + 1, u1);
     // ---- BODYU (calc.c:168-200)
     {
-      float um[4], u2[4];
-      U4(t - 1, um); U4(t + 2, u2);
+      float u0[8], u1[4], um[4], u2[4], vm[8], v0[8];
+      U8(t, u0); U4(t + 1, u1); U4(t - 1, um); U4(t + 2, u2); V8(t - 1, vm); V8(t, v0);
       const float kc = Qr(q, Q_KXC, j), kv = Qr(q, Q_KYV, j), k2xe = Qr(q, Q_K2XE, j), idxe = Qr(q, Q_IDXE, j);
       float xu[5];
 #pragma unroll
@@ -845,24 +943,24 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
 #pragma unroll
       for (int c = 0; c < 4; c++) {
         const float uc = u0[c + 2];
-        const float2 yn = face2_shared<SCH>(um[c], uc, u1[c + 2], u2[c]);
+        const float2 yn = face2_shared<SCH>(um[c], uc, u1[c], u2[c]);
         const float vs0 = vm[c + 2], vs1 = vm[c + 3], vn0 = v0[c + 2], vn1 = v0[c + 3];
         const float p1 = (xu[c] - xu[c + 1]) +
                          (face2_term(ysu[c], um[c], uc, cpos2(vs0, vs1, kv), cneg2(vs0, vs1, kv)) -
-                          face2_term(yn, uc, u1[c + 2], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv)));
+                          face2_term(yn, uc, u1[c], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv)));
         ysu[c] = yn;
         const float p2 = fmaf(uc * (u0[c + 3] - u0[c + 1]), k2xe, (uc * (0.5f * (vn0 + vn1) - 0.5f * (vs0 + vs1))) * kv);
-        float r = fmaf(-(EXTRA ? uraw[c] : uc), sigdt, p1 + p2);
-        r = fmaf(nu2dt, lc[c], r);
-        du[c] = fmaf(nu4dt, llu[c], r);
-        if (valid[c]) mxu = fmaxf(mxu, fabsf(uc) * idxe);
+        du[c] = fmaf(-(EXTRA ? uraw[c] : uc), sigdt, p1 + p2) + visu[c];
+        if (ib + c <= nx) mxu = fmaxf(mxu, fabsf(uc) * idxe);
       }
       st4f(d.dup, P, ib, j, du);
     }
+    section();
+
     // ---- BODYV (calc.c:205-237)
     {
-      float v1[4], v2[4];
-      V4(t + 1, v1); V4(t + 2, v2);
+      float v0[8], vm[4], v1[4], v2[4], u0[8], u1[8];
+      V8(t, v0); V4(t - 1, vm); V4(t + 1, v1); V4(t + 2, v2); U8(t, u0); U8(t + 1, u1);
       const float kxv = Qr(q, Q_KXV, j), kyc = Qr(q, Q_KYC, j), kdyns = Qr(q, Q_KDYNS, j), idyn = Qr(q, Q_IDYN, j);
       float xv[5];
 #pragma unroll
@@ -874,7 +972,7 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
       float dv[4];
 #pragma unroll
       for (int c = 0; c < 4; c++) {
-        const float vsm = vm[c + 2], vc = v0[c + 2], vnp = v1[c];
+        const float vsm = vm[c], vc = v0[c + 2], vnp = v1[c];
         const float2 yn = face2_shared<SCH>(vsm, vc, vnp, v2[c]);
         const float p1 = (xv[c] - xv[c + 1]) +
                          (face2_term(ysv[c], vsm, vc, cpos2(vsm, vc, kyc), cneg2(vsm, vc, kyc)) -
@@ -882,15 +980,16 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
         ysv[c] = yn;
         const float uw1 = u1[c + 1], uw0 = u0[c + 1], ue1 = u1[c + 2], ue0 = u0[c + 2];
         const float p2 = fmaf(vc * (0.5f * (ue0 + ue1) - 0.5f * (uw0 + uw1)), kxv, (vc * (vnp - vsm)) * kdyns);
-        float r = fmaf(-(EXTRA ? vraw[c] : vc), sigdt, p1 + p2);
-        r = fmaf(nu2dt, mc[c], r);
-        dv[c] = fmaf(nu4dt, llv[c], r);
-        if (valid[c]) mxv = fmaxf(mxv, fabsf(vc) * idyn);
+        dv[c] = fmaf(-(EXTRA ? vraw[c] : vc), sigdt, p1 + p2) + visv[c];
+        if (ib + c <= nx) mxv = fmaxf(mxv, fabsf(vc) * idyn);
       }
       st4f(d.dvp, P, ib, j, dv);
     }
+    section();
   }
   ring_end(rg);
+  ring_end(rl);
+  cpa_wait0();
   flush_checks(d, vw, mxu, mxv, oor);
   return true;
 }
@@ -1204,13 +1303,13 @@ __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw,
       const int* __restrict__ counter, unsigned* queue
 
 template <int N>
-__global__ void __launch_bounds__(NT) kb_lap1(SW2G_KPARAMS) {
+__global__ void __launch_bounds__(NT, 5) kb_lap1(SW2G_KPARAMS) {
   SW2G_STRIP_LOOP(2, kDLap, (strip_lap<false>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
 // Third Laplacian level (nu6): members without it skip their strips.
 template <int N>
-__global__ void __launch_bounds__(NT) kb_lap3(SW2G_KPARAMS) {
+__global__ void __launch_bounds__(NT, 5) kb_lap3(SW2G_KPARAMS) {
   SW2G_STRIP_LOOP(2, kDLap, (d.nu6dt == 0.f || strip_lap<true>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
@@ -1221,12 +1320,31 @@ __global__ void __launch_bounds__(NT) kb_tracer(SW2G_KPARAMS) {
 }
 
 template <int SCH, bool EXTRA, int N>
-__global__ void __launch_bounds__(NT) kb_main1(SW2G_KPARAMS) {
-  SW2G_STRIP_LOOP(EXTRA ? 8 : 5, kDMain1, (strip_main1<SCH, EXTRA>(d, v, tl.y, tl.z, SR, rg, test)))
+__global__ void __launch_bounds__(NT, EXTRA ? 2 : 3) kb_main1(SW2G_KPARAMS) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  Ring<main1_fields<EXTRA>(), kDMain1> rg;
+  Ring<2, kDLapIn> rl;
+  unsigned char* a = smem_base(sm);
+  ring_init_at(a, 0, main1_bars<EXTRA>(), rg);
+  ring_init_at(a, NWARP * kDMain1 * 8, main1_lrows<EXTRA>(), rl);
+  const unsigned stg = smem_u32(a + main1_stage<EXTRA>() + (threadIdx.x >> 5) * kStageMain1);
+  const int n = *counter;
+  bool first = true;
+  for (;;) {
+    const int s = take_strip(queue);
+    if (s >= nstrips) break;
+    const int4 tl = strip_at<N>(tiles, s, nbx);
+    const MemberDesc& d = ds.m[N == 1 ? 0 : tl.x];
+    const View v = view_of(d, n);
+    const bool test = first && d.tile_test > 0;
+    first = false;
+    if (!strip_main1<SCH, EXTRA>(d, v, tl.y, tl.z, SR, rg, rl, stg, test)) break;
+  }
+  warp_done(queue);
 }
 
 template <int N>
-__global__ void __launch_bounds__(NT) kb_main2(SW2G_KPARAMS) {
+__global__ void __launch_bounds__(NT, 4) kb_main2(SW2G_KPARAMS) {
   SW2G_STRIP_LOOP(3, kDMain2, (strip_main2(d, v, tl.y, tl.z, SR, rg, test)))
 }
 #undef SW2G_STRIP_LOOP
@@ -1239,7 +1357,7 @@ constexpr int smem_bytes() {
 constexpr int kSmemLap = smem_bytes<2, kDLap>();
 constexpr int kSmemMain2 = smem_bytes<3, kDMain2>();
 template <bool EX>
-constexpr int smem_main1() { return smem_bytes<EX ? 8 : 5, kDMain1>(); }
+constexpr int smem_main1() { return 128 + main1_stage<EX>() + NWARP * kStageMain1; }
 template <bool EX>
 constexpr int smem_tracer() { return smem_bytes<EX ? 5 : 3, kDMain1>(); }
 
