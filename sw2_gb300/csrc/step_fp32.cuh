@@ -64,8 +64,8 @@ constexpr int RS = 160;          // floats per ring slot row: 640 bytes, keeping
 constexpr unsigned FULL = 0xffffffffu;
 // Ring depths (staged rows per warp): kb_main1 and kb_tracer read rows j-1..j+2
 // for row j and prefetch one row; kb_main2 reads j..j+1 and prefetches two;
-// the Laplacian kernels, whose rows are short, prefetch four.
-constexpr int kDMain1 = 5, kDMain2 = 4, kDLap = 6;
+// the Laplacian kernels, whose rows are short, prefetch three.
+constexpr int kDMain1 = 5, kDMain2 = 4, kDLap = 5;
 constexpr int NONE = INT_MIN;
 static_assert(ROWB % 16 == 0, "tensor rows are whole 16-byte units");
 static_assert((RS * 4) % 128 == 0 && RS >= BOXW, "tensor copies land on 128-byte boundaries");
@@ -1303,13 +1303,13 @@ __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw,
       const int* __restrict__ counter, unsigned* queue
 
 template <int N>
-__global__ void __launch_bounds__(NT, 5) kb_lap1(SW2G_KPARAMS) {
+__global__ void __launch_bounds__(NT, 6) kb_lap1(SW2G_KPARAMS) {
   SW2G_STRIP_LOOP(2, kDLap, (strip_lap<false>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
 // Third Laplacian level (nu6): members without it skip their strips.
 template <int N>
-__global__ void __launch_bounds__(NT, 5) kb_lap3(SW2G_KPARAMS) {
+__global__ void __launch_bounds__(NT, 6) kb_lap3(SW2G_KPARAMS) {
   SW2G_STRIP_LOOP(2, kDLap, (d.nu6dt == 0.f || strip_lap<true>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
