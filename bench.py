@@ -63,10 +63,15 @@ KERNEL_BYTES = {
     "add": 8 * (2 + 1),
     "cfl": 8 * 2,
     "range": 8 * 1,
-    # FP32 form: FP64 state (8 B), FP32 histories and intermediates (4 B)
-    "f32_lap1": 8 * 2 + 4 * 2,                      # u v -> Lu Lv
-    "f32_main1": 8 * 3 + 4 * 2 + 4 * 2 + 8 + 4 + 4 * 2,  # eta u v, L, 2 hist -> eta, hist, partial Du Dv
-    "f32_main2": 8 * 3 + 4 * 2 + 4 * 4 + 8 * 2 + 4 * 2,  # eta u v, partials, 4 hist -> u v, 2 hist
+    # FP32 form: FP64 state (8 B), FP32 shadows of the state, histories and
+    # intermediates (4 B)
+    "f32_lap1": 4 * 2 + 4 * 2,  # u v shadows -> Lu Lv
+    # eta u v shadows, Lu Lv, eta, 2 eta hist -> eta + shadow, hist, partial Du Dv
+    "f32_main1": 4 * 3 + 4 * 2 + 8 + 4 * 2 + 8 + 4 + 4 + 4 * 2,
+    # new eta shadow, u v, their shadows, partials, 4 hist -> u v + shadows, 2 hist
+    "f32_main2": 4 + 8 * 2 + 4 * 2 + 4 * 2 + 4 * 4 + 8 * 2 + 4 * 2 + 4 * 2,
+    "f32_lap3": 4 * 2 + 4 * 2 + 4 * 2,  # LLu LLv, partials -> partials
+    "f32_tracer": 4 * 3 + 8 + 4 * 2 + 8 + 4 + 4,  # tracer u v shadows, tracer, 2 hist -> tracer + shadow, hist
 }
 # DRAM bytes (read + write) of one launch of the dominant kernels on the
 # 2048x1024 workload, from an ncu capture of the same step (one launch each,
@@ -390,7 +395,7 @@ def ensemble(lib, nsteps, tune_steps, acc_steps, local, seed=7):
     out = {"members": len(cs), "grids": "16 x 512x256, 24 x 1024x512, 24 x 2048x1024",
            "cells_per_step": cells, "steps": nsteps, "value": cells * nsteps / (ms * 1e-3), "unit": UNIT,
            "ms_per_step": ms / nsteps, "launches_per_step": b.last_launches() / nsteps,
-           "schedule": f"32x{b.tile_rows()}/{b.schedule()}", "tune_ms_per_step": tune,
+           "schedule": f"128x{b.tile_rows()}/{b.schedule()}", "tune_ms_per_step": tune,
            "tune_spread": max(tune.values()) / min(tune.values()), "limiter": "Van Leer (r <= 0 -> 0)"}
     b.close()
     if acc_steps > 0:
