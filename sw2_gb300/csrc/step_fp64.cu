@@ -236,8 +236,36 @@ __device__ __forceinline__ double mass_cell(const DevState& s, const F7& f, int 
   return acc;
 }
 
+// Programmatic dependent launch of the step's kernels: each kernel starts by
+// waiting for the previous kernel of the stream to complete (a no-op for a
+// kernel launched without the attribute) and then lets the next one be
+// scheduled, which happens once all of its own blocks are resident; so a
+// launch's scheduling overlaps the drain of the kernel before it, and no
+// kernel reads or writes memory before its predecessor has finished.
+#define SW2G_PDL_ENTRY()                                            \
+  do {                                                              \
+    asm volatile("griddepcontrol.wait;" ::: "memory");              \
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); \
+  } while (0)
+
+template <typename... KArgs, typename... Args>
+void pdl_launch(void (*k)(KArgs...), dim3 g, dim3 b, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = g;
+  cfg.blockDim = b;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
+
 template <int SCH>
 __global__ void k_mass(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   out[IX(W, i, j)] = mass_cell<SCH>(s, f, i, j);
 }
@@ -245,6 +273,7 @@ __global__ void k_mass(DevState s, F7 f, double* out) {
 // BODYTRACER (calc.c:117-163)
 template <int SCH>
 __global__ void k_tracer(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const double Dt = s.Dt, dxe = RW(s, R_DXE, j), dyn = RW(s, R_DYN, j);
   double qx[5], qy[5];
@@ -281,6 +310,7 @@ __device__ __forceinline__ double advu_cell(const DevState& s, const F7& f, int 
 
 template <int SCH>
 __global__ void k_adv_u(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   out[IX(W, i, j)] = advu_cell<SCH>(s, f, i, j);
 }
@@ -304,6 +334,7 @@ __device__ __forceinline__ double advv_cell(const DevState& s, const F7& f, int 
 
 template <int SCH>
 __global__ void k_adv_v(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   out[IX(W, i, j)] = advv_cell<SCH>(s, f, i, j);
 }
@@ -566,6 +597,7 @@ __device__ __forceinline__ void strips_done(unsigned* q, int lane) {
 // BODYH + damping, fast form.
 template <int SCH, bool PL, bool UD>
 __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_mass_fast(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   const double damp = 2.0 * Dt * (s.sigma);  // calc.c:112: (2.0*Dt*sigma)*ETA
@@ -616,6 +648,7 @@ __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_mass_fast(DevS
 // BODYU, fast form.
 template <int SCH, bool PL>
 __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_adv_u_fast(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   FAST_SETUP
   const int ic1 = min(i + 1, nx + 2);
   // U at this lane's column, rows j-1 .. j+1, and V at columns i, i+1 of row j-1
@@ -673,6 +706,7 @@ __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_adv_u_fast(Dev
 // BODYV, fast form.
 template <int SCH, bool PL>
 __global__ void __launch_bounds__(32 * FWARPS, FAST_MIN_BLOCKS) k_adv_v_fast(DevState s, F7 f, double* out) {
+  SW2G_PDL_ENTRY();
   FAST_SETUP
   const int iu = min(i - 1, nx + 2);
   // V at this lane's column, rows j-1 .. j+1; U at column i-1, row j
@@ -848,6 +882,7 @@ __global__ void k_check_add(long long samples, unsigned long long seed, unsigned
 
 // do_AdamsBashforth (calc.c:651-699) via copy_scaf/linop_scaf (sppde_core.c:247-298)
 __global__ void k_ab(DevState s, int k, double* ab, const double* dn, const double* dm1, const double* dm2) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   if (k == 0) {
@@ -862,6 +897,7 @@ __global__ void k_ab(DevState s, int k, double* ab, const double* dn, const doub
 
 // forall x += dx (core.c:175-177, 203-205)
 __global__ void k_add(DevState s, double* x, const double* dx) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   x[q] = x[q] + dx[q];
@@ -937,6 +973,7 @@ __device__ __forceinline__ void put_images(const DevState& s, double* f, int i, 
 
 // laplacian_eta first pass (laplacian.c:120-123)
 __global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* xi) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   psi[q] = div_rcp(RW(s, R_KX, j) * (e[IX(W, i + 1, j)] - e[q]), RW(s, R_DXC, j), RW(s, R_IDXC, j));
@@ -946,6 +983,7 @@ __global__ void k_lape_pass1(DevState s, const double* e, double* psi, double* x
 // laplacian_eta second pass (laplacian.c:125-127)
 // (with its halo update and wall rows written from here, laplacian.c:129-146)
 __global__ void k_lape_pass2(DevState s, const double* psi, const double* xi, double* eo) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double v =
@@ -991,6 +1029,7 @@ __device__ __forceinline__ double hyper_terms(const DevState& s, double x, const
 
 template <int NZ>
 __global__ void k_hyper_add(DevState s, double* d, const double* l2, const double* l4, const double* l6) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   d[q] = hyper_terms<NZ>(s, d[q], l2, l4, l6, q);
@@ -1006,19 +1045,20 @@ void hyper_add(const DevState& s, dim3 g, cudaStream_t st, double* d, const doub
                const double* l6) {
   const int m = (s.nu2dt != 0.0 ? 1 : 0) | (s.nu4dt != 0.0 ? 2 : 0) | (s.nu6dt != 0.0 ? 4 : 0);
   switch (m) {
-    case 0: k_hyper_add<0><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    case 1: k_hyper_add<1><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    case 2: k_hyper_add<2><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    case 3: k_hyper_add<3><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    case 4: k_hyper_add<4><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    case 5: k_hyper_add<5><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    case 6: k_hyper_add<6><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
-    default: k_hyper_add<7><<<g, TX, 0, st>>>(s, d, l2, l4, l6); break;
+    case 0: pdl_launch(k_hyper_add<0>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    case 1: pdl_launch(k_hyper_add<1>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    case 2: pdl_launch(k_hyper_add<2>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    case 3: pdl_launch(k_hyper_add<3>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    case 4: pdl_launch(k_hyper_add<4>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    case 5: pdl_launch(k_hyper_add<5>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    case 6: pdl_launch(k_hyper_add<6>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
+    default: pdl_launch(k_hyper_add<7>, dim3(g), dim3(TX), st, s, d, l2, l4, l6); break;
   }
 }
 
 // do_eta_geofactor (calc.c:403-422)
 __global__ void k_geofactor(DevState s, F7 f, double* ab) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   ab[q] -= (RW(s, R_GEO, j) * HH(i, j) * 0.5 * (VW(i, j) + VW(i, j - 1)));
@@ -1032,6 +1072,7 @@ __device__ __noinline__ double minus_damping(double x, double U, double sigma, d
 // only where the sum is zero or an operand is not finite.
 template <bool UD>
 __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* dvadv, double* dun, double* dvn) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double* e = f.eta;
@@ -1063,6 +1104,7 @@ __global__ void k_pres_sum(DevState s, F7 f, const double* duadv, const double* 
 // 2048x1024) keep enough threads in flight for the integer-pipe additions.
 constexpr int LV_ROWS = 4;
 __global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, double* ze, double* di) {
+  SW2G_PDL_ENTRY();
   const int W = s.W;
   const int i = blockIdx.x * TX + threadIdx.x + 1;
   const int j0 = blockIdx.y * LV_ROWS + 1;
@@ -1091,6 +1133,7 @@ __global__ void k_lapv_pass1(DevState s, const double* uu, const double* vv, dou
 // laplacian_vels second pass (laplacian.c:83-89)
 // (with the halo update and wall fixes of lu and lv written from here, laplacian.c:91-107)
 __global__ void k_lapv_pass2(DevState s, const double* ze, const double* di, double* lu, double* lv) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   double a = -RW(s, R_IDYN, j), b = RW(s, R_IDXC, j);
@@ -1105,6 +1148,7 @@ __global__ void k_lapv_pass2(DevState s, const double* ze, const double* di, dou
 
 // solve_Coriolis_u (calc.c:542-569), in place
 __global__ void k_coriolis_u(DevState s, double* u, const double* v, const double* duab) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double semi = 0.25 * (v[IX(W, i, j)] + v[IX(W, i + 1, j)] + v[IX(W, i, j - 1)] + v[IX(W, i + 1, j - 1)]);
@@ -1116,6 +1160,7 @@ __global__ void k_coriolis_u(DevState s, double* u, const double* v, const doubl
 
 // solve_Coriolis_v (calc.c:571-598), in place, reading the new u interior
 __global__ void k_coriolis_v(DevState s, const double* u, double* v, const double* dvab) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double semi = 0.25 * (u[IX(W, i - 1, j + 1)] + u[IX(W, i, j + 1)] + u[IX(W, i, j)] + u[IX(W, i - 1, j)]);
@@ -1158,6 +1203,7 @@ __device__ __forceinline__ void check_range(int* bad, double x, int i, int j) {
 template <int NZ, bool PL>
 __global__ void k_eta_ab3(DevState s, F7 f, double* eta, double* dn, const double* dm1, const double* dm2,
                           const double* l2, const double* l4, const double* l6, int* bad) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
@@ -1179,6 +1225,7 @@ template <int NZ>
 __global__ void k_coriolis_u_ab3(DevState s, double* u, const double* v, double* dn, const double* dm1,
                                  const double* dm2, const double* l2, const double* l4, const double* l6,
                                  int* bad) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
@@ -1198,6 +1245,7 @@ template <int NZ>
 __global__ void k_coriolis_v_ab3(DevState s, const double* u, double* v, double* dn, const double* dm1,
                                  const double* dm2, const double* l2, const double* l4, const double* l6,
                                  int* bad) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const double x = hyper_terms<NZ>(s, dn[q], l2, l4, l6, q);
@@ -1219,16 +1267,16 @@ template <int NZ>
 void fused_tails(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buffers& b, int which, int* bad) {
   if (which == 0) {
     if (s.plain)
-      k_eta_ab3<NZ, true><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2],
+      pdl_launch(k_eta_ab3<NZ, true>, dim3(g), dim3(TX), st, s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1], b.Le[2],
                                             bad);
     else
-      k_eta_ab3<NZ, false><<<g, TX, 0, st>>>(s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1],
+      pdl_launch(k_eta_ab3<NZ, false>, dim3(g), dim3(TX), st, s, f, b.f[0], b.deta[0], b.deta[1], b.deta[2], b.Le[0], b.Le[1],
                                              b.Le[2], bad);
   } else if (which == 1) {
-    k_coriolis_u_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.du[0], b.du[1], b.du[2], b.L[0], b.L[2], b.L[4],
+    pdl_launch(k_coriolis_u_ab3<NZ>, dim3(g), dim3(TX), st, s, b.f[1], b.f[2], b.du[0], b.du[1], b.du[2], b.L[0], b.L[2], b.L[4],
                                            bad);
   } else {
-    k_coriolis_v_ab3<NZ><<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dv[0], b.dv[1], b.dv[2], b.L[1], b.L[3], b.L[5],
+    pdl_launch(k_coriolis_v_ab3<NZ>, dim3(g), dim3(TX), st, s, b.f[1], b.f[2], b.dv[0], b.dv[1], b.dv[2], b.L[1], b.L[3], b.L[5],
                                            bad);
   }
 }
@@ -1252,6 +1300,7 @@ void fused_tail(const DevState& s, dim3 g, cudaStream_t st, const F7& f, Fp64Buf
 // compose to: every halo cell copies the interior cell (wrapx(i), wrapy(j)).
 // blockIdx.y selects the field: one launch wraps x and, when given, y.
 __global__ void k_halo(double* x, double* y, int nx, int ny) {
+  SW2G_PDL_ENTRY();
   const int W = nx + 4;
   const int nh = 4 * W + 4 * ny;  // 4 full halo rows + 4 halo columns over interior rows
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1275,6 +1324,7 @@ __global__ void k_halo(double* x, double* y, int nx, int ny) {
 
 // do_channel (calc.c:600-649), polar 0: interior columns of the wall rows
 __global__ void k_channel(int nx, int ny, double* u, double* v, double* wx, double* wy) {
+  SW2G_PDL_ENTRY();
   const int W = nx + 4;
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   if (i > nx) return;
@@ -1303,6 +1353,7 @@ __device__ __forceinline__ long long mag_bits(double x) {
 // serialise in L2).
 constexpr int CFL_T = 256;
 __global__ void __launch_bounds__(CFL_T) k_cfl(DevState s, F7 f, unsigned long long* out) {
+  SW2G_PDL_ENTRY();
   __shared__ long long red[2][CFL_T / 32];
   const int W = s.W;
   const int j = blockIdx.x + 1;
@@ -1346,6 +1397,7 @@ struct RangeFields {
   int n;
 };
 __global__ void k_range(DevState s, RangeFields r, int* bad) {
+  SW2G_PDL_ENTRY();
   INTERIOR_IJ
   const int q = IX(W, i, j);
   const bool first = (i == 1 && j == 1);
@@ -1390,7 +1442,7 @@ void fast_launch(K kernel, cudaStream_t st, const DevState& s0, const F7& f, dou
   s.fk = choose_strip_rows(s.nx, s.ny, full * FWARPS);
   const long long strips = (long long)((s.nx + FW - 1) / FW) * ((s.ny + s.fk - 1) / s.fk);
   const long long need = (strips + FWARPS - 1) / FWARPS;
-  kernel<<<(int)(need < full ? need : full), 32 * FWARPS, 0, st>>>(s, f, out);
+  pdl_launch(kernel, dim3((int)(need < full ? need : full)), dim3(32 * FWARPS), st, s, f, out);
 }
 
 template <int SCH>
@@ -1410,10 +1462,10 @@ void launch_bodies(int which, dim3 g, cudaStream_t st, const DevState& s, const 
       if (which == 3) { fast_launch(k_adv_v_fast<SCH, false>, st, s, f, out); return; }
     }
   }
-  if (which == 0) k_mass<SCH><<<g, TX, 0, st>>>(s, f, out);
-  else if (which == 1) k_tracer<SCH><<<g, TX, 0, st>>>(s, f, out);
-  else if (which == 2) k_adv_u<SCH><<<g, TX, 0, st>>>(s, f, out);
-  else k_adv_v<SCH><<<g, TX, 0, st>>>(s, f, out);
+  if (which == 0) pdl_launch(k_mass<SCH>, dim3(g), dim3(TX), st, s, f, out);
+  else if (which == 1) pdl_launch(k_tracer<SCH>, dim3(g), dim3(TX), st, s, f, out);
+  else if (which == 2) pdl_launch(k_adv_u<SCH>, dim3(g), dim3(TX), st, s, f, out);
+  else pdl_launch(k_adv_v<SCH>, dim3(g), dim3(TX), st, s, f, out);
 }
 
 void body(int which, int sch, dim3 g, cudaStream_t st, const DevState& s, const F7& f, double* out) {
@@ -1499,12 +1551,12 @@ void fp64_check_division(const double* d_div, int n, long long samples, unsigned
 
 void halo_wrap(double* x, int nx, int ny, cudaStream_t st) {
   const int nh = 4 * (nx + 4) + 4 * ny;
-  k_halo<<<(nh + 255) / 256, 256, 0, st>>>(x, x, nx, ny);
+  pdl_launch(k_halo, dim3((nh + 255) / 256), dim3(256), st, x, x, nx, ny);
 }
 // Two fields in one launch.
 void halo_wrap2(double* x, double* y, int nx, int ny, cudaStream_t st) {
   const int nh = 4 * (nx + 4) + 4 * ny;
-  k_halo<<<dim3((nh + 255) / 256, 2), 256, 0, st>>>(x, y, nx, ny);
+  pdl_launch(k_halo, dim3(dim3((nh + 255) / 256, 2)), dim3(256), st, x, y, nx, ny);
 }
 
 // One reference time step; returns the number of kernels launched.
@@ -1545,9 +1597,9 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     const double* src = s.lape_eta ? b.f[0] : b.f[1];  // the reference passes u, not eta (calc.c:332)
     const int nlap = (s.nu4 != 0 || s.nu6 != 0) ? ((s.nu6 != 0) ? 3 : 2) : 1;
     for (int q = 0; q < nlap; q++) {
-      LAUNCH("lape_pass1", k_lape_pass1<<<g, TX, 0, st>>>(s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
+      LAUNCH("lape_pass1", pdl_launch(k_lape_pass1, dim3(g), dim3(TX), st, s, q == 0 ? src : b.Le[q - 1], b.psi, b.xi));
       // halo and wall rows of Le are written by the pass (a polar cap has no walls)
-      LAUNCH("lape_pass2", k_lape_pass2<<<g, TX, 0, st>>>(s, b.psi, b.xi, b.Le[q]));
+      LAUNCH("lape_pass2", pdl_launch(k_lape_pass2, dim3(g), dim3(TX), st, s, b.psi, b.xi, b.Le[q]));
     }
   };
   // Reading u alone, and nothing that the kernels before their place in the
@@ -1559,15 +1611,15 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
   if (hk.v_in) cudaStreamWaitEvent(st, hk.v_in, 0);
 
   // compute_Dt (core.c:155-159): maxima at the start of the step
-  LAUNCH("cfl", k_cfl<<<s.ny, CFL_T, 0, st>>>(s, F(), chk.cfl + 2 * slot));
+  LAUNCH("cfl", pdl_launch(k_cfl, dim3(s.ny), dim3(CFL_T), st, s, F(), chk.cfl + 2 * slot));
 
   // tracer (core.c:161-182); skipped while the tracer is identically +0, which
   // the step then provably leaves unchanged
   if (tracer) {
     LAUNCH("tracer", body(1, sch, g, st, s, F(), b.dtr[0]));
-    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.dtrAB, b.dtr[0], b.dtr[1], b.dtr[2]));
+    LAUNCH("ab", pdl_launch(k_ab, dim3(g), dim3(TX), st, s, k, b.dtrAB, b.dtr[0], b.dtr[1], b.dtr[2]));
     rotate3(b.dtr);
-    LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[3], b.dtrAB));
+    LAUNCH("add", pdl_launch(k_add, dim3(g), dim3(TX), st, s, b.f[3], b.dtrAB));
     LAUNCH("halo", halo_wrap(b.f[3], s.nx, s.ny, st));
   }
 
@@ -1586,19 +1638,19 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     LAUNCH("eta_ab3", fused_tail(s, g, st, F(), b, 0, fbad));  // writes eta's halo images too
     rotate3(b.deta);
   } else {
-    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
-    LAUNCH("geofactor", k_geofactor<<<g, TX, 0, st>>>(s, F(), b.detaAB));
+    LAUNCH("ab", pdl_launch(k_ab, dim3(g), dim3(TX), st, s, k, b.detaAB, b.deta[0], b.deta[1], b.deta[2]));
+    LAUNCH("geofactor", pdl_launch(k_geofactor, dim3(g), dim3(TX), st, s, F(), b.detaAB));
     rotate3(b.deta);
-    LAUNCH("add", k_add<<<g, TX, 0, st>>>(s, b.f[0], b.detaAB));
+    LAUNCH("add", pdl_launch(k_add, dim3(g), dim3(TX), st, s, b.f[0], b.detaAB));
     LAUNCH("halo", halo_wrap(b.f[0], s.nx, s.ny, st));
   }
   if (hk.eta_out) cudaEventRecord(hk.eta_out, st);  // eta is final for this step
 
   // momentum (core.c:212-280)
   if (s.polar == 0 && s.sigma == 0.0)
-    LAUNCH("pres_sum", k_pres_sum<true><<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
+    LAUNCH("pres_sum", pdl_launch(k_pres_sum<true>, dim3(g), dim3(TX), st, s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
   else
-    LAUNCH("pres_sum", k_pres_sum<false><<<g, TX, 0, st>>>(s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
+    LAUNCH("pres_sum", pdl_launch(k_pres_sum<false>, dim3(g), dim3(TX), st, s, F(), b.duadv, b.dvadv, b.du[0], b.dv[0]));
   if (hyper) {
     // As above: each level rewrites every cell of ze, di and its two L fields
     // (interior, halo wraps, wall fixes), and L of levels not run stay zero.
@@ -1607,8 +1659,8 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
       const double* uu = q == 0 ? b.f[1] : b.L[2 * q - 2];
       const double* vv = q == 0 ? b.f[2] : b.L[2 * q - 1];
       // halos and wall fixes of ze, di and of the outputs are written by the passes
-      LAUNCH("lapv_pass1", k_lapv_pass1<<<dim3(g.x, (s.ny + LV_ROWS - 1) / LV_ROWS), TX, 0, st>>>(s, uu, vv, b.ze, b.di));
-      LAUNCH("lapv_pass2", k_lapv_pass2<<<g, TX, 0, st>>>(s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
+      LAUNCH("lapv_pass1", pdl_launch(k_lapv_pass1, dim3(dim3(g.x, (s.ny + LV_ROWS - 1) / LV_ROWS)), dim3(TX), st, s, uu, vv, b.ze, b.di));
+      LAUNCH("lapv_pass2", pdl_launch(k_lapv_pass2, dim3(g), dim3(TX), st, s, b.ze, b.di, b.L[2 * q], b.L[2 * q + 1]));
     }
     if (k < 2) {
       LAUNCH("hyper_add", hyper_add(s, g, st, b.du[0], b.L[0], b.L[2], b.L[4]));
@@ -1624,14 +1676,14 @@ int step_head(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
     rotate3(b.du);
     rotate3(b.dv);
   } else {
-    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.duAB, b.du[0], b.du[1], b.du[2]));
-    LAUNCH("ab", k_ab<<<g, TX, 0, st>>>(s, k, b.dvAB, b.dv[0], b.dv[1], b.dv[2]));
+    LAUNCH("ab", pdl_launch(k_ab, dim3(g), dim3(TX), st, s, k, b.duAB, b.du[0], b.du[1], b.du[2]));
+    LAUNCH("ab", pdl_launch(k_ab, dim3(g), dim3(TX), st, s, k, b.dvAB, b.dv[0], b.dv[1], b.dv[2]));
     rotate3(b.du);
     rotate3(b.dv);
     // Coriolis (core.c:282-285)
-    LAUNCH("coriolis_u", k_coriolis_u<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.duAB));
+    LAUNCH("coriolis_u", pdl_launch(k_coriolis_u, dim3(g), dim3(TX), st, s, b.f[1], b.f[2], b.duAB));
     if (hk.u_out) cudaEventRecord(hk.u_out, st);
-    LAUNCH("coriolis_v", k_coriolis_v<<<g, TX, 0, st>>>(s, b.f[1], b.f[2], b.dvAB));
+    LAUNCH("coriolis_v", pdl_launch(k_coriolis_v, dim3(g), dim3(TX), st, s, b.f[1], b.f[2], b.dvAB));
   }
 
   // halos (core.c:287-290)
@@ -1648,7 +1700,7 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
   const dim3 g((s.nx + TX - 1) / TX, s.ny);
   const int gw = (s.nx + 127) / 128;
   int nl = 0;
-  if (s.polar == 0) LAUNCH("channel", k_channel<<<gw, 128, 0, st>>>(s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
+  if (s.polar == 0) LAUNCH("channel", pdl_launch(k_channel, dim3(gw), dim3(128), st, s.nx, s.ny, b.f[1], b.f[2], b.f[4], b.f[5]));
 
   // range checks of tracer, eta, u, v (core.c:309-312); an all-zero tracer
   // passes trivially
@@ -1657,7 +1709,7 @@ int step_tail(const DevState& s, Fp64Buffers& b, bool tracer, StepChecks chk, in
   r.f[r.n++] = b.f[0];
   r.f[r.n++] = b.f[1];
   r.f[r.n++] = b.f[2];
-  if (!fused_checks) LAUNCH("range", k_range<<<g, TX, 0, st>>>(s, r, chk.bad + slot));
+  if (!fused_checks) LAUNCH("range", pdl_launch(k_range, dim3(g), dim3(TX), st, s, r, chk.bad + slot));
   return nl;
 }
 #undef LAUNCH

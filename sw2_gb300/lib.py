@@ -380,15 +380,15 @@ class Batch:
         return load().sw2g_batch_last_launches(self.h)
 
     def tune(self, steps_per_candidate: int):
-        """Times every (tile shape, schedule) pair and keeps the fastest;
-        returns {"32xTH/schedule": ms per step}."""
+        """Times every (strip shape, schedule) pair and keeps the fastest;
+        returns {"128xTH/schedule": ms per step}."""
         nc = len(self.TILE_ROWS) * len(self.SCHEDULES)
         ms = (ctypes.c_double * nc)()
         rc = load().sw2g_batch_tune(self.h, int(steps_per_candidate), ms)
         if rc != OK:
             raise SW2GError(rc, "sw2g_batch_tune")
         ns = len(self.SCHEDULES)
-        return {f"32x{th}/{self.SCHEDULES[k]}": ms[i * ns + k] for i, th in enumerate(self.TILE_ROWS)
+        return {f"128x{th}/{self.SCHEDULES[k]}": ms[i * ns + k] for i, th in enumerate(self.TILE_ROWS)
                 for k in range(ns)}
 
     def set_schedule(self, tile_rows: int, schedule: str):
