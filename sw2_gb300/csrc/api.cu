@@ -179,6 +179,8 @@ struct sw2g_ctx {
   int err_step = -1;
   long long last_launches = 0;
   bool open = false;  // between sw2g_step_open and sw2g_step_close
+  int open_slot = 0;  // FP32 form: check slot of the opened step
+  unsigned forced = 0;  // FP32 form, opened step: fields changed by forcing (bit per field)
   // FP32 precision form
   Fp32Engine e32;
   Fp32Ctx c32{};
@@ -928,11 +930,118 @@ static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
   return SW2G_OK;
 }
 
+namespace {
+// The FP64 field a forcing call changes: the reference layout's field, or in
+// the FP32 form its FP64 state (eta as eta - eta_ref(j)).
+double* force_target(sw2g_ctx* x, int which) {
+  if (x->precision == SW2G_FP32) {
+    Fp32Engine& e = x->e32;
+    return which == 0 ? e.eta[e.cur] : which == 1 ? e.u[e.cur] : which == 2 ? e.v[e.cur] : e.tr[e.cur];
+  }
+  return x->b.f[which];
+}
+
+// FP32 form: the FP32 shadow of a field after its FP64 state changed.
+void fp32_reshadow(sw2g_ctx* x, int which) {
+  Fp32Engine& e = x->e32;
+  float* dst = which == 0 ? e.es[e.cur] : which == 1 ? e.us[e.cur] : which == 2 ? e.vs[e.cur] : e.ts[e.cur];
+  fp32_shadow(dst, force_target(x, which), x->s.nx, x->s.ny, x->c32.P, x->stream);
+}
+
+// FP32 form: do_channel (calc.c:600-649) on the FP64 u, v and the winds, then
+// their FP32 shadows.
+void fp32_channel(sw2g_ctx* x) {
+  Fp32Engine& e = x->e32;
+  const int nx = x->s.nx, ny = x->s.ny, P = x->c32.P;
+  fp64_channel(e.u[e.cur], e.v[e.cur], x->d_aux64[0], x->d_aux64[1], nx, ny, x->stream);
+  fp32_reshadow(x, 1);
+  fp32_reshadow(x, 2);
+  fp32_shadow(x->d_aux32[0], x->d_aux64[0], nx, ny, P, x->stream);
+  fp32_shadow(x->d_aux32[1], x->d_aux64[1], nx, ny, P, x->stream);
+}
+
+// FP32 form: one whole step with the plain halo update of u and v (its range
+// flags are not used: the checks come after the forcing).
+sw2g_status fp32_step_open(sw2g_ctx* x) {
+  x->c32.open_step = 1;
+  CK(x->run32.sync_to({fp32_desc(x->c32, x->e32, x->k)}, x->stream));
+  x->c32.open_step = 0;
+  const int slot = x->run32.slot();
+  CK(cudaMemsetAsync(x->e32.cfl + 2 * slot, 0, sizeof(unsigned) * 2, x->stream));
+  CK(cudaMemsetAsync(x->e32.bad + slot, 0, sizeof(int), x->stream));
+  CK(cudaEventRecord(x->ev[0], x->stream));
+  x->last_launches = 0;
+  CK(x->run32.enqueue(1, x->stream, &x->timers, x->last_launches));
+  CK(cudaGetLastError());
+  x->e32.advance_host(1);
+  x->k++;
+  x->open_slot = slot;
+  x->forced = 0;
+  x->open = true;
+  return SW2G_OK;
+}
+
+// FP32 form, after the forcing (core.c:297-312): the halo update of the
+// forced tracer and eta, do_channel, the FP32 shadows of what changed, the
+// range checks of the four fields; then the step's CFL check.
+sw2g_status fp32_step_close(sw2g_ctx* x) {
+  Fp32Engine& e = x->e32;
+  const int nx = x->s.nx, ny = x->s.ny;
+  for (int w : {3, 0})
+    if (x->forced & (1u << w)) {
+      halo_wrap(force_target(x, w), nx, ny, x->stream);
+      fp32_reshadow(x, w);
+    }
+  fp32_channel(x);
+  add_row_ref(x->d_tmp, e.eta[e.cur], x->d_ref, nx, ny, x->stream);  // eta itself, for its range check
+  const double* f[4];
+  int nf = 0;
+  if (e.tracer) f[nf++] = e.tr[e.cur];
+  f[nf++] = x->d_tmp;
+  f[nf++] = e.u[e.cur];
+  f[nf++] = e.v[e.cur];
+  CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int), x->stream));
+  fp64_range(x->s, f, nf, x->d_bad, x->stream);
+  CK(cudaEventRecord(x->ev[1], x->stream));
+  CK(cudaGetLastError());
+  x->open = false;
+  unsigned* const cfl = x->h_cfl32;
+  int* const bad = x->h_bad;
+  CK(cudaMemcpyAsync(cfl, e.cfl + 2 * x->open_slot, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaMemcpyAsync(bad, e.bad + x->open_slot, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaMemcpyAsync(bad + 1, x->d_bad, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
+  x->last_step_ms = ms;
+  if (x->timers.on) x->timers.collect();
+  float a, b2;
+  std::memcpy(&a, &cfl[0], sizeof(float));
+  std::memcpy(&b2, &cfl[1], sizeof(float));
+  double mx = a, my = b2;
+  if (mx + my == 0) { mx = x->rest_mx; my = x->rest_my; }
+  if (x->c.Dt > (x->c.courant / (mx + my))) {  // core.c:158
+    x->err_step = (int)x->steps;
+    return SW2G_ERR_CFL;
+  }
+  x->steps += 1;
+  if (bad[0] & kCheckTimeout) {
+    x->err_step = (int)(x->steps - 1);
+    return SW2G_ERR_TIMEOUT;
+  }
+  if (bad[1]) {
+    x->err_step = (int)(x->steps - 1);
+    return SW2G_ERR_NONFINITE;
+  }
+  return SW2G_OK;
+}
+}  // namespace
+
 sw2g_status sw2g_step_open(sw2g_ctx* x) {
   if (!x) return SW2G_ERR_BAD_ARG;
-  if (x->precision != SW2G_FP64) return SW2G_ERR_BAD_ARG;
   if (!x->uploaded || x->open) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
+  if (x->precision == SW2G_FP32) return fp32_step_open(x);
   CK(cudaMemsetAsync(x->d_cfl, 0, sizeof(unsigned long long) * 2, x->stream));
   CK(cudaMemsetAsync(x->d_bad, 0, sizeof(int), x->stream));
   StepChecks chk{x->d_cfl, x->d_bad};
@@ -948,6 +1057,7 @@ sw2g_status sw2g_step_close(sw2g_ctx* x) {
   if (!x) return SW2G_ERR_BAD_ARG;
   if (!x->open) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
+  if (x->precision == SW2G_FP32) return fp32_step_close(x);
   StepChecks chk{x->d_cfl, x->d_bad};
   x->last_launches += fp64_step(x->s, x->b, x->sch, x->k - 1, x->tracer_active, chk, 0, x->stream, &x->timers,
                                 STEP_TAIL);
@@ -1122,19 +1232,39 @@ sw2g_status sw2g_checkpoint_load(sw2g_ctx* x, const double* buf, size_t n) {
 }
 
 namespace {
-// Forcing calls are for uploaded FP64 contexts; the staging field is
-// allocated on first use.
+// Forcing calls are for uploaded contexts; the staging field is allocated on
+// first use. In the FP32 form a forced tracer is advected from then on.
 sw2g_status force_ready(sw2g_ctx* x, int which) {
   if (!x || which < 0 || which > 3) return SW2G_ERR_BAD_ARG;
-  if (x->precision != SW2G_FP64) return SW2G_ERR_BAD_ARG;
   if (!x->uploaded) return SW2G_ERR_STATE;
   CK(cudaSetDevice(x->device));
   if (!x->d_force) {
     sw2g_status st = dalloc(x, &x->d_force, (size_t)x->s.W * x->s.H);
     if (st != SW2G_OK) return st;
   }
+  if (x->precision == SW2G_FP32 && which == 3 && !x->e32.tracer) {
+    Fp32Engine& e = x->e32;
+    sw2g_status st = tracer_fp32(x);
+    if (st != SW2G_OK) return st;
+    const size_t S = (size_t)x->s.W * x->s.H, S32 = (size_t)x->c32.P * x->c32.R;
+    CK(cudaMemsetAsync(e.tr[e.cur], 0, S * sizeof(double), x->stream));
+    CK(cudaMemsetAsync(e.ts[e.cur], 0, S32 * sizeof(float), x->stream));
+    e.tracer = true;
+  }
   return SW2G_OK;
 }
+
+
+// After a forcing call: the FP32 form refreshes the shadow at once between
+// steps, or at sw2g_step_close inside an opened step.
+void forced_field(sw2g_ctx* x, int which) {
+  if (x->precision != SW2G_FP32) return;
+  if (x->open) x->forced |= 1u << which;
+  else fp32_reshadow(x, which);
+}
+
+// FP32 form, setting eta: the values are heights, the state holds eta - eta_ref(j).
+double eta_ref_of_cell(const sw2g_ctx* x, int q) { return x->ref[q / x->s.W]; }
 }  // namespace
 
 sw2g_status sw2g_add_field(sw2g_ctx* x, int which, const double* delta, double scale) {
@@ -1143,7 +1273,8 @@ sw2g_status sw2g_add_field(sw2g_ctx* x, int which, const double* delta, double s
   if (!delta) return SW2G_ERR_BAD_ARG;
   const size_t S = (size_t)x->s.W * x->s.H;
   CK(cudaMemcpyAsync(x->d_force, delta, S * sizeof(double), cudaMemcpyHostToDevice, x->stream));
-  fp64_add_scaled(x->b.f[which], x->d_force, scale, x->s.nx, x->s.ny, x->stream);
+  fp64_add_scaled(force_target(x, which), x->d_force, scale, x->s.nx, x->s.ny, x->stream);
+  forced_field(x, which);
   CK(cudaGetLastError());
   if (which == 3 && !x->tracer_active) {
     // the tracer step runs once any interior tracer value can be nonzero
@@ -1164,9 +1295,16 @@ sw2g_status sw2g_set_field_where(sw2g_ctx* x, int which, const double* value, co
   if (!value || !mask) return SW2G_ERR_BAD_ARG;
   const size_t S = (size_t)x->s.W * x->s.H;
   if (!x->d_mask) CK(cudaMalloc(&x->d_mask, S));
-  CK(cudaMemcpyAsync(x->d_force, value, S * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  std::vector<double> pert;
+  if (x->precision == SW2G_FP32 && which == 0) {  // heights -> eta - eta_ref(j)
+    pert.resize(S);
+    for (size_t q = 0; q < S; q++) pert[q] = value[q] - eta_ref_of_cell(x, (int)q);
+  }
+  CK(cudaMemcpyAsync(x->d_force, pert.empty() ? value : pert.data(), S * sizeof(double), cudaMemcpyHostToDevice,
+                     x->stream));
   CK(cudaMemcpyAsync(x->d_mask, mask, S, cudaMemcpyHostToDevice, x->stream));
-  fp64_set_where(x->b.f[which], x->d_force, (const unsigned char*)x->d_mask, x->s.nx, x->s.ny, x->stream);
+  fp64_set_where(force_target(x, which), x->d_force, (const unsigned char*)x->d_mask, x->s.nx, x->s.ny, x->stream);
+  forced_field(x, which);
   CK(cudaGetLastError());
   if (which == 3 && !x->tracer_active) {
     for (int j = 1; j <= x->s.ny && !x->tracer_active; j++)
@@ -1251,8 +1389,9 @@ sw2g_status sw2g_add_cells(sw2g_ctx* x, int which, const int* cells, const doubl
   // every interior cell gets field += scale * delta, as the reference's loop
   // over the whole grid does (perturbs.c:308), with delta zero off the list
   fp64_scatter_cells(x->d_delta, x->d_cells, x->d_cellv, n, x->stream);
-  fp64_add_scaled(x->b.f[which], x->d_delta, scale, x->s.nx, x->s.ny, x->stream);
+  fp64_add_scaled(force_target(x, which), x->d_delta, scale, x->s.nx, x->s.ny, x->stream);
   fp64_scatter_cells(x->d_delta, x->d_cells, nullptr, n, x->stream);
+  forced_field(x, which);
   CK(cudaGetLastError());
   tracer_from_list(x, which, values, n);
   return SW2G_OK;
@@ -1261,9 +1400,15 @@ sw2g_status sw2g_add_cells(sw2g_ctx* x, int which, const int* cells, const doubl
 sw2g_status sw2g_set_cells(sw2g_ctx* x, int which, const int* cells, const double* values, int n) {
   sw2g_status st = force_ready(x, which);
   if (st != SW2G_OK) return st;
-  if ((st = stage_cells(x, cells, values, n)) != SW2G_OK) return st;
-  fp64_scatter_cells(x->b.f[which], x->d_cells, x->d_cellv, n, x->stream);
-  halo_wrap(x->b.f[which], x->s.nx, x->s.ny, x->stream);
+  std::vector<double> pert;
+  if (x->precision == SW2G_FP32 && which == 0 && n > 0 && cells && values) {  // heights -> eta - eta_ref(j)
+    pert.resize((size_t)n);
+    for (int k = 0; k < n; k++) pert[k] = values[k] - eta_ref_of_cell(x, cells[k]);
+  }
+  if ((st = stage_cells(x, cells, pert.empty() ? values : pert.data(), n)) != SW2G_OK) return st;
+  fp64_scatter_cells(force_target(x, which), x->d_cells, x->d_cellv, n, x->stream);
+  halo_wrap(force_target(x, which), x->s.nx, x->s.ny, x->stream);
+  forced_field(x, which);
   CK(cudaGetLastError());
   tracer_from_list(x, which, values, n);
   return SW2G_OK;
@@ -1273,7 +1418,11 @@ sw2g_status sw2g_apply_channel(sw2g_ctx* x) {
   sw2g_status st = force_ready(x, 0);
   if (st != SW2G_OK) return st;
   if (x->s.polar != 0) return SW2G_OK;  // periodic in y: the wall loops run over no cells (sppde_core.c:589)
-  fp64_channel(x->b.f[1], x->b.f[2], x->b.f[4], x->b.f[5], x->s.nx, x->s.ny, x->stream);
+  if (x->precision == SW2G_FP32) {
+    fp32_channel(x);
+  } else {
+    fp64_channel(x->b.f[1], x->b.f[2], x->b.f[4], x->b.f[5], x->s.nx, x->s.ny, x->stream);
+  }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(x->stream));
   return SW2G_OK;

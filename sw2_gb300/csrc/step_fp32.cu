@@ -99,7 +99,6 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
   d.extra = c.extra;
   d.sig2dt = c.sig2dt; d.sigdt = c.sigdt; d.nu2dt = c.nu2dt; d.nu4dt = c.nu4dt; d.nu6dt = c.nu6dt;
   d.q = c.q;
-  d.wx = c.wx; d.wy = c.wy; d.hb = c.hb;
   for (int q = 0; q < 2; q++) {
     d.eta[q] = e.eta[q]; d.u[q] = e.u[q]; d.v[q] = e.v[q];
     d.es[q] = e.es[q]; d.us[q] = e.us[q]; d.vs[q] = e.vs[q];
@@ -116,6 +115,7 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
   d.w0 = e.w;
   d.k0 = k > 2 ? 2 : k;
   d.tile_test = c.tile_test;
+  d.open_step = c.open_step;
   return d;
 }
 

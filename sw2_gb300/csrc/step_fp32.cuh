@@ -1180,8 +1180,13 @@ __device__ __forceinline__ void unew5(const MemberDesc& d, const View& vw, int i
       oor = oor || ((ib + c <= nx) && !in_range(unw[c]));
     }
     st4f(d.hu[vw.w], P, ib, jr, hist);
-    put4<IMG_U, 1>(d.u[1 - vw.cur], nx + 4, nx, ny, ib, jr, unw);
-    put4<IMG_U, 3>(d.us[1 - vw.cur], P, nx, ny, ib, jr, usn);
+    if (d.open_step) {  // the plain halo update only; do_channel comes after the forcing
+      put4<IMG_ETA, 1>(d.u[1 - vw.cur], nx + 4, nx, ny, ib, jr, unw);
+      put4<IMG_ETA, 3>(d.us[1 - vw.cur], P, nx, ny, ib, jr, usn);
+    } else {
+      put4<IMG_U, 1>(d.u[1 - vw.cur], nx + 4, nx, ny, ib, jr, unw);
+      put4<IMG_U, 3>(d.us[1 - vw.cur], P, nx, ny, ib, jr, usn);
+    }
   }
 }
 
@@ -1264,11 +1269,16 @@ __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw,
       hist[c] = dvn;
       vn[c] = vc[c] + f2d(dv);
       vsn[c] = d2f(vn[c]);
-      oor = oor || ((ib + c <= nx) && !in_range(vn[c]));
+      oor = oor || ((ib + c <= nx) && j != ny && !in_range(vn[c]));  // row ny is a wall: do_channel zeroes it
     }
     st4f(d.hv[vw.w], P, ib, j, hist);
-    put4<IMG_V, 1>(d.v[1 - vw.cur], W, nx, ny, ib, j, vn);
-    put4<IMG_V, 3>(d.vs[1 - vw.cur], P, nx, ny, ib, j, vsn);
+    if (d.open_step) {
+      put4<IMG_ETA, 1>(d.v[1 - vw.cur], W, nx, ny, ib, j, vn);
+      put4<IMG_ETA, 3>(d.vs[1 - vw.cur], P, nx, ny, ib, j, vsn);
+    } else {
+      put4<IMG_V, 1>(d.v[1 - vw.cur], W, nx, ny, ib, j, vn);
+      put4<IMG_V, 3>(d.vs[1 - vw.cur], P, nx, ny, ib, j, vsn);
+    }
 #pragma unroll
     for (int c = 0; c < 5; c++) unc[c] = unn[c];
   }

@@ -1540,6 +1540,13 @@ void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, 
   k_channel<<<(nx + 127) / 128, 128, 0, st>>>(nx, ny, u, v, wx, wy);
 }
 
+void fp64_range(const DevState& s, const double* const* fields, int n, int* bad, cudaStream_t st) {
+  RangeFields r{};
+  for (int k = 0; k < n && k < 4; k++) r.f[r.n++] = fields[k];
+  const dim3 g((s.nx + TX - 1) / TX, s.ny);
+  pdl_launch(k_range, g, dim3(TX), st, s, r, bad);
+}
+
 void fp64_check_add(long long samples, unsigned long long seed, unsigned long long* bad, cudaStream_t st) {
   k_check_add<<<152 * 8, 256, 0, st>>>(samples, seed, bad);
 }

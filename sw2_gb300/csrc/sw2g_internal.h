@@ -143,6 +143,9 @@ int fp64_step(const DevState& s, Fp64Buffers& b, int sch, int k, bool tracer, St
 void fp64_add_scaled(double* f, const double* d, double scale, int nx, int ny, cudaStream_t st);
 void fp64_set_where(double* f, const double* val, const unsigned char* mask, int nx, int ny, cudaStream_t st);
 void fp64_channel(double* u, double* v, double* wx, double* wy, int nx, int ny, cudaStream_t st);
+// The reference's range check (check_stats_scaf, sppde_core.c:386-395) of n
+// padded fields of the grid; sets *bad (device) to 1 when one fails.
+void fp64_range(const DevState& s, const double* const* fields, int n, int* bad, cudaStream_t st);
 // f[cells[k]] = values[k] (values NULL: 0.0) for k < n; the cells are distinct.
 void fp64_scatter_cells(double* f, const int* cells, const double* values, int n, cudaStream_t st);
 // Compares the step's division by a row metric (div_rcp) with IEEE division
@@ -190,6 +193,10 @@ struct Fp32Ctx {
   // loads of the next steps also wait for a barrier phase that never
   // completes, giving up after that many tries; 0 in normal use.
   int tile_test = 0;
+  // 1 while a step is run for sw2g_step_open: the step writes u and v with
+  // the plain halo update only (core.c:287-288), leaving do_channel and the
+  // range checks to sw2g_step_close, after the forcing (core.c:292-312).
+  int open_step = 0;
 };
 
 struct Fp32Engine {
@@ -246,7 +253,6 @@ struct MemberDesc {
   int extra;
   float sig2dt, sigdt, nu2dt, nu4dt, nu6dt;
   const float* q;
-  const float* wx; const float* wy; const float* hb;
   double* eta[2]; double* u[2]; double* v[2];
   float* es[2]; float* us[2]; float* vs[2];
   float* heta[3]; float* hu[3]; float* hv[3];
@@ -256,6 +262,7 @@ struct MemberDesc {
   const CUtensorMap* tm;  // TM_NUM tensor maps of this member's FP32 fields
   unsigned* cfl; int* bad;
   int cur0, w0, k0, tile_test;
+  int open_step;  // Fp32Ctx::open_step
 };
 
 // Most members of one batch: their descriptors fill at most ~28 KB of the

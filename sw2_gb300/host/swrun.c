@@ -348,10 +348,6 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
     goto done;
   }
   if (c.reftype != 0 && !quiet) fprintf(stderr, "sw2g-run: reftype %d: the comparison is not run\n", c.reftype);
-  if (fp32 && (c.num_gaussians || c.num_vortices || c.nu6 != 0)) {
-    fprintf(stderr, "sw2g-run: the FP32 form runs cases without forcing and without nu6\n");
-    goto done;
-  }
   if (fp32 && (checkpoint || resume >= 0)) {
     fprintf(stderr, "sw2g-run: checkpoints are written and read by the FP64 step only\n");
     goto done;
@@ -407,7 +403,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
   const double Dt = c.Dt;
   double t = c.t0;
   /* forcing at t0 and the wall fixes (core.c:96-101) */
-  if (!fp32 && resume < 0) {
+  if (resume < 0) {
     if (apply_forcing(&c, g, &w, &pm, Dt, t, err, sizeof err)) {
       if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
       goto done;
@@ -452,7 +448,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
       k++;
     }
     /* the last step of the group takes its forcing between its two halves */
-    const int forced = !fp32 && forcing_active(&c, Dt, tk);
+    const int forced = forcing_active(&c, Dt, tk);
     sw2g_status st = SW2G_OK;
     if (k > 1 || !forced) st = sw2g_step(g, forced ? k - 1 : k);
     if (st == SW2G_OK && forced) {

@@ -173,3 +173,31 @@ def test_fp32_form_runs_a_case_file(tmp_path):
     h = a["eta"][2:-2, 2:-2] + p.depth
     err = np.linalg.norm((b["eta"] - a["eta"])[2:-2, 2:-2]) / np.linalg.norm(h)
     assert err <= 1e-6, err
+
+
+@pytest.mark.parametrize("name", FULL)
+def test_fp32_form_runs_the_forcing_cases(tmp_path, name):
+    """The FP32 form with forcing (Gaussians, vortices, tracer injection)
+    through the runner: sw2g_step_open runs the step with the plain halo
+    update of u and v, the forcing changes the FP64 state, sw2g_step_close
+    makes the halo update of eta and the tracer, do_channel and the range
+    checks (core.c:287-312). Every frame of the reference's run, halos
+    included, within the FP32 form's tolerance: h relative L2 <= 1e-5 over
+    the interior, every padded cell of u, v and the tracer within 1e-3 of the
+    field's largest magnitude; the injected fields and the times exact."""
+    p = gc.forcing_params(name)
+    formats.write_sw(str(tmp_path / f"{name}.sw"), p)
+    _, frames = run(tmp_path, name, flags=("--fp32",))
+    ref = gc.forcing_frames(name)
+    assert sorted(frames) == list(range(len(ref)))
+    inner = (slice(2, -2), slice(2, -2))
+    for k, rf in enumerate(ref):
+        nstep, t, nx, ny, fl = frames[k]
+        assert t == float(rf["t"])
+        assert np.array_equal(fl["perturbs"], rf["perturbs"]), k
+        h = rf["eta"][inner] + p.depth
+        assert np.linalg.norm((fl["eta"] - rf["eta"])[inner]) <= 1e-5 * np.linalg.norm(h), k
+        assert np.max(np.abs(fl["eta"] - rf["eta"])) <= 2e-6 * p.depth, k
+        for f in ("u", "v", "tracer"):
+            scale = float(np.max(np.abs(rf[f])))
+            assert np.max(np.abs(fl[f] - rf[f])) <= 1e-3 * max(scale, 1e-300), (k, f)
