@@ -31,7 +31,7 @@ typedef enum {
   SW2G_ERR_BAD_ARG = 1,   /* invalid case or argument (the reference CRASHes in init.c) */
   SW2G_ERR_CFL = 2,       /* Dt > Dt_CFL at the start of a step (core.c:156-158) */
   SW2G_ERR_NONFINITE = 3, /* field range check failed after a step (core.c:309-312) */
-  SW2G_ERR_TIMEOUT = 4,   /* a bounded device wait gave up (the FP32 form's TMA tile loads;
+  SW2G_ERR_TIMEOUT = 4,   /* a bounded device wait gave up (the FP32 form's TMA row loads;
                              the step's state is then not advanced consistently) */
   SW2G_ERR_CUDA = 5,      /* a CUDA runtime call failed */
   SW2G_ERR_NOMEM = 6,     /* device or host allocation failed */
@@ -116,7 +116,10 @@ sw2g_status sw2g_step(sw2g_ctx *ctx, int nsteps);
  * velocity halo update (core.c:134-290); the forcing calls below may then
  * change eta, u, v and the tracer; sw2g_step_close applies do_channel and the
  * range checks (core.c:303-312) and returns the step's status as sw2g_step
- * does. FP64 contexts only; no other step call may come in between. */
+ * does. No other step call may come in between. In the FP32 form
+ * sw2g_step_open runs the whole fused step with the plain halo update of u and
+ * v, and sw2g_step_close also makes the halo update of a forced eta and
+ * tracer (core.c:297-300) and refreshes the FP32 copies of what changed. */
 sw2g_status sw2g_step_open(sw2g_ctx *ctx);
 sw2g_status sw2g_step_close(sw2g_ctx *ctx);
 
@@ -147,11 +150,11 @@ sw2g_status sw2g_diag(sw2g_ctx *ctx, double *ke, double *ape, double *mass);
 sw2g_status sw2g_reset_ab(sw2g_ctx *ctx);
 
 /* Test of the failure path of the FP32 form's bounded device waits: with
- * waits > 0 the tile loads of the following steps, once their rows have
- * arrived, also wait for a barrier phase that nothing completes, give up
- * after `waits` tries, and the step returns SW2G_ERR_TIMEOUT with the device
- * still usable; waits = 0 restores normal operation. FP32 contexts only. No
- * counterpart in the reference. */
+ * waits > 0 each warp of the following steps' kernels, once the first rows of
+ * its first strip have arrived, also waits for a barrier phase that nothing
+ * completes, gives up after `waits` tries, and the step returns
+ * SW2G_ERR_TIMEOUT with the device still usable; waits = 0 restores normal
+ * operation. FP32 contexts only. No counterpart in the reference. */
 sw2g_status sw2g_test_tile_timeout(sw2g_ctx *ctx, int waits);
 
 /* Exact restart of an FP64 context. The reference restarts from a frame
@@ -175,9 +178,11 @@ long long sw2g_steps_done(const sw2g_ctx *ctx);
 
 /* Forcing between steps, for the reference's time-dependent perturbations
  * (add_Gaussians and add_vortices, perturbs.c:22-477), which it applies after
- * a step's velocity update. FP64 contexts only; `which` is 0 eta, 1 u, 2 v,
- * 3 tracer; arrays are padded host arrays of which the interior is read; each
- * call ends with the single-rank halo wrap of the field.
+ * a step's velocity update. `which` is 0 eta, 1 u, 2 v, 3 tracer; arrays are
+ * padded host arrays of which the interior is read; each call ends with the
+ * single-rank halo wrap of the field. Either form: an FP32 context changes its
+ * FP64 state (heights given to the set calls are taken as eta) and starts
+ * advecting a tracer that is forced.
  *   sw2g_add_field:       field(i,j) += scale * delta(i,j)   (perturbs.c:308, 474-481)
  *   sw2g_set_field_where: field(i,j) = value(i,j) where mask(i,j) != 0 (perturbs.c:356-358)
  *   sw2g_apply_channel:   do_channel on u, v, windx and windy (calc.c:600-649), for
@@ -204,7 +209,7 @@ sw2g_status sw2g_apply_channel(sw2g_ctx *ctx);
  *   sw2g_set_cells: field(i,j) = value for listed cells (TRACER inside the
  *                   radius, perturbs.c:356), others unchanged.
  * The lists are copied before the call returns; the work is queued on the
- * context's stream without waiting for it. FP64 contexts only. */
+ * context's stream without waiting for it. Either form. */
 sw2g_status sw2g_add_cells(sw2g_ctx *ctx, int which, const int *cells, const double *values, int n,
                            double scale);
 sw2g_status sw2g_set_cells(sw2g_ctx *ctx, int which, const int *cells, const double *values, int n);
@@ -239,7 +244,7 @@ void sw2g_destroy(sw2g_ctx *ctx);
 /* ------------------------------------------------------------------ batches
  * Ensembles of independent runs (the reference runs one case per MPI job).
  * A batch steps several SW2G_FP32 contexts together: one launch per phase of
- * the step covers every tile of every member, grids may differ in size, and
+ * the step covers every strip of every member, grids may differ in size, and
  * the time loop replays a captured CUDA graph of one step. Members must be
  * uploaded FP32 contexts on one device with the same limiter; each member's
  * state stays readable through its own context (sw2g_download, sw2g_diag). */
@@ -258,16 +263,17 @@ int sw2g_batch_error_step(const sw2g_batch *b);
 double sw2g_batch_last_step_ms(const sw2g_batch *b);
 long long sw2g_batch_last_launches(const sw2g_batch *b);
 
-/* Autotuner of the batch's launch shape. Neither the tile shape (32 cells
- * wide, 4, 8 or 16 rows high: SW2G_TILE_SHAPES shapes) nor the order in which
- * the tiles of all members are assigned to blocks (SW2G_SCHEDULES orders:
- * rows, columns, members interleaved, bands of 8 tile columns) changes any
- * result, so the candidates are timed on the live run: each of the
- * SW2G_TILE_SHAPES x SW2G_SCHEDULES pairs advances the batch
+/* Autotuner of the batch's launch shape. Neither the strip shape (128 cells
+ * wide, 16, 32 or 64 rows high: SW2G_TILE_SHAPES shapes) nor the order in
+ * which the strips of all members are taken by the kernels' warps
+ * (SW2G_SCHEDULES orders: rows, columns, members interleaved, bands of 8
+ * strip columns) changes any result, so the candidates are timed on the live
+ * run: each of the SW2G_TILE_SHAPES x SW2G_SCHEDULES pairs advances the batch
  * steps_per_candidate steps (after one untimed step per shape, which captures
  * its graph); ms_per_step[shape * SW2G_SCHEDULES + schedule] receives its time
  * per step (may be NULL), and the fastest pair is kept.
- * sw2g_batch_set_schedule picks a pair by hand (tile_rows 4, 8 or 16). */
+ * sw2g_batch_set_schedule picks a pair by hand (tile_rows 16, 32 or 64). A
+ * batch of one member sizes its strips itself, as a single context does. */
 #define SW2G_SCHEDULES 4
 #define SW2G_TILE_SHAPES 3
 sw2g_status sw2g_batch_tune(sw2g_batch *b, int steps_per_candidate, double *ms_per_step);
