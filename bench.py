@@ -74,16 +74,19 @@ KERNEL_BYTES = {
     "f32_tracer": 4 * 3 + 8 + 4 * 2 + 8 + 4 + 4,  # tracer u v shadows, tracer, 2 hist -> tracer + shadow, hist
 }
 # DRAM bytes (read + write) of one launch of the dominant kernels on the
-# 2048x1024 workload, from an ncu capture of the same step (one launch each,
-# third step). With zero winds the plain bodies read eta or u and v only; part
-# of each input is still in L2 from the kernel before, and most of the output
-# leaves L2 later, so DRAM bytes are below the algorithmic bytes.
-NCU_TRAFFIC = {("band2048", "mass"): 57.15e6, ("band2048", "adv_u"): 37.34e6, ("band2048", "adv_v"): 36.00e6}
+# 2048x1024 workload, from an ncu capture of the same step (third step, one
+# launch each, the current kernels). With zero winds the plain bodies read eta
+# or u and v only; part of each input is still in L2 from the kernel before,
+# and most of the output leaves L2 later, so DRAM bytes are below the
+# algorithmic bytes.
+NCU_TRAFFIC = {("band2048", "mass"): 52.60e6, ("band2048", "adv_u"): 34.18e6, ("band2048", "adv_v"): 34.26e6}
 # FP64 thread instructions (DADD + DMUL + DFMA) per interior cell of the
 # dominant kernels on the 2048x1024 workload, from ncu's instruction counters
-# of the same step, and GB300's FP64 peak per cycle over the whole GPU (ncu's peak for DFMA:
-# 304 = 2 lanes per SM x 152 SMs). The FP64 form is bound by this unit.
-NCU_FP64_PER_CELL = {("band2048", "mass"): 59.0, ("band2048", "adv_u"): 77.4, ("band2048", "adv_v"): 77.8}
+# of the same capture, and the FP64 unit's busy fraction there; GB300's FP64
+# peak per cycle over the whole GPU (ncu's peak for DFMA: 304 = 2 lanes per SM
+# x 152 SMs). The FP64 form is bound by this unit.
+NCU_FP64_PER_CELL = {("band2048", "mass"): 52.5, ("band2048", "adv_u"): 68.8, ("band2048", "adv_v"): 69.2}
+NCU_FP64_PIPE_BUSY = {("band2048", "mass"): 0.827, ("band2048", "adv_u"): 0.838, ("band2048", "adv_v"): 0.838}
 FP64_LANES_PER_CYCLE = 304
 # The whole step: read eta u v, write eta u v, read two history levels of
 # three tendencies, write one (a per-cell count for the step's GB/s figure).
@@ -577,7 +580,9 @@ def main():
         pk = FP64_LANES_PER_CYCLE * clocks["sm_mhz"] * 1e6
         fp64_roof = {"bound": "fp64", "kernel": m64["kernel"], "achieved": ach, "peak": pk,
                      "unit": "FP64 instr/s", "frac": ach / pk, "instr_per_cell": n64,
-                     "peak_kind": "ncu per-cycle FP64 peak x median SM clock under load"}
+                     "pipe_busy_ncu": NCU_FP64_PIPE_BUSY.get((args.config, m64["kernel"])),
+                     "peak_kind": "ncu per-cycle FP64 peak x median SM clock under load; frac counts DADD, DMUL "
+                                  "and DFMA only, pipe_busy_ncu every instruction on the FP64 unit"}
 
     forms = {
         "fp64": form_line(m64, args.config, cells),
@@ -602,7 +607,7 @@ def main():
                      "traffic": NCU_TRAFFIC.get((args.config, m64["kernel"])), "peak_kind": peak_kind,
                      "bytes_per_cell": m64["bytes_per_cell"],
                      "per_launch_ms": m64["per_launch_ms"], "kernel_share": m64["kernel_share"],
-                     "note": "the FP64 form is bound by GB300's FP64 unit (85 % busy in ncu), not by HBM: "
+                     "note": "the FP64 form is bound by GB300's FP64 unit (84 % busy in ncu), not by HBM: "
                              "see roofline_fp64"},
         "roofline_fp64": fp64_roof,
         "kernels_ms_per_step": m64["kernels_ms_per_step"],

@@ -74,7 +74,7 @@ typedef struct {
    * Coriolis from each point's angular distance to the pole and a sponge of
    * rate sigma_sponge beyond beta_sponge from it (degrees, radians with
    * SW2G_FLAG_RADIANS); no walls. rE and rP are the case file's values.
-   * FP64 contexts only. polar = 0: the band. */
+   * Either form; an FP32 cap is batched alone. polar = 0: the band. */
   int polar;
   double beta_sponge, sigma_sponge;
 } sw2g_case;
@@ -246,8 +246,10 @@ void sw2g_destroy(sw2g_ctx *ctx);
  * A batch steps several SW2G_FP32 contexts together: one launch per phase of
  * the step covers every strip of every member, grids may differ in size, and
  * the time loop replays a captured CUDA graph of one step. Members must be
- * uploaded FP32 contexts on one device with the same limiter; each member's
- * state stays readable through its own context (sw2g_download, sw2g_diag). */
+ * uploaded FP32 contexts on one device with the same limiter; a polar cap
+ * batches alone (n = 1; a cap among other members gives SW2G_ERR_BAD_ARG).
+ * Each member's state stays readable through its own context (sw2g_download,
+ * sw2g_diag). */
 typedef struct sw2g_batch sw2g_batch;
 
 /* Most members of one batch. */

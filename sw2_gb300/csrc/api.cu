@@ -575,9 +575,8 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   if (!out) return SW2G_ERR_BAD_ARG;
   *out = nullptr;
   if (!case_ok(c) || (precision != SW2G_FP64 && precision != SW2G_FP32)) return SW2G_ERR_BAD_ARG;
-  // the FP32 form covers the band (no polar caps) and the reference's u source of the eta Laplacian
-  if (precision == SW2G_FP32 && (c->polar != 0 || (c->flags & SW2G_FLAG_LAPE_ETA)))
-    return SW2G_ERR_BAD_ARG;
+  // the FP32 form covers the reference's u source of the eta Laplacian
+  if (precision == SW2G_FP32 && (c->flags & SW2G_FLAG_LAPE_ETA)) return SW2G_ERR_BAD_ARG;
   sw2g_ctx* x = new (std::nothrow) sw2g_ctx();
   if (!x) return SW2G_ERR_NOMEM;
   x->c = *c;
@@ -621,8 +620,8 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
   s.rows = x->d_rows;
   s.polar = c->polar;
   s.pf = nullptr;
+  std::vector<double> pf;
   if (c->polar != 0) {  // gravity, Coriolis and sponge fields of the cap
-    std::vector<double> pf;
     polar_fields(*c, pf, &x->rest_mx, &x->rest_my);
     double* d_pf = nullptr;
     if ((st = dalloc(x, &d_pf, pf.size())) != SW2G_OK) return fail(st);
@@ -657,6 +656,34 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     c32.wx = x->d_aux32[0];
     c32.wy = x->d_aux32[1];
     c32.hb = x->d_aux32[2];
+    if (c->polar != 0) {  // the cap's per-cell factors, FP64 arithmetic rounded once
+      const int P = c32.P, R = c32.R, W = s.W, H = s.H;
+      const size_t S32 = (size_t)P * R;
+      std::vector<float> q32((size_t)PQ_NUM * S32, 0.f);
+      auto row = [&](int t, int j) { return x->rows[(size_t)t * H + (j + 1)]; };
+      const double Dt = c->Dt;
+      for (int j = -1; j <= c->ny + 2; j++)
+        for (int i = -1; i <= c->nx + 2; i++) {
+          const size_t q = (size_t)(i + 1) + (size_t)(j + 1) * W, r = (size_t)(i + 3) + (size_t)(j + 1) * P;
+          auto F = [&](int t) { return pf[(size_t)t * S + q]; };
+          q32[PQ_GEX * S32 + r] = (float)(-F(P_GE) * Dt / row(R_DXC, j));
+          q32[PQ_GNY * S32 + r] = (float)(j + 1 <= c->ny + 2 ? -F(P_GN) * Dt / row(R_DYC, j + 1) : 0.0);
+          q32[PQ_DTFE * S32 + r] = (float)(Dt * F(P_FE));
+          q32[PQ_DTFN * S32 + r] = (float)(Dt * F(P_FN));
+          q32[PQ_SH2 * S32 + r] = (float)(2.0 * Dt * F(P_SH));
+          q32[PQ_SU * S32 + r] = (float)(F(P_SU) * Dt);
+          q32[PQ_SV * S32 + r] = (float)(F(P_SV) * Dt);
+          q32[PQ_STR2 * S32 + r] = (float)(2.0 * Dt * F(P_STR));
+        }
+      float* d_pf32 = nullptr;
+      if ((st = dalloc32(x, &d_pf32, q32.size())) != SW2G_OK) return fail(st);
+      if ((st = cuda_fail(cudaMemcpyAsync(d_pf32, q32.data(), q32.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                          x->stream), "polar fields")) != SW2G_OK)
+        return fail(st);
+      c32.polar = c->polar;
+      c32.pf = d_pf32;
+      (void)R;
+    }
     fp32_tiles(c->nx, c->ny, x->run32.th, &x->run32.nbx, &x->run32.nby);
     if ((st = cuda_fail(x->run32.alloc(0), "batch")) != SW2G_OK) return fail(st);
     x->run32.sch = c32.sch;
@@ -1600,6 +1627,7 @@ sw2g_status sw2g_batch_create(sw2g_ctx* const* members, int n, sw2g_batch** out)
     const sw2g_ctx* x = members[m];
     if (!x || x->precision != SW2G_FP32 || x->device != members[0]->device) return SW2G_ERR_BAD_ARG;
     if (x->c32.sch != members[0]->c32.sch) return SW2G_ERR_BAD_ARG;
+    if (x->c32.polar != 0 && n > 1) return SW2G_ERR_BAD_ARG;  // polar caps step alone
     if (!x->uploaded) return SW2G_ERR_STATE;
     for (int q = 0; q < m; q++)
       if (members[q] == x) return SW2G_ERR_BAD_ARG;

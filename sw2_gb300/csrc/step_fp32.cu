@@ -116,6 +116,8 @@ MemberDesc fp32_desc(const Fp32Ctx& c, const Fp32Engine& e, int k) {
   d.k0 = k > 2 ? 2 : k;
   d.tile_test = c.tile_test;
   d.open_step = c.open_step;
+  d.polar = c.polar;
+  d.pf = c.pf;
   return d;
 }
 
@@ -143,6 +145,7 @@ int batch_step_n(int sch, int sr, const MemberDesc* desc, int nmem, const int4* 
   std::memset(&ds, 0, sizeof ds);
   for (int m = 0; m < nmem; m++) ds.m[m] = desc[m];
   const PhaseArgs<N> a{&ds, tiles, (N == 1) ? nbx * nby : ntiles, nbx, sr, desc[0].ny, counter, queue, st, tm};
+  const bool polar = (N == 1) && desc[0].polar != 0;  // polar caps step alone
   bool extra = false, tracer = false, nu6 = false;
   for (int m = 0; m < nmem; m++) {
     extra = extra || desc[m].extra;
@@ -152,33 +155,45 @@ int batch_step_n(int sch, int sr, const MemberDesc* desc, int nmem, const int4* 
   int nl = 0;
   if (tracer) {  // reads the step's old u, v and tracer only (core.c:161-182)
     switch (sch) {
-      case 0: sch_tracer<0, N>(extra, a, nl); break;
-      case 1: sch_tracer<1, N>(extra, a, nl); break;
-      case 2: sch_tracer<2, N>(extra, a, nl); break;
-      case 4: sch_tracer<4, N>(extra, a, nl); break;
-      case 5: sch_tracer<5, N>(extra, a, nl); break;
-      case 6: sch_tracer<6, N>(extra, a, nl); break;
-      case 7: sch_tracer<7, N>(extra, a, nl); break;
-      case 8: sch_tracer<8, N>(extra, a, nl); break;
-      case 9: sch_tracer<9, N>(extra, a, nl); break;
-      default: sch_tracer<kVanLeerSafe, N>(extra, a, nl); break;
+      case 0: sch_tracer<0, N>(extra, polar, a, nl); break;
+      case 1: sch_tracer<1, N>(extra, polar, a, nl); break;
+      case 2: sch_tracer<2, N>(extra, polar, a, nl); break;
+      case 4: sch_tracer<4, N>(extra, polar, a, nl); break;
+      case 5: sch_tracer<5, N>(extra, polar, a, nl); break;
+      case 6: sch_tracer<6, N>(extra, polar, a, nl); break;
+      case 7: sch_tracer<7, N>(extra, polar, a, nl); break;
+      case 8: sch_tracer<8, N>(extra, polar, a, nl); break;
+      case 9: sch_tracer<9, N>(extra, polar, a, nl); break;
+      default: sch_tracer<kVanLeerSafe, N>(extra, polar, a, nl); break;
     }
   }
-  run_phase<kb_lap1<N>, N>("f32_lap1", kSmemLap, a, nl);
-  switch (sch) {  // the FP32 form runs Van Leer in its safe form (kVanLeerSafe)
-    case 0: sch_main1<0, N>(extra, a, nl); break;
-    case 1: sch_main1<1, N>(extra, a, nl); break;
-    case 2: sch_main1<2, N>(extra, a, nl); break;
-    case 4: sch_main1<4, N>(extra, a, nl); break;
-    case 5: sch_main1<5, N>(extra, a, nl); break;
-    case 6: sch_main1<6, N>(extra, a, nl); break;
-    case 7: sch_main1<7, N>(extra, a, nl); break;
-    case 8: sch_main1<8, N>(extra, a, nl); break;
-    case 9: sch_main1<9, N>(extra, a, nl); break;
-    default: sch_main1<kVanLeerSafe, N>(extra, a, nl); break;
+  if constexpr (N == 1) {
+    if (polar) run_phase<kb_lap1<1, true>, 1>("f32_lap1", kSmemLap, a, nl);
+    else run_phase<kb_lap1<1>, 1>("f32_lap1", kSmemLap, a, nl);
+  } else {
+    run_phase<kb_lap1<N>, N>("f32_lap1", kSmemLap, a, nl);
   }
-  if (nu6) run_phase<kb_lap3<N>, N>("f32_lap3", kSmemLap, a, nl);
-  run_phase<kb_main2<N>, N>("f32_main2", kSmemMain2, a, nl);
+  switch (sch) {  // the FP32 form runs Van Leer in its safe form (kVanLeerSafe)
+    case 0: sch_main1<0, N>(extra, polar, a, nl); break;
+    case 1: sch_main1<1, N>(extra, polar, a, nl); break;
+    case 2: sch_main1<2, N>(extra, polar, a, nl); break;
+    case 4: sch_main1<4, N>(extra, polar, a, nl); break;
+    case 5: sch_main1<5, N>(extra, polar, a, nl); break;
+    case 6: sch_main1<6, N>(extra, polar, a, nl); break;
+    case 7: sch_main1<7, N>(extra, polar, a, nl); break;
+    case 8: sch_main1<8, N>(extra, polar, a, nl); break;
+    case 9: sch_main1<9, N>(extra, polar, a, nl); break;
+    default: sch_main1<kVanLeerSafe, N>(extra, polar, a, nl); break;
+  }
+  if constexpr (N == 1) {
+    if (nu6 && polar) run_phase<kb_lap3<1, true>, 1>("f32_lap3", kSmemLap, a, nl);
+    else if (nu6) run_phase<kb_lap3<1>, 1>("f32_lap3", kSmemLap, a, nl);
+    if (polar) run_phase<kb_main2<1, true>, 1>("f32_main2", kSmemMain2, a, nl);
+    else run_phase<kb_main2<1>, 1>("f32_main2", kSmemMain2, a, nl);
+  } else {
+    if (nu6) run_phase<kb_lap3<N>, N>("f32_lap3", kSmemLap, a, nl);
+    run_phase<kb_main2<N>, N>("f32_main2", kSmemMain2, a, nl);
+  }
   kb_advance<<<1, 1, 0, st>>>(counter);
   nl++;
   return nl;
@@ -189,6 +204,11 @@ void prepare_n() {
   grid_cap<kb_lap1<N>>(kSmemLap);
   grid_cap<kb_lap3<N>>(kSmemLap);
   grid_cap<kb_main2<N>>(kSmemMain2);
+  if constexpr (N == 1) {
+    grid_cap<kb_lap1<1, true>>(kSmemLap);
+    grid_cap<kb_lap3<1, true>>(kSmemLap);
+    grid_cap<kb_main2<1, true>>(kSmemMain2);
+  }
 }
 
 }  // namespace

@@ -525,9 +525,30 @@ __device__ __forceinline__ float4 di_source(const float* gU, const float* gV, in
 // 1..ny and beyond column nx; ZE(0, j) is the wrapped ZE(nx, j), evaluated at
 // its source column from the global arrays gU, gV (pitch P). ua, ub: u rows j,
 // j+1; va: v row j (windows).
+// A polar cap has no walls: its halo rows wrap, so ZE(i, 0) is ZE(i, ny),
+// evaluated at its source row from the global arrays.
+template <bool POLAR = false>
 __device__ __forceinline__ void ze5(const float* q, int nx, int ny, int P, int ib, int j, const float (&ua)[8],
                                     const float (&ub)[8], const float (&va)[8], const float* gU, const float* gV,
                                     float (&ze)[5]) {
+  if constexpr (POLAR) {
+    if (j == 0) {
+      const float idxv = Qr(q, Q_IDXV, ny), idyc = Qr(q, Q_IDYC, ny + 1);
+      const float dxc1 = Qr(q, Q_DXC, ny + 1), dxc0 = Qr(q, Q_DXC, ny);
+#pragma unroll
+      for (int k = 0; k < 5; k++) {
+        const int i = ib - 1 + k, is = (i == 0) ? nx : i;
+        float z = 0.f;
+        if (i <= nx) {
+          const float v1 = gV[IX32(P, is + 1, ny)], v0 = gV[IX32(P, is, ny)];
+          const float u1 = gU[IX32(P, is, ny + 1)], u0 = gU[IX32(P, is, ny)];
+          z = idxv * ((v1 - v0) - idyc * (dxc1 * u1 - dxc0 * u0));
+        }
+        ze[k] = z;
+      }
+      return;
+    }
+  }
   const bool rowok = (j >= 1 && j <= ny);
   const float idxv = Qr(q, Q_IDXV, j), idyc = Qr(q, Q_IDYC, j + 1);
   const float dxc1 = Qr(q, Q_DXC, j + 1), dxc0 = Qr(q, Q_DXC, j);
@@ -547,10 +568,30 @@ __device__ __forceinline__ void ze5(const float* q, int nx, int ny, int P, int i
 // stencil, DI(nx+1, jd) the wrapped DI(1, jd) from the source column, the
 // north wall row ny+1 the difference of u along row ny, zero elsewhere.
 // uj, vj: u, v rows jd; vjm, ujm: v, u rows jd-1 (windows).
+// A polar cap: DI(i, ny+1) is DI(i, 1), evaluated at its source row.
+template <bool POLAR = false>
 __device__ __forceinline__ void di5(const float* q, int nx, int ny, int P, int ib, int jd, const float (&uj)[8],
                                     const float (&vj)[8], const float (&vjm)[8], const float (&ujm)[8],
                                     const float* gU, const float* gV, float (&di)[5]) {
-  const bool rowok = (jd >= 1 && jd <= ny), wall = (jd == ny + 1);
+  if constexpr (POLAR) {
+    if (jd == ny + 1) {
+      const float idxe = Qr(q, Q_IDXE, 1), idyn = Qr(q, Q_IDYN, 1);
+      const float dxv1 = Qr(q, Q_DXV, 1), dxv0 = Qr(q, Q_DXV, 0);
+#pragma unroll
+      for (int k = 0; k < 5; k++) {
+        const int i = ib + k, is = (i == nx + 1) ? 1 : i;
+        float r = 0.f;
+        if (i >= 1 && i <= nx + 1) {
+          const float uc = gU[IX32(P, is, 1)], uw = gU[IX32(P, is - 1, 1)];
+          const float vc = gV[IX32(P, is, 1)], vs = gV[IX32(P, is, 0)];
+          r = idxe * ((uc - uw) + idyn * (dxv1 * vc - dxv0 * vs));
+        }
+        di[k] = r;
+      }
+      return;
+    }
+  }
+  const bool rowok = (jd >= 1 && jd <= ny), wall = !POLAR && (jd == ny + 1);
   const float idxe = Qr(q, Q_IDXE, jd), idyn = Qr(q, Q_IDYN, jd);
   const float dxv1 = Qr(q, Q_DXV, jd), dxv0 = Qr(q, Q_DXV, jd - 1), idxew = Qr(q, Q_IDXE, ny);
 #pragma unroll
@@ -641,7 +682,7 @@ __device__ __forceinline__ void flush_checks(const MemberDesc& d, const View& v,
 // images. ACC = true: the Laplacian of the second level LL, i.e. the third
 // level LLL (kb_lap3), added as nu6*Dt*LLL to the partial tendencies
 // (core.c:233-268). Rows j0-1 .. j1+1 are staged (ring row t <-> j0-1+t).
-template <bool ACC>
+template <bool ACC, bool POLAR>
 __device__ __forceinline__ bool strip_lap(const MemberDesc& d, const View& vw, int sx, int sy, int SR,
                                           Ring<2, kDLap>& rg, bool test) {
   const int nx = d.nx, ny = d.ny, P = d.P;
@@ -664,10 +705,10 @@ __device__ __forceinline__ bool strip_lap(const MemberDesc& d, const View& vw, i
     float ua[8], ub[8], va[8], vb[8], zt[5];
     win8(rg.row(0, 0), ua); win8(rg.row(1, 0), ub);
     win8(rg.row(0, 1), va); win8(rg.row(1, 1), vb);
-    ze5(q, nx, ny, P, ib, j0 - 1, ua, ub, va, gU, gV, zt);
+    ze5<POLAR>(q, nx, ny, P, ib, j0 - 1, ua, ub, va, gU, gV, zt);
 #pragma unroll
     for (int c = 0; c < 4; c++) zm[c] = zt[c + 1];
-    di5(q, nx, ny, P, ib, j0, ub, vb, va, ua, gU, gV, dj);
+    di5<POLAR>(q, nx, ny, P, ib, j0, ub, vb, va, ua, gU, gV, dj);
   }
   const float nu6dt = d.nu6dt;
   for (int j = j0; j <= j1; j++) {
@@ -677,8 +718,8 @@ __device__ __forceinline__ bool strip_lap(const MemberDesc& d, const View& vw, i
     float ua[8], ub[8], va[8], vb[8], zj[5], dn[5];
     win8(rg.row(t, 0), ua); win8(rg.row(t + 1, 0), ub);
     win8(rg.row(t, 1), va); win8(rg.row(t + 1, 1), vb);
-    ze5(q, nx, ny, P, ib, j, ua, ub, va, gU, gV, zj);
-    di5(q, nx, ny, P, ib, j + 1, ub, vb, va, ua, gU, gV, dn);
+    ze5<POLAR>(q, nx, ny, P, ib, j, ua, ub, va, gU, gV, zj);
+    di5<POLAR>(q, nx, ny, P, ib, j + 1, ub, vb, va, ua, gU, gV, dn);
     float lu[4], lv[4];
     lap_out4(q, j, zj, zm, dj, dn, lu, lv);
     if constexpr (ACC) {
@@ -690,8 +731,8 @@ __device__ __forceinline__ bool strip_lap(const MemberDesc& d, const View& vw, i
       *reinterpret_cast<float4*>(du) = a;
       *reinterpret_cast<float4*>(dv) = b;
     } else {
-      put4<IMG_LU, 3>(d.Lu, P, nx, ny, ib, j, lu);
-      put4<IMG_LV, 3>(d.Lv, P, nx, ny, ib, j, lv);
+      put4<POLAR ? IMG_ETA : IMG_LU, 3>(d.Lu, P, nx, ny, ib, j, lu);
+      put4<POLAR ? IMG_ETA : IMG_LV, 3>(d.Lv, P, nx, ny, ib, j, lv);
     }
 #pragma unroll
     for (int c = 0; c < 4; c++) zm[c] = zj[c + 1];
@@ -731,7 +772,7 @@ __host__ __device__ constexpr int main1_stage() {
 // held in registers across the row.
 __device__ __forceinline__ void section() { asm volatile("" ::: "memory"); }
 
-template <int SCH, bool EXTRA>
+template <int SCH, bool EXTRA, bool POLAR>
 __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw, int sx, int sy, int SR,
                                             Ring<main1_fields<EXTRA>(), kDMain1>& rg, Ring<2, kDLapIn>& rl,
                                             unsigned stg, bool test) {
@@ -813,14 +854,15 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
     float la[8], lb[8], ma[8], mb[8], zt[5];
     win8(rl.row(0, 0), la); win8(rl.row(1, 0), lb);
     win8(rl.row(0, 1), ma); win8(rl.row(1, 1), mb);
-    ze5(q, nx, ny, P, ib, jm, la, lb, ma, d.Lu, d.Lv, zt);
+    ze5<POLAR>(q, nx, ny, P, ib, jm, la, lb, ma, d.Lu, d.Lv, zt);
 #pragma unroll
     for (int c = 0; c < 4; c++) zm[c] = zt[c + 1];
-    di5(q, nx, ny, P, ib, j0, lb, mb, ma, la, d.Lu, d.Lv, dj);
+    di5<POLAR>(q, nx, ny, P, ib, j0, lb, mb, ma, la, d.Lu, d.Lv, dj);
   }
 
   const float sig2dt = d.sig2dt, sigdt = d.sigdt, nu2dt = d.nu2dt, nu4dt = d.nu4dt;
   const bool keep_ll = (d.nu6dt != 0.f);
+  const int PR = P * (ny + 4);  // stride of a cap's per-cell fields
   const double* eta_in = d.eta[vw.cur];
   double* eta_out = d.eta[1 - vw.cur];
   float* es_out = d.es[1 - vw.cur];
@@ -876,6 +918,8 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
       for (int m = 0; m < 5; m++) fx[m] = face1<SCH>(e0[m], e0[m + 1], e0[m + 2], e0[m + 3], u0[m + 1] * kx);
       float eraw[4];
       if constexpr (EXTRA) own4(rg.row(t, FE), eraw);
+      float damp[4] = {sig2dt, sig2dt, sig2dt, sig2dt};  // 2*Dt*sigma; per cell with a cap's sponge
+      if constexpr (POLAR) arr(ld4f(d.pf + PQ_SH2 * PR, P, ib, j), damp);
       float hist[4], esn[4];
       double en[4];
 #pragma unroll
@@ -887,7 +931,7 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
         const float cw = u0[c + 1] * kx, ce = u0[c + 2] * kx, cs = vm[c] * ky, cn = v0[c] * ky;
         float de = (fx[c] - fx[c + 1]) + (face1_term(fs, cs) - face1_term(fn, cn));
         de = fmaf(hb, (cw - ce) + (cs - cn), de);
-        de = fmaf(-sig2dt, eref + (EXTRA ? eraw[c] : e0[c + 2]), de);
+        de = fmaf(-damp[c], eref + (EXTRA ? eraw[c] : e0[c + 2]), de);
         // Adams-Bashforth (calc.c:651-699) then the geofactor (calc.c:403-422)
         float ab = ab3(kab, de, h1[c], h2[c]);
         ab = fmaf(-(geo * (hb + e0[c + 2])), 0.5f * (v0[c] + vm[c]), ab);
@@ -909,8 +953,8 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
       float la[8], lb[8], ma[8], mb[8], zj[5], dn[5], llu[4], llv[4];
       win8(rl.row(k + 1, 0), la); win8(rl.row(k + 2, 0), lb);
       win8(rl.row(k + 1, 1), ma); win8(rl.row(k + 2, 1), mb);
-      ze5(q, nx, ny, P, ib, j, la, lb, ma, d.Lu, d.Lv, zj);
-      di5(q, nx, ny, P, ib, j + 1, lb, mb, ma, la, d.Lu, d.Lv, dn);
+      ze5<POLAR>(q, nx, ny, P, ib, j, la, lb, ma, d.Lu, d.Lv, zj);
+      di5<POLAR>(q, nx, ny, P, ib, j + 1, lb, mb, ma, la, d.Lu, d.Lv, dn);
       lap_out4(q, j, zj, zm, dj, dn, llu, llv);
 #pragma unroll
       for (int c = 0; c < 4; c++) {
@@ -921,8 +965,8 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
 #pragma unroll
       for (int c = 0; c < 5; c++) dj[c] = dn[c];
       if (keep_ll) {  // with its halo images, for the third level
-        put4<IMG_LU, 3>(d.LLu, P, nx, ny, ib, j, llu);
-        put4<IMG_LV, 3>(d.LLv, P, nx, ny, ib, j, llv);
+        put4<POLAR ? IMG_ETA : IMG_LU, 3>(d.LLu, P, nx, ny, ib, j, llu);
+        put4<POLAR ? IMG_ETA : IMG_LV, 3>(d.LLv, P, nx, ny, ib, j, llv);
       }
     }
     section();
@@ -939,6 +983,8 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
                            cneg2(u0[m + 1], u0[m + 2], kc));
       float uraw[4];
       if constexpr (EXTRA) own4(rg.row(t, FU), uraw);
+      float damp[4] = {sigdt, sigdt, sigdt, sigdt};
+      if constexpr (POLAR) arr(ld4f(d.pf + PQ_SU * PR, P, ib, j), damp);
       float du[4];
 #pragma unroll
       for (int c = 0; c < 4; c++) {
@@ -950,7 +996,7 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
                           face2_term(yn, uc, u1[c], cpos2(vn0, vn1, kv), cneg2(vn0, vn1, kv)));
         ysu[c] = yn;
         const float p2 = fmaf(uc * (u0[c + 3] - u0[c + 1]), k2xe, (uc * (0.5f * (vn0 + vn1) - 0.5f * (vs0 + vs1))) * kv);
-        du[c] = fmaf(-(EXTRA ? uraw[c] : uc), sigdt, p1 + p2) + visu[c];
+        du[c] = fmaf(-(EXTRA ? uraw[c] : uc), damp[c], p1 + p2) + visu[c];
         if (ib + c <= nx) mxu = fmaxf(mxu, fabsf(uc) * idxe);
       }
       st4f(d.dup, P, ib, j, du);
@@ -969,6 +1015,8 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
                            cneg2(u1[m + 1], u0[m + 1], kxv));
       float vraw[4];
       if constexpr (EXTRA) own4(rg.row(t, FV), vraw);
+      float damp[4] = {sigdt, sigdt, sigdt, sigdt};
+      if constexpr (POLAR) arr(ld4f(d.pf + PQ_SV * PR, P, ib, j), damp);
       float dv[4];
 #pragma unroll
       for (int c = 0; c < 4; c++) {
@@ -980,7 +1028,7 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
         ysv[c] = yn;
         const float uw1 = u1[c + 1], uw0 = u0[c + 1], ue1 = u1[c + 2], ue0 = u0[c + 2];
         const float p2 = fmaf(vc * (0.5f * (ue0 + ue1) - 0.5f * (uw0 + uw1)), kxv, (vc * (vnp - vsm)) * kdyns);
-        dv[c] = fmaf(-(EXTRA ? vraw[c] : vc), sigdt, p1 + p2) + visv[c];
+        dv[c] = fmaf(-(EXTRA ? vraw[c] : vc), damp[c], p1 + p2) + visv[c];
         if (ib + c <= nx) mxv = fmaxf(mxv, fabsf(vc) * idyn);
       }
       st4f(d.dvp, P, ib, j, dv);
@@ -1001,7 +1049,7 @@ __device__ __forceinline__ bool strip_main1(const MemberDesc& d, const View& vw,
 // Adams-Bashforth combination (calc.c:651-699) and the update with the
 // single-rank halo wrap (core.c:161-182). Staged rows j0-2 .. j1+2 of the
 // tracer shadow, u and v (and the winds with EXTRA).
-template <int SCH, bool EXTRA>
+template <int SCH, bool EXTRA, bool POLAR>
 __device__ __forceinline__ bool strip_tracer(const MemberDesc& d, const View& vw, int sx, int sy, int SR,
                                              Ring<EXTRA ? 5 : 3, kDMain1>& rg, bool test) {
   enum { FT, FU, FV, FWX, FWY };
@@ -1072,6 +1120,8 @@ __device__ __forceinline__ bool strip_tracer(const MemberDesc& d, const View& vw
     win8(rg.row(t, FT), tw); own4(rg.row(t - 1, FT), tm); own4(rg.row(t + 1, FT), t1); own4(rg.row(t + 2, FT), t2);
     U8(t, uw); V4(t - 1, vm); V4(t, vc);
     const float kx = Qr(q, Q_KXE, j), ky = Qr(q, Q_KYN, j);
+    float damp[4] = {sig2dt, sig2dt, sig2dt, sig2dt};  // 2*Dt*TracerDis; per cell with a cap's sponge
+    if constexpr (POLAR) arr(ld4f(d.pf + PQ_STR2 * P * (ny + 4), P, ib, j), damp);
     float fx[5];
 #pragma unroll
     for (int m = 0; m < 5; m++)
@@ -1087,7 +1137,7 @@ __device__ __forceinline__ bool strip_tracer(const MemberDesc& d, const View& vw
       yst[c] = yn;
       float dtr = (fx[c] - fx[c + 1]) + (fs - fn);
       dtr = fmaf(T, fmaf(uw[c + 2] - uw[c + 1], kx, (vc[c] - vm[c]) * ky), dtr);
-      dtr = fmaf(-sig2dt, T, dtr);
+      dtr = fmaf(-damp[c], T, dtr);
       const float ab = ab3(kab, dtr, h1[c], h2[c]);
       hist[c] = dtr;
       tn[c] = tc[c] + f2d(ab);
@@ -1095,7 +1145,7 @@ __device__ __forceinline__ bool strip_tracer(const MemberDesc& d, const View& vw
       oor = oor || ((ib + c <= nx) && !in_range(tn[c]));
     }
     st4f(hw, P, ib, j, hist);
-    put4<IMG_ETA, 1>(tout, W, nx, ny, ib, j, tn);
+    put4<IMG_ETA, 1>(tout, W, nx, ny, ib, j, tn);  // the tracer's halo update wraps (core.c:180-181)
     put4<IMG_ETA, 3>(tsout, P, nx, ny, ib, j, tsn);
   }
   ring_end(rg);
@@ -1146,22 +1196,42 @@ __device__ __forceinline__ void load_unew(const MemberDesc& d, const View& vw, i
 // New u of row jr at columns ib-1+k, k = 0..4 (calc.c:542-573); with `own`
 // the lane's four cells are written (tendency history, FP64 state and shadow
 // with their images).
+// The per-cell -GE*Dt/DXC and Dt*FE of a polar cap at columns ib-1..ib+3 of row jr.
+__device__ __forceinline__ void cap5(const MemberDesc& d, int t, int ib, int jr, float (&v)[5]) {
+  const float* f = d.pf + t * d.P * (d.ny + 4);
+  float a[4];
+  arr(ld4f(f, d.P, ib, jr), a);
+  v[0] = __ldg(f + IX32(d.P, ib - 1, jr));
+#pragma unroll
+  for (int c = 0; c < 4; c++) v[c + 1] = a[c];
+}
+
+template <bool POLAR>
 __device__ __forceinline__ void unew5(const MemberDesc& d, const View& vw, int ib, int jr, bool own,
                                       const float (&ew)[8], const float (&uw)[8], const float (&vr)[8],
                                       const float (&vrm)[8], const UnewIn& in, float (&un)[5], bool& oor) {
   const int nx = d.nx, ny = d.ny, P = d.P;
   const float* q = d.q;
   const bool rowok = (jr <= ny);
-  const float gex = Qr(q, Q_GEX, jr), geo = Qr(q, Q_GEO, jr), dtfe = Qr(q, Q_DTFE, jr);
+  const float geo = Qr(q, Q_GEO, jr);
+  float gex[5], dtfe[5];
+  if constexpr (POLAR) {
+    cap5(d, PQ_GEX, ib, jr, gex);
+    cap5(d, PQ_DTFE, ib, jr, dtfe);
+  } else {
+    const float g = Qr(q, Q_GEX, jr), f = Qr(q, Q_DTFE, jr);
+#pragma unroll
+    for (int k = 0; k < 5; k++) { gex[k] = g; dtfe[k] = f; }
+  }
   float dun[5], du[5];
 #pragma unroll
   for (int k = 0; k < 5; k++) {
     const int i = ib - 1 + k, m = k + 1;
     const float uu = uw[m];
-    const float dn = fmaf(gex, ew[m + 1] - ew[m], in.dup[k]);
+    const float dn = fmaf(gex[k], ew[m + 1] - ew[m], in.dup[k]);
     const float ab = ab3(vw.k, dn, in.h1[k], in.h2[k]);
     const float semi = 0.25f * (((vr[m] + vr[m + 1]) + vrm[m]) + vrm[m + 1]);
-    const float al = fmaf(uu, geo, dtfe);
+    const float al = fmaf(uu, geo, dtfe[k]);
     const float be = 0.25f * (al * al);
     const float dd = __fdividef(fmaf(al, semi, fmaf(-2.f * be, uu, ab)), 1.f + be);
     const bool live = rowok && i >= 1 && i <= nx;
@@ -1180,7 +1250,7 @@ __device__ __forceinline__ void unew5(const MemberDesc& d, const View& vw, int i
       oor = oor || ((ib + c <= nx) && !in_range(unw[c]));
     }
     st4f(d.hu[vw.w], P, ib, jr, hist);
-    if (d.open_step) {  // the plain halo update only; do_channel comes after the forcing
+    if (POLAR || d.open_step) {  // the plain halo update only (no walls, or do_channel after the forcing)
       put4<IMG_ETA, 1>(d.u[1 - vw.cur], nx + 4, nx, ny, ib, jr, unw);
       put4<IMG_ETA, 3>(d.us[1 - vw.cur], P, nx, ny, ib, jr, usn);
     } else {
@@ -1190,6 +1260,7 @@ __device__ __forceinline__ void unew5(const MemberDesc& d, const View& vw, int i
   }
 }
 
+template <bool POLAR>
 __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw, int sx, int sy, int SR,
                                             Ring<3, kDMain2>& rg, bool test) {
   enum { FE, FU, FV };
@@ -1214,7 +1285,7 @@ __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw,
   {  // the new u of row j0
     float ew[8], uw[8], vr[8], vrm[8];
     win8(rg.row(1, FE), ew); win8(rg.row(1, FU), uw); win8(rg.row(1, FV), vr); win8(rg.row(0, FV), vrm);
-    unew5(d, vw, ib, j0, true, ew, uw, vr, vrm, in, unc, oor);
+    unew5<POLAR>(d, vw, ib, j0, true, ew, uw, vr, vrm, in, unc, oor);
   }
   const float* hv1p = d.hv[vw.h1];
   const float* hv2p = d.hv[vw.h2];
@@ -1249,30 +1320,41 @@ __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw,
     {
       float ew[8], uw[8], vr[8], vrm[8];
       win8(rg.row(t + 1, FE), ew); win8(rg.row(t + 1, FU), uw); win8(rg.row(t + 1, FV), vr); win8(rg.row(t, FV), vrm);
-      unew5(d, vw, ib, j + 1, j + 1 <= j1, ew, uw, vr, vrm, cur_in, unn, oor);
+      unew5<POLAR>(d, vw, ib, j + 1, j + 1 <= j1, ew, uw, vr, vrm, cur_in, unn, oor);
     }
     // v of row j
     float e0[4], e1[4], vv[4];
     own4(rg.row(t, FE), e0); own4(rg.row(t + 1, FE), e1); own4(rg.row(t, FV), vv);
-    const float gny = Qr(q, Q_GNY, j), dp1 = Qr(q, Q_DHBP1, j), dtfn = Qr(q, Q_DTFN, j), cv = Qr(q, Q_CV, j);
+    const float dp1 = Qr(q, Q_DHBP1, j), cv = Qr(q, Q_CV, j);
+    float gny[4], dtfn[4];
+    if constexpr (POLAR) {
+      const int PR = P * (ny + 4);
+      arr(ld4f(d.pf + PQ_GNY * PR, P, ib, j), gny);
+      arr(ld4f(d.pf + PQ_DTFN * PR, P, ib, j), dtfn);
+    } else {
+      const float g = Qr(q, Q_GNY, j), f = Qr(q, Q_DTFN, j);
+#pragma unroll
+      for (int c = 0; c < 4; c++) { gny[c] = g; dtfn[c] = f; }
+    }
     float hist[4], vsn[4];
     double vn[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-      const float dvn = fmaf(gny, (e1[c] - e0[c]) + dp1, dvpv[c]);
+      const float dvn = fmaf(gny[c], (e1[c] - e0[c]) + dp1, dvpv[c]);
       const float ab = ab3(kab, dvn, h1[c], h2[c]);
       // new u at (i-1, j+1), (i, j+1), (i, j), (i-1, j)
       const float semi = 0.25f * (((unn[c] + unn[c + 1]) + unc[c + 1]) + unc[c]);
-      const float al = fmaf(semi, cv, dtfn);
+      const float al = fmaf(semi, cv, dtfn[c]);
       const float be = 0.25f * (al * al);
       const float dv = __fdividef(fmaf(-al, semi, fmaf(-2.f * be, vv[c], ab)), 1.f + be);
       hist[c] = dvn;
       vn[c] = vc[c] + f2d(dv);
       vsn[c] = d2f(vn[c]);
-      oor = oor || ((ib + c <= nx) && j != ny && !in_range(vn[c]));  // row ny is a wall: do_channel zeroes it
+      // a band's row ny is a wall: do_channel zeroes it before the check
+      oor = oor || ((ib + c <= nx) && (POLAR || j != ny) && !in_range(vn[c]));
     }
     st4f(d.hv[vw.w], P, ib, j, hist);
-    if (d.open_step) {
+    if (POLAR || d.open_step) {
       put4<IMG_ETA, 1>(d.v[1 - vw.cur], W, nx, ny, ib, j, vn);
       put4<IMG_ETA, 3>(d.vs[1 - vw.cur], P, nx, ny, ib, j, vsn);
     } else {
@@ -1312,24 +1394,25 @@ __device__ __forceinline__ bool strip_main2(const MemberDesc& d, const View& vw,
   const __grid_constant__ DescSet<N> ds, const int4* __restrict__ tiles, int nstrips, int nbx, int SR, \
       const int* __restrict__ counter, unsigned* queue
 
-template <int N>
+template <int N, bool POLAR = false>
 __global__ void __launch_bounds__(NT, 6) kb_lap1(SW2G_KPARAMS) {
-  SW2G_STRIP_LOOP(2, kDLap, (strip_lap<false>(d, v, tl.y, tl.z, SR, rg, test)))
+  SW2G_STRIP_LOOP(2, kDLap, (strip_lap<false, POLAR>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
 // Third Laplacian level (nu6): members without it skip their strips.
-template <int N>
+template <int N, bool POLAR = false>
 __global__ void __launch_bounds__(NT, 6) kb_lap3(SW2G_KPARAMS) {
-  SW2G_STRIP_LOOP(2, kDLap, (d.nu6dt == 0.f || strip_lap<true>(d, v, tl.y, tl.z, SR, rg, test)))
+  SW2G_STRIP_LOOP(2, kDLap, (d.nu6dt == 0.f || strip_lap<true, POLAR>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
 // Tracer advection: members without an active tracer skip their strips.
-template <int SCH, bool EXTRA, int N>
+template <int SCH, bool EXTRA, int N, bool POLAR = false>
 __global__ void __launch_bounds__(NT) kb_tracer(SW2G_KPARAMS) {
-  SW2G_STRIP_LOOP(EXTRA ? 5 : 3, kDMain1, (!d.trd || strip_tracer<SCH, EXTRA>(d, v, tl.y, tl.z, SR, rg, test)))
+  SW2G_STRIP_LOOP(EXTRA ? 5 : 3, kDMain1,
+                  (!d.trd || strip_tracer<SCH, EXTRA, POLAR>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 
-template <int SCH, bool EXTRA, int N>
+template <int SCH, bool EXTRA, int N, bool POLAR = false>
 __global__ void __launch_bounds__(NT, EXTRA ? 2 : 3) kb_main1(SW2G_KPARAMS) {
   extern __shared__ __align__(128) unsigned char sm[];
   Ring<main1_fields<EXTRA>(), kDMain1> rg;
@@ -1348,14 +1431,14 @@ __global__ void __launch_bounds__(NT, EXTRA ? 2 : 3) kb_main1(SW2G_KPARAMS) {
     const View v = view_of(d, n);
     const bool test = first && d.tile_test > 0;
     first = false;
-    if (!strip_main1<SCH, EXTRA>(d, v, tl.y, tl.z, SR, rg, rl, stg, test)) break;
+    if (!strip_main1<SCH, EXTRA, POLAR>(d, v, tl.y, tl.z, SR, rg, rl, stg, test)) break;
   }
   warp_done(queue);
 }
 
-template <int N>
+template <int N, bool POLAR = false>
 __global__ void __launch_bounds__(NT, 4) kb_main2(SW2G_KPARAMS) {
-  SW2G_STRIP_LOOP(3, kDMain2, (strip_main2(d, v, tl.y, tl.z, SR, rg, test)))
+  SW2G_STRIP_LOOP(3, kDMain2, (strip_main2<POLAR>(d, v, tl.y, tl.z, SR, rg, test)))
 }
 #undef SW2G_STRIP_LOOP
 #undef SW2G_KPARAMS
@@ -1428,10 +1511,11 @@ void run_phase(const char* tag, int smem, const PhaseArgs<N>& a, int& nl) {
 
 // The limiter-dependent phases (mass and momentum sweeps, tracer), one
 // instantiation per limiter in step_fp32_limiters.cu.
+// polar: a single polar-cap member (N = 1; its kernels always read the winds)
 template <int SCH, int N>
-void sch_main1(bool extra, const PhaseArgs<N>& a, int& nl);
+void sch_main1(bool extra, bool polar, const PhaseArgs<N>& a, int& nl);
 template <int SCH, int N>
-void sch_tracer(bool extra, const PhaseArgs<N>& a, int& nl);
+void sch_tracer(bool extra, bool polar, const PhaseArgs<N>& a, int& nl);
 template <int SCH>
 void sch_prepare();
 

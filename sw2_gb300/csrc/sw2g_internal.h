@@ -183,8 +183,17 @@ struct TracerDesc {
   float sig2dt;
 };
 
+// Per-cell FP32 fields of a polar cap in the FP32 form (layout of the FP32
+// arrays, one after another): -GE*Dt/DXC and -GN*Dt/DYC(j+1) of the pressure
+// terms (calc.c:517, 538), Dt*FE and Dt*FN of the Coriolis updates
+// (calc.c:563, 592), and the damping with the sponge (calc.c:102-111,
+// 152-161, 374-394): 2*Dt*sigma of height and tracer, sigma*Dt of u and v.
+enum PolarQ { PQ_GEX, PQ_GNY, PQ_DTFE, PQ_DTFN, PQ_SH2, PQ_SU, PQ_SV, PQ_STR2, PQ_NUM };
+
 struct Fp32Ctx {
   int nx, ny, sch, extra;
+  int polar = 0;             // 0 band, +-1 polar cap (single contexts only)
+  const float* pf = nullptr;  // PQ_NUM fields of P*R floats (polar caps)
   int P, R;  // FP32 arrays: row pitch and rows (padded so tile windows stay in bounds)
   const float* q;
   float sig2dt, sigdt, nu2dt, nu4dt, nu6dt;
@@ -263,6 +272,8 @@ struct MemberDesc {
   unsigned* cfl; int* bad;
   int cur0, w0, k0, tile_test;
   int open_step;  // Fp32Ctx::open_step
+  int polar;      // Fp32Ctx::polar
+  const float* pf;  // Fp32Ctx::pf
 };
 
 // Most members of one batch: their descriptors fill at most ~28 KB of the

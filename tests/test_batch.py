@@ -131,6 +131,30 @@ def test_batch_rejects_mixed_members():
         lib.Batch([s32, s32])
 
 
+def test_polar_cap_members_step_alone():
+    """A polar cap's FP32 kernels read per-cell cap factors and are built for
+    one member: a cap batches alone, bit for bit as stepped by itself, and a
+    batch that mixes it with other members is refused."""
+    from tests import golden_cases as gc
+
+    entry, case, _ = gc.load_case("p02_south_superbee_tracer")
+
+    def cap():
+        s = lib.Solver(case.params, precision=lib.FP32)
+        s.upload(*case.fields(), mode=lib.UPLOAD_FRAME)
+        return s
+
+    a, b = cap(), cap()
+    with pytest.raises(lib.SW2GError):
+        lib.Batch([a, fresh(members()[0])])
+    bt = lib.Batch([a])
+    assert bt.step(6) == lib.OK
+    assert b.step(6) == lib.OK
+    ga, gb = a.download(), b.download()
+    for k in ("eta", "u", "v", "tracer"):
+        assert np.array_equal(ga[k], gb[k]), k
+
+
 def fresh(c):
     s = lib.Solver(c.params, precision=lib.FP32, flags=lib.FLAG_VANLEER_SAFE)
     s.upload(*c.fields())

@@ -8,10 +8,13 @@ semantics) with FP32 stencils and FP64 state accumulation. Checks:
   * after many steps the relative L2 error of h = eta + depth is below 1e-5
     (the stated bar), and u, v stay close.
 """
+import dataclasses
+
 import numpy as np
 import pytest
 
 from sw2_gb300 import cases, lib
+from tests import golden_cases as gc
 
 pytestmark = pytest.mark.gpu
 
@@ -115,13 +118,84 @@ def test_fp32_tracer_with_winds(sch):
 
 def test_fp32_rejects_what_it_does_not_cover():
     case = cases.make_case(nx=16, ny=8, sch=2, seed=1)
-    case.params.polar, case.params.angleSim = 1, 20.0
-    case.params.nx = case.params.ny = 16
-    with pytest.raises(lib.SW2GError):
-        lib.Solver(case.params, precision=lib.FP32)
-    case = cases.make_case(nx=16, ny=8, sch=2, seed=1)
     with pytest.raises(lib.SW2GError):
         lib.Solver(case.params, precision=lib.FP32, flags=lib.FLAG_LAPE_ETA)
+
+
+def _polar_pair(params, fields):
+    flags = lib.FLAG_VANLEER_SAFE if params.sch == 3 else 0
+    a = lib.Solver(params, precision=lib.FP32, flags=flags)
+    b = lib.Solver(params, precision=lib.FP64, flags=flags)
+    for s in (a, b):
+        s.upload(*fields, mode=lib.UPLOAD_FRAME)
+    return a, b
+
+
+def _pole_distance(params):
+    """Distance of every padded cell from the cap's pole (the grid's centre), in cells."""
+    H, W = params.ny + 4, params.nx + 4
+    jj, ii = np.mgrid[0:H, 0:W]
+    return np.hypot(jj - (H - 1) / 2.0, ii - (W - 1) / 2.0)
+
+
+def _check_fp32_polar(ga, gb, depth, mask=None):
+    m = np.ones(ga["eta"].shape, bool) if mask is None else mask
+    assert np.max(np.abs(ga["eta"] - gb["eta"])[m]) <= 2e-6 * depth
+    for k in ("u", "v", "tracer"):
+        scale = max(float(np.max(np.abs(gb[k]))), 1e-300)
+        err = np.max(np.abs(ga[k] - gb[k])[m])
+        assert err <= 2e-4 * scale, (k, err / scale)
+
+
+@pytest.mark.parametrize("name", gc.polar_cases())
+def test_fp32_polar_caps(name):
+    """Polar caps (init.c:66-79) in the FP32 form: per-cell gravity, Coriolis
+    and sponge factors, turned winds, no walls (every halo wraps, and the
+    Laplacian intermediates of the halo rows are those of the rows they wrap
+    from), against the FP64 form and the reference's own frames at every
+    saved frame.
+
+    Limiter 2 (calc.c:54-63, psi(r) = r below 1, no lower bound) makes the
+    limited slope psi(r)*d jump from 0 to the upwind difference n when the
+    face difference d changes sign. At the pole the turned winds of mirrored
+    cells are equal up to FP64 rounding, so the FP64 form (like the
+    reference) follows the sign of a rounding residue where the FP32 shadows
+    hold an exact zero. With that limiter the FP32 form stays within its
+    tolerance 12 cells or more from the pole, and within a bound set by the
+    wind's Courant number (1e-3 of eta's range, 2e-3 of the velocity range)
+    at the pole."""
+    entry, case, frames = gc.load_case(name)
+    a, b = _polar_pair(case.params, case.fields())
+    depth = case.params.depth
+    near = _pole_distance(case.params) <= 12
+    for fr in frames:
+        assert a.step(entry["save_every"]) == lib.OK
+        assert b.step(entry["save_every"]) == lib.OK
+        ga, gb = a.download(), b.download()
+        assert np.max(np.abs(gb["eta"][2:-2, 2:-2] - fr["eta"])) <= 1e-9 * depth
+        if case.params.sch != 2:
+            _check_fp32_polar(ga, gb, depth)
+            assert np.max(np.abs(ga["eta"][2:-2, 2:-2] - fr["eta"])) <= 2e-6 * depth
+            continue
+        _check_fp32_polar(ga, gb, depth, mask=~near)
+        assert np.max(np.abs(ga["eta"] - gb["eta"])) <= 1e-3 * float(np.ptp(gb["eta"]))
+        for k in ("u", "v"):
+            assert np.max(np.abs(ga[k] - gb[k])) <= 2e-3 * float(np.max(np.abs(gb[k])))
+    ka, pa, ma = a.diag()
+    kb, pb, mb = b.diag()
+    assert abs(ma - mb) <= 1e-8 * abs(mb)
+
+
+def test_fp32_polar_cap_bounded_limiter():
+    """The north cap with limiter 1 (superbee, a bounded psi) in place of
+    limiter 2: every padded cell of the FP32 form within tolerance of the
+    FP64 form, the pole included, over 60 steps."""
+    entry, case, _ = gc.load_case("p01_north_minmod_nu4")
+    params = dataclasses.replace(case.params, sch=1)
+    a, b = _polar_pair(params, case.fields())
+    for _ in range(3):
+        assert a.step(20) == lib.OK and b.step(20) == lib.OK
+        _check_fp32_polar(a.download(), b.download(), params.depth)
 
 
 @pytest.mark.slow
