@@ -116,6 +116,32 @@ def test_restart_cases_match_the_reference(tmp_path, name):
         assert same_energy(a, "%e %e %e %e" % tuple(b)), (a, b)
 
 
+def test_fp32_form_runs_a_polar_cap(tmp_path):
+    """The south cap (superbee, tracer, nu2+nu4+nu6) from its LoadFrom frame
+    through the runner in the FP32 form: every saved frame within the FP32
+    form's tolerance of the reference's frames (eta within 2e-6 of the depth,
+    u, v and the tracer within 2e-4 of the field's largest magnitude)."""
+    name = "p02_south_superbee_tracer"
+    entry, case, ref = gc.load_case(name)
+    p = case.params
+    p.LoadFrom = 1
+    formats.write_sw(str(tmp_path / f"{name}.sw"), p)
+    os.makedirs(tmp_path / "out")
+    z = np.zeros_like(case.eta)
+    fr = [np.zeros_like(case.eta) for _ in range(4)]
+    for dst, src in zip(fr, (case.eta, case.u, case.v, case.tracer)):
+        dst[2:-2, 2:-2] = src[2:-2, 2:-2]
+    formats.write_frame(str(tmp_path / "out" / f"{name}.0001.bin"), 0, 0.0, p.nx, p.ny, fr + [z])
+    _, frames = run(tmp_path, name, flags=("--fp32",))
+    assert sorted(k for k in frames if k >= 2) == list(range(2, 2 + len(ref)))
+    for k, rf in enumerate(ref):
+        fl = frames[k + 2][4]
+        assert np.max(np.abs(fl["eta"][2:-2, 2:-2] - rf["eta"])) <= 2e-6 * p.depth, k
+        for f in ("u", "v", "tracer"):
+            scale = float(np.max(np.abs(rf[f])))
+            assert np.max(np.abs(fl[f][2:-2, 2:-2] - rf[f])) <= 2e-4 * scale, (k, f)
+
+
 def test_checkpoint_resume_continues_exactly(tmp_path):
     """--checkpoint writes an exact-restart file beside each frame; --resume F
     continues from it and writes the uninterrupted run's later frames bit for
