@@ -179,26 +179,34 @@ def test_known_answer_file(tmp_path):
         assert abs(tot - totk) <= 2.0e-5 * abs(totk)
 
 
-def test_fp32_form_runs_a_case_file(tmp_path):
-    entry, case, ref = gc.load_case("g12_minmod_long")
+@pytest.mark.parametrize("name", ["g12_minmod_long", "g11_wind_tracer", "g02_superbee_nu246"])
+def test_fp32_form_runs_a_case_file(tmp_path, name):
+    """A case file run from its LoadFrom frame by the runner in both forms (a
+    long minmod run; winds with a tracer; nu2+nu4+nu6): the FP32 form's last
+    frame within its tolerance of the FP64 form's (h relative L2 <= 1e-6
+    over the interior, the tracer within 1e-4 of its largest magnitude)."""
+    entry, case, ref = gc.load_case(name)
     p = case.params
     p.LoadFrom = 1
     for sub in ("a", "b"):
         d = tmp_path / sub
         os.makedirs(d / "out")
-        formats.write_sw(str(d / "g12.sw"), p)
+        formats.write_sw(str(d / f"{name}.sw"), p)
         z = np.zeros_like(case.eta)
         fr = [np.zeros_like(case.eta) for _ in range(4)]
         for dst, src in zip(fr, (case.eta, case.u, case.v, case.tracer)):
             dst[2:-2, 2:-2] = src[2:-2, 2:-2]
-        formats.write_frame(str(d / "out" / "g12.0001.bin"), 0, 0.0, p.nx, p.ny, fr + [z])
-    _, f64 = run(tmp_path / "a", "g12")
-    _, f32 = run(tmp_path / "b", "g12", ["--fp32"])
+        formats.write_frame(str(d / "out" / f"{name}.0001.bin"), 0, 0.0, p.nx, p.ny, fr + [z])
+    _, f64 = run(tmp_path / "a", name)
+    _, f32 = run(tmp_path / "b", name, ["--fp32"])
     last = max(f64)
+    assert max(f32) == last
     a, b = f64[last][4], f32[last][4]
     h = a["eta"][2:-2, 2:-2] + p.depth
     err = np.linalg.norm((b["eta"] - a["eta"])[2:-2, 2:-2]) / np.linalg.norm(h)
     assert err <= 1e-6, err
+    tr = float(np.max(np.abs(a["tracer"])))
+    assert np.max(np.abs(b["tracer"] - a["tracer"])) <= 1e-4 * max(tr, 1e-300)
 
 
 @pytest.mark.parametrize("name", FULL)
