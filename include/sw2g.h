@@ -35,7 +35,9 @@ typedef enum {
                              the step's state is then not advanced consistently) */
   SW2G_ERR_CUDA = 5,      /* a CUDA runtime call failed */
   SW2G_ERR_NOMEM = 6,     /* device or host allocation failed */
-  SW2G_ERR_STATE = 7      /* call out of order (e.g. step before upload) */
+  SW2G_ERR_STATE = 7,     /* call out of order (e.g. step before upload) */
+  SW2G_ERR_FORCING = 8    /* a Gaussian evaluated on the device injected no volume, or the
+                             rescaled volume missed its target (perturbs.c:310-326) */
 } sw2g_status;
 
 /* Arithmetic of the step. */
@@ -213,6 +215,32 @@ sw2g_status sw2g_apply_channel(sw2g_ctx *ctx);
 sw2g_status sw2g_add_cells(sw2g_ctx *ctx, int which, const int *cells, const double *values, int n,
                            double scale);
 sw2g_status sw2g_set_cells(sw2g_ctx *ctx, int which, const int *cells, const double *values, int n);
+
+/* A Gaussian injection evaluated on the device (add_Gaussian_core and
+ * get_Gaussian_field, perturbs.c:199-364): the caller gives the values the
+ * reference derives per step from its Gaussian table (the ramped flow rate,
+ * the moved centre, the peak before rescaling, perturbs.c:56-241), the GPU
+ * evaluates every cell's great-circle distance to the centre and to the
+ * requested periodic images, sums the injected volume over the cells inside
+ * the radius, rescales it to `volume` and adds it to eta, and sets the tracer
+ * inside the radius. The distance, exp and volume sum use the GPU's FP64
+ * arithmetic, so results are within rounding of the reference's (the
+ * bit-identical path is the host evaluation with sw2g_add_cells and
+ * sw2g_set_cells); a cell whose distance is within rounding of the radius can
+ * fall on the other side of it. Either form; nothing crosses to the GPU but
+ * these scalars, and the call does not wait for the GPU inside an opened step
+ * (sw2g_step_open): a volume failure is then returned by sw2g_step_close as
+ * SW2G_ERR_FORCING; outside one the call waits and returns it. */
+typedef struct {
+  double lon, lat;       /* centre, radians: planetographic latitude; lon within [lon0, lon1] */
+  double amp;            /* peak height before the rescale (perturbs.c:241) */
+  double sigma, radius;  /* metres */
+  double inject;         /* tracer value at the centre (the tracer is set to inject*exp(-r^2/2sigma^2)) */
+  double volume;         /* Dt times the ramped flow rate; |volume| <= 1e-7: no rescale and eta unchanged */
+  int images;            /* bit 0: also the image at lon - (lon1 - lon0); bit 1: at lon + (lon1 - lon0)
+                            (perturbs.c:250-258), evaluated after the centre in that order */
+} sw2g_gaussian;
+sw2g_status sw2g_add_gaussian(sw2g_ctx *ctx, const sw2g_gaussian *g);
 
 /* Device pointer of a padded state field (0 eta, 1 u, 2 v, 3 tracer) for
  * callers that keep data on the GPU; NULL on a bad index. */

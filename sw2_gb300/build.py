@@ -40,6 +40,7 @@ UNITS = [
     ("step_fp32.cu", ["-fmad=false"], "step_fp32.o"),
     *[("step_fp32_limiters.cu", ["-fmad=false", f"-DSW2G_LIMITER_GROUP={g}"], f"step_fp32_limiters{g}.o")
       for g in range(4)],
+    ("forcing.cu", ["-fmad=false"], "forcing.o"),
     ("geometry.cpp", None, "geometry.o"),  # plain host C++
 ]
 

@@ -223,6 +223,16 @@ struct sw2g_ctx {
   unsigned long long* h_cfl = nullptr;
   unsigned* h_cfl32 = nullptr;
   int* h_bad = nullptr;
+  // Gaussians evaluated on the device (sw2g_add_gaussian, made on first use):
+  // the forcing tables, the scratch, a pinned copy of the error word, and
+  // whether an injection ran since that word was last read
+  double* d_grows = nullptr;
+  double* d_glonc = nullptr;
+  std::vector<double> gpl;  // planetocentric latc(j), j = 0..ny+1
+  GaussScratch gs;
+  int* h_gerr = nullptr;
+  bool gerr_pending = false;
+  bool gerr_host = false;   // an injection whose rows hold no cell had a volume to rescale
 };
 
 namespace {
@@ -567,6 +577,7 @@ const char* sw2g_status_string(sw2g_status s) {
     case SW2G_ERR_CUDA: return "CUDA error";
     case SW2G_ERR_NOMEM: return "out of memory";
     case SW2G_ERR_STATE: return "call out of order";
+    case SW2G_ERR_FORCING: return "injected volume is zero or missed its target";
   }
   return "unknown status";
 }
@@ -958,6 +969,9 @@ static sw2g_status run_steps(sw2g_ctx* x, int nsteps, HostIO* io) {
 }
 
 namespace {
+sw2g_status gauss_queue_check(sw2g_ctx* x);
+bool gauss_failed(sw2g_ctx* x);
+
 // The FP64 field a forcing call changes: the reference layout's field, or in
 // the FP32 form its FP64 state (eta as eta - eta_ref(j)).
 double* force_target(sw2g_ctx* x, int which) {
@@ -1037,11 +1051,17 @@ sw2g_status fp32_step_close(sw2g_ctx* x) {
   CK(cudaMemcpyAsync(cfl, e.cfl + 2 * x->open_slot, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, x->stream));
   CK(cudaMemcpyAsync(bad, e.bad + x->open_slot, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
   CK(cudaMemcpyAsync(bad + 1, x->d_bad, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
+  sw2g_status gst = gauss_queue_check(x);
+  if (gst != SW2G_OK) return gst;
   CK(cudaStreamSynchronize(x->stream));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
   x->last_step_ms = ms;
   if (x->timers.on) x->timers.collect();
+  if (gauss_failed(x)) {  // the reference stops inside add_Gaussians (perturbs.c:316-326)
+    x->err_step = (int)x->steps;
+    return SW2G_ERR_FORCING;
+  }
   float a, b2;
   std::memcpy(&a, &cfl[0], sizeof(float));
   std::memcpy(&b2, &cfl[1], sizeof(float));
@@ -1095,11 +1115,17 @@ sw2g_status sw2g_step_close(sw2g_ctx* x) {
   int* const bad = x->h_bad;
   CK(cudaMemcpyAsync(cfl, x->d_cfl, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, x->stream));
   CK(cudaMemcpyAsync(bad, x->d_bad, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
+  sw2g_status gst = gauss_queue_check(x);
+  if (gst != SW2G_OK) return gst;
   CK(cudaStreamSynchronize(x->stream));
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, x->ev[0], x->ev[1]));
   x->last_step_ms = ms;
   if (x->timers.on) x->timers.collect();
+  if (gauss_failed(x)) {  // the reference stops inside add_Gaussians (perturbs.c:316-326)
+    x->err_step = (int)x->steps;
+    return SW2G_ERR_FORCING;
+  }
   double mx, my;
   std::memcpy(&mx, &cfl[0], sizeof(double));
   std::memcpy(&my, &cfl[1], sizeof(double));
@@ -1441,6 +1467,114 @@ sw2g_status sw2g_set_cells(sw2g_ctx* x, int which, const int* cells, const doubl
   return SW2G_OK;
 }
 
+namespace {
+// Tables and scratch of the device Gaussians, made on the first injection.
+sw2g_status gauss_ready(sw2g_ctx* x) {
+  if (x->d_grows) return SW2G_OK;
+  std::vector<double> rows3, lonc;
+  forcing_tables(x->c, rows3, x->gpl, lonc);
+  sw2g_status st;
+  const size_t S = (size_t)x->s.W * x->s.H;
+  const size_t nparts = (size_t)((x->s.nx + 127) / 128) * (size_t)x->s.ny;
+  if ((st = dalloc(x, &x->d_grows, rows3.size())) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->d_glonc, lonc.size())) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->gs.gp, S)) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->gs.gt, S)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &x->gs.gm, S)) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->gs.part, nparts)) != SW2G_OK) return st;
+  if ((st = dalloc(x, &x->gs.rf, 1)) != SW2G_OK) return st;
+  if ((st = dalloc32(x, &x->gs.err, 1)) != SW2G_OK) return st;
+  CK(cudaHostAlloc((void**)&x->h_gerr, sizeof(int), cudaHostAllocDefault));
+  *x->h_gerr = 0;
+  CK(cudaMemcpyAsync(x->d_grows, rows3.data(), rows3.size() * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->d_glonc, lonc.data(), lonc.size() * sizeof(double), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaStreamSynchronize(x->stream));  // the host tables go out of scope
+  return SW2G_OK;
+}
+
+// Queues the read-back of the device Gaussians' error word (and its reset);
+// gauss_failed tells, once the stream is done, whether an injection failed.
+sw2g_status gauss_queue_check(sw2g_ctx* x) {
+  if (!x->gerr_pending) return SW2G_OK;
+  CK(cudaMemcpyAsync(x->h_gerr, x->gs.err, sizeof(int), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaMemsetAsync(x->gs.err, 0, sizeof(int), x->stream));
+  return SW2G_OK;
+}
+bool gauss_failed(sw2g_ctx* x) {
+  const bool f = x->gerr_host || (x->gerr_pending && *x->h_gerr != 0);
+  x->gerr_pending = false;
+  x->gerr_host = false;
+  if (x->h_gerr) *x->h_gerr = 0;
+  return f;
+}
+}  // namespace
+
+sw2g_status sw2g_add_gaussian(sw2g_ctx* x, const sw2g_gaussian* g) {
+  if (!x || !g) return SW2G_ERR_BAD_ARG;
+  if (x->s.polar != 0) return SW2G_ERR_BAD_ARG;  // the reference's Gaussians are placed on the band
+  if (!std::isfinite(g->lon) || !std::isfinite(g->lat) || !std::isfinite(g->amp) || !(g->sigma > 0) ||
+      !std::isfinite(g->sigma) || std::isnan(g->radius) || !std::isfinite(g->inject) ||
+      !std::isfinite(g->volume) || g->images < 0 || g->images > 3)
+    return SW2G_ERR_BAD_ARG;
+  sw2g_status st = force_ready(x, 0);
+  if (st != SW2G_OK) return st;
+  if ((st = force_ready(x, 3)) != SW2G_OK) return st;
+  if ((st = gauss_ready(x)) != SW2G_OK) return st;
+  const sw2g_case& c = x->c;
+  const int nx = x->s.nx, ny = x->s.ny;
+  GaussJob job{};
+  job.nx = nx;
+  job.R = (c.rE + c.rP) / 2.0;  // perturbs.c:377
+  const double plat = forcing_pclat(c, g->lat);
+  job.sp = std::sin(plat);
+  job.cp = std::cos(plat);
+  job.amp = g->amp;
+  job.den = 2.0 * (g->sigma * g->sigma);
+  job.radius = g->radius;
+  job.inject = g->inject;
+  job.volume = g->volume;
+  const double span = forcing_lon_span(c);
+  job.lon[job.nimg++] = g->lon;
+  if (g->images & 1) job.lon[job.nimg++] = g->lon - span;  // lonLeft
+  if (g->images & 2) job.lon[job.nimg++] = g->lon + span;  // lonRight
+  // Rows that can hold a cell inside the radius: the central angle to the
+  // centre is at least the difference of the planetocentric latitudes. The
+  // margin covers the rounding of the distance (1e-6 rad against ~1e-15).
+  const double th = g->radius / job.R + 1e-6;
+  int j0 = 1, j1 = ny;
+  if (th < 3.0) {
+    j0 = ny + 1;
+    j1 = 0;
+    for (int j = 1; j <= ny; j++)
+      if (std::fabs(x->gpl[j] - plat) <= th) {
+        if (j < j0) j0 = j;
+        j1 = j;
+      }
+  }
+  if (j0 > j1) {  // no cell can be inside: the tracer and eta keep their values
+    if (std::fabs(g->volume) > 1e-7) x->gerr_host = true;  // perturbs.c:316: no volume to rescale
+  } else {
+    job.j0 = j0;
+    job.nrows = j1 - j0 + 1;
+    double* eta = force_target(x, 0);
+    double* tr = force_target(x, 3);
+    gauss_inject(job, x->d_grows, x->d_glonc, x->gs, eta, tr, x->stream);
+    CK(cudaGetLastError());
+    if (x->precision == SW2G_FP64) {  // the calls end with the halo wrap of the fields
+      halo_wrap(eta, nx, ny, x->stream);
+      halo_wrap(tr, nx, ny, x->stream);
+    }
+    forced_field(x, 0);
+    forced_field(x, 3);
+    x->gerr_pending = true;
+    if (g->inject != 0.0 || std::signbit(g->inject)) x->tracer_active = true;
+  }
+  if (x->open) return SW2G_OK;  // reported by sw2g_step_close
+  if ((st = gauss_queue_check(x)) != SW2G_OK) return st;
+  CK(cudaStreamSynchronize(x->stream));
+  return gauss_failed(x) ? SW2G_ERR_FORCING : SW2G_OK;
+}
+
 sw2g_status sw2g_apply_channel(sw2g_ctx* x) {
   sw2g_status st = force_ready(x, 0);
   if (st != SW2G_OK) return st;
@@ -1486,6 +1620,7 @@ void sw2g_destroy(sw2g_ctx* x) {
     if (sl.done) cudaEventDestroy(sl.done);
   }
   if (x->h_chk) cudaFreeHost(x->h_chk);
+  if (x->h_gerr) cudaFreeHost(x->h_gerr);
   x->timers.release();
   x->run32.release();
   for (int e = 0; e < 2; e++)

@@ -200,4 +200,34 @@ void energy_row_geometry(const sw2g_case& c, int j0, int n, double* surf, double
   }
 }
 
+double forcing_lon_span(const sw2g_case& c) { return angle(c, c.lon1) - angle(c, c.lon0); }
+
+double forcing_pclat(const sw2g_case& c, double lat) {
+  const Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};
+  return lat2pclat(p, lat);
+}
+
+void forcing_tables(const sw2g_case& c, std::vector<double>& rows3, std::vector<double>& pl,
+                    std::vector<double>& lonc) {
+  const Planet p{c.rE, c.rP, (c.rE / c.rP) * (c.rE / c.rP), c.gE, c.Omega};
+  const double lon0 = angle(c, c.lon0), lon1 = angle(c, c.lon1);
+  const double lat0 = angle(c, c.lat0), lat1 = angle(c, c.lat1);
+  const double dlon = (lon1 - lon0) / ((double)c.nx);                    // coords.c:60-65
+  const double dlat = (lat1 - lat0) / ((double)c.ny);
+  auto latn = [&](int j) { return linspace_val(j, lat0, lat1, c.ny); };  // sw.h:116
+  auto latc = [&](int j) { return (latn(j) + latn(j - 1)) / 2.; };       // sw.h:117
+  auto lone = [&](int i) { return linspace_val(i, lon0, lon1, c.nx); };  // sw.h:113
+  rows3.assign(3 * (size_t)(c.ny + 2), 0.0);
+  pl.assign((size_t)c.ny + 2, 0.0);
+  lonc.assign((size_t)c.nx + 2, 0.0);
+  for (int j = 0; j <= c.ny + 1; j++) {
+    const double pc = lat2pclat(p, latc(j));
+    pl[j] = pc;
+    rows3[3 * j] = std::sin(pc);
+    rows3[3 * j + 1] = std::cos(pc);
+    rows3[3 * j + 2] = (dlon * rZ(p, latc(j))) * (dlat * rM(p, latn(j - 1)));  // DXC * DYC
+  }
+  for (int i = 0; i <= c.nx + 1; i++) lonc[i] = (lone(i) + lone(i - 1)) / 2.;  // sw.h:114
+}
+
 }  // namespace sw2g

@@ -71,6 +71,40 @@ void build_rows(const sw2g_case& c, std::vector<double>& rows, double* rest_mx, 
 // The fields of a polar cap (P_NUM x (nx+4)(ny+4)) and the at-rest CFL maxima
 // computed with them.
 void polar_fields(const sw2g_case& c, std::vector<double>& f, double* rest_mx, double* rest_my);
+// Tables of the Gaussian forcing (perturbs.c:333-364, tools.c:104-119), with
+// the reference's expressions: rows3[3*j..] = {sin, cos of the planetocentric
+// latitude of latc(j), DXC(j)*DYC(j)} and pl[j] that latitude, j = 0..ny+1;
+// lonc[i] = lonc(i), i = 0..nx+1. forcing_pclat: the planetocentric latitude
+// of a planetographic one (sw.h:170).
+void forcing_tables(const sw2g_case& c, std::vector<double>& rows3, std::vector<double>& pl,
+                    std::vector<double>& lonc);
+double forcing_pclat(const sw2g_case& c, double lat);
+// lon1 - lon0 in radians (the shift of a Gaussian's periodic images, perturbs.c:250-251).
+double forcing_lon_span(const sw2g_case& c);
+
+// A Gaussian injection on the device (forcing.cu): rows j0 .. j0+nrows-1
+// (1 <= j0, j0+nrows-1 <= ny) hold every cell that can be inside the radius.
+struct GaussJob {
+  int nx, j0, nrows, nimg;
+  double lon[3];           // the centre and its periodic images, in evaluation order
+  double sp, cp;           // sin, cos of the centre's planetocentric latitude
+  double R;                // mean radius (rE + rP) / 2
+  double amp, den;         // peak before the rescale; 2 * sigma^2
+  double radius, inject, volume;
+};
+// Device scratch of the injections: per-cell field, tracer value and mask
+// (padded), partial volumes (one per block: ceil(nx/128) * ny), the rescale
+// factor and the error word (nonzero after a failed volume check).
+struct GaussScratch {
+  double* gp = nullptr;
+  double* gt = nullptr;
+  unsigned char* gm = nullptr;
+  double* part = nullptr;
+  double* rf = nullptr;
+  int* err = nullptr;
+};
+void gauss_inject(const GaussJob& g, const double* rows, const double* lonc, GaussScratch& sc, double* eta,
+                  double* tracer, cudaStream_t st);
 
 // FP64 reference-exact step (step_fp64.cu).
 struct Fp64Buffers {

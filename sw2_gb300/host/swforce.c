@@ -179,11 +179,9 @@ static void gaussian_field(const swcase *c, double lon, double lat, double amp, 
   }
 }
 
-int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, double *scale, char *err,
-                     size_t errlen) {
+int swforce_gaussian_plan(const swcase *c, int g, double Dt, double t, swf_gplan *p, char *err, size_t errlen) {
   const double *G = c->gaussians + (size_t)g * SWC_GAUSS_COLS;
   const double t0 = G[0], t1 = G[1];
-  *scale = 0.0;
   if (!((t0 <= t) && (t1 >= t))) return 1;  /* perturbs.c:63 */
   const double tau = G[2];
   if (tau < 0) {
@@ -228,7 +226,27 @@ int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, do
   /* add_Gaussian_core (perturbs.c:199-330) */
   while (lon < c->lon0) lon += (c->lon1 - c->lon0);
   while (lon > c->lon1) lon -= (c->lon1 - c->lon0);
-  const double amp = volume / (2.0 * PI_() * sq(sigma) * (1.0 - exp(-sq(radius) / (2.0 * sq(sigma)))));
+  p->lon = lon;
+  p->lat = lat;
+  p->sigma = sigma;
+  p->radius = radius;
+  p->inject = inject;
+  p->volume = volume;
+  p->amp = volume / (2.0 * PI_() * sq(sigma) * (1.0 - exp(-sq(radius) / (2.0 * sq(sigma)))));
+  p->images = 0;
+  if ((lon + radius / swf_rZ(c, lat)) >= c->lon1) p->images |= 1;  /* perturbs.c:250-258 */
+  if ((lon - radius / swf_rZ(c, lat)) <= c->lon0) p->images |= 2;
+  return 0;
+}
+
+int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, double *scale, char *err,
+                     size_t errlen) {
+  *scale = 0.0;
+  swf_gplan p;
+  const int prc = swforce_gaussian_plan(c, g, Dt, t, &p, err, errlen);
+  if (prc != 0) return prc;
+  const double lon = p.lon, lat = p.lat, sigma = p.sigma, radius = p.radius, inject = p.inject;
+  const double volume = p.volume, amp = p.amp;
   tables(c, w);
   /* the previous injection's cells back to zero (the reference starts from a
    * zeroed perturb_field, perturbs.c:237-238) */
@@ -240,8 +258,8 @@ int swforce_gaussian(const swcase *c, int g, double Dt, double t, swforce *w, do
   gaussian_field(c, lon, lat, amp, sigma, radius, inject, w);
   const double lonRight = lon + (c->lon1 - c->lon0);
   const double lonLeft = lon - (c->lon1 - c->lon0);
-  if ((lon + radius / swf_rZ(c, lat)) >= c->lon1) gaussian_field(c, lonLeft, lat, amp, sigma, radius, inject, w);
-  if ((lon - radius / swf_rZ(c, lat)) <= c->lon0) gaussian_field(c, lonRight, lat, amp, sigma, radius, inject, w);
+  if (p.images & 1) gaussian_field(c, lonLeft, lat, amp, sigma, radius, inject, w);
+  if (p.images & 2) gaussian_field(c, lonRight, lat, amp, sigma, radius, inject, w);
   /* padded index order is the reference's loop order (j outer, i inner) */
   qsort(w->cells, (size_t)w->ncells, sizeof(int), cmp_int);
   const int W = c->nx + 4;

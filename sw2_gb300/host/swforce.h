@@ -54,6 +54,18 @@ double swf_g_eff(const swcase *c, double pclat);
 double swf_DXC(const swcase *c, int j);
 double swf_DYC(const swcase *c, int j);
 
+/* The per-step scalars of Gaussian row g at time t (add_Gaussians and the
+ * start of add_Gaussian_core, perturbs.c:56-258): the centre moved and
+ * wrapped into [lon0, lon1], sigma and radius in metres, the ramped volume
+ * Dt*Q(t), the peak before rescaling, and which periodic images the field
+ * needs (bit 0: lon - (lon1 - lon0), bit 1: lon + (lon1 - lon0)). Returns 0,
+ * 1 if the row is not active at t, or -1 on an error of the case. */
+typedef struct {
+  double lon, lat, amp, sigma, radius, inject, volume;
+  int images;
+} swf_gplan;
+int swforce_gaussian_plan(const swcase *c, int g, double Dt, double t, swf_gplan *p, char *err, size_t errlen);
+
 /* One Gaussian injection that is active at time t (t0 <= t <= t1 of row g):
  * fills w->pert (zeroed first), sets w->tracer/w->mask for the cells inside
  * the radius (mask zeroed first), sets w->perturbs to 1 there, lists those

@@ -2,9 +2,13 @@
  * sw2g-run: runs an SW2 case file on the GPU step, as the reference's
  * executable runs it on one rank:
  *
- *     sw2g-run [--fp32] [--quiet] [--checkpoint] [--resume F] NPX NPY CASE OUTDIR
+ *     sw2g-run [--fp32] [--quiet] [--checkpoint] [--resume F] [--device-forcing] NPX NPY CASE OUTDIR
  *
- * (NPX = NPY = 1). --checkpoint writes, next to each frame, an exact-restart
+ * (NPX = NPY = 1). --device-forcing evaluates the Gaussian injections on the
+ * GPU (sw2g_add_gaussian: results within rounding of the reference's); by
+ * default the host evaluates them with the reference's expressions and libm
+ * and only the cells inside each radius cross to the GPU (bit for bit).
+ * --checkpoint writes, next to each frame, an exact-restart
  * checkpoint (full padded state, Adams-Bashforth histories and index);
  * --resume F continues from the checkpoint of frame F bit for bit as the
  * uninterrupted run would (the reference's LoadFrom restarts with an Euler
@@ -283,10 +287,34 @@ static void perturbs_clear(swforce *w, marks *m) {
  * the velocity halos, before do_channel); at t0 it is followed by
  * sw2g_apply_channel (core.c:96-101). A Gaussian sends only the cells inside
  * its radius to the GPU (sw2g_set_cells, sw2g_add_cells). */
-static int apply_forcing(const swcase *c, sw2g_ctx *g, swforce *w, marks *pm, double Dt, double t, char *err,
-                         size_t errlen) {
+static int apply_forcing(const swcase *c, sw2g_ctx *g, swforce *w, marks *pm, double Dt, double t, int device,
+                         int need_mask, char *err, size_t errlen) {
   perturbs_clear(w, pm);
   for (int k = 0; k < c->num_gaussians; k++) {
+    if (device) {
+      /* the field, the volume and its rescale evaluated on the GPU; the host
+       * evaluates the cells inside the radius only for a frame's PERTURBS */
+      swf_gplan p;
+      const int prc = swforce_gaussian_plan(c, k, Dt, t, &p, err, errlen);
+      if (prc < 0) return -1;
+      if (prc == 1) continue;
+      const sw2g_gaussian dg = {p.lon, p.lat, p.amp, p.sigma, p.radius, p.inject, p.volume, p.images};
+      const sw2g_status st = sw2g_add_gaussian(g, &dg);
+      if (st == SW2G_ERR_FORCING) {
+        snprintf(err, errlen, "Gaussian %d: total injected volume is 0 or missed its target", k);
+        return -1;
+      }
+      if (ck(st, "Gaussian")) return -1;
+      if (need_mask) {
+        double rf_unused = 0;
+        if (swforce_gaussian(c, k, Dt, t, w, &rf_unused, err, errlen) < 0) return -1;
+        if (marks_add(pm, w->cells, w->ncells)) {
+          snprintf(err, errlen, "out of host memory");
+          return -1;
+        }
+      }
+      continue;
+    }
     double rf = 0;
     const int rc = swforce_gaussian(c, k, Dt, t, w, &rf, err, errlen);
     if (rc < 0) return -1;
@@ -326,7 +354,8 @@ static int print_energy(sw2g_ctx *g, double t) {
   return 0;
 }
 
-int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, int checkpoint, int resume) {
+int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, int checkpoint, int resume,
+                  int device_forcing) {
   char err[512] = {0}, path[4096];
   snprintf(path, sizeof path, "%s.sw", bname);
   swcase c;
@@ -404,7 +433,7 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
   double t = c.t0;
   /* forcing at t0 and the wall fixes (core.c:96-101) */
   if (resume < 0) {
-    if (apply_forcing(&c, g, &w, &pm, Dt, t, err, sizeof err)) {
+    if (apply_forcing(&c, g, &w, &pm, Dt, t, device_forcing, 1, err, sizeof err)) {
       if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
       goto done;
     }
@@ -435,8 +464,8 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
   frame++;
   nstart++;
   if (!quiet)
-    fprintf(stderr, "sw2g-run: %s %dx%d, steps %d..%d, Dt %g, %s\n", bname, nx, ny, nstart, c.N, Dt,
-            fp32 ? "FP32 form" : "FP64");
+    fprintf(stderr, "sw2g-run: %s %dx%d, steps %d..%d, Dt %g, %s%s\n", bname, nx, ny, nstart, c.N, Dt,
+            fp32 ? "FP32 form" : "FP64", device_forcing ? ", Gaussians evaluated on the GPU" : "");
   for (int n = nstart; n <= c.N;) {
     /* steps without output or forcing are run in one call */
     int k = 1;
@@ -454,17 +483,21 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
     if (st == SW2G_OK && forced) {
       st = sw2g_step_open(g);
       if (st == SW2G_OK) {
-        if (apply_forcing(&c, g, &w, &pm, Dt, tk, err, sizeof err)) {
+        /* the step ending at tk writes a frame: its PERTURBS are needed */
+        const int frame_step = ((n + k - 1) % c.saveEvery == 0);
+        if (apply_forcing(&c, g, &w, &pm, Dt, tk, device_forcing, frame_step, err, sizeof err)) {
           if (err[0]) fprintf(stderr, "sw2g-run: %s\n", err);
           goto done;
         }
         st = sw2g_step_close(g);
       }
     }
-    if (st == SW2G_ERR_CFL || st == SW2G_ERR_NONFINITE) {
+    if (st == SW2G_ERR_CFL || st == SW2G_ERR_NONFINITE || st == SW2G_ERR_FORCING) {
       /* error steps count from the last upload, which preceded step nstart */
       fprintf(stderr, "sw2g-run: %s at step %d\n",
-              st == SW2G_ERR_CFL ? "Dt exceeds the CFL bound" : "nonsense value detected",
+              st == SW2G_ERR_CFL        ? "Dt exceeds the CFL bound"
+              : st == SW2G_ERR_FORCING ? "a Gaussian's injected volume is 0 or missed its target"
+                                       : "nonsense value detected",
               nstart + sw2g_error_step(g));
       rc = 3;
       goto done;

@@ -17,7 +17,7 @@ from .formats import CaseParams
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsw2g.so")
 
-OK, ERR_BAD_ARG, ERR_CFL, ERR_NONFINITE, ERR_TIMEOUT, ERR_CUDA, ERR_NOMEM, ERR_STATE = range(8)
+OK, ERR_BAD_ARG, ERR_CFL, ERR_NONFINITE, ERR_TIMEOUT, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_FORCING = range(9)
 FP64, FP32 = 0, 1
 FLAG_VANLEER_SAFE = 0x1
 FLAG_RADIANS = 0x2
@@ -47,6 +47,13 @@ class Case(ctypes.Structure):
                 ("tau", ctypes.c_double), ("tracer_dis", ctypes.c_double),
                 ("hypernu", ctypes.c_double * 3), ("flags", ctypes.c_uint),
                 ("polar", ctypes.c_int), ("beta_sponge", ctypes.c_double), ("sigma_sponge", ctypes.c_double)]
+
+
+class Gaussian(ctypes.Structure):
+    """sw2g_gaussian: one injection evaluated on the device (sw2g_add_gaussian)."""
+    _fields_ = [("lon", ctypes.c_double), ("lat", ctypes.c_double), ("amp", ctypes.c_double),
+                ("sigma", ctypes.c_double), ("radius", ctypes.c_double), ("inject", ctypes.c_double),
+                ("volume", ctypes.c_double), ("images", ctypes.c_int)]
 
 
 class SW2GError(RuntimeError):
@@ -314,6 +321,12 @@ class Solver:
         v = np.ascontiguousarray(values, dtype=np.float64)
         return L.sw2g_set_cells(self.h, int(which), c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), _ptr(v),
                                 int(c.size))
+
+    def add_gaussian(self, g: "Gaussian") -> int:
+        """sw2g_add_gaussian: the injection evaluated on the device; returns the status."""
+        L = load()
+        L.sw2g_add_gaussian.argtypes = [ctypes.c_void_p, ctypes.POINTER(Gaussian)]
+        return L.sw2g_add_gaussian(self.h, ctypes.byref(g))
 
     def apply_channel(self):
         L = load()

@@ -69,6 +69,53 @@ def test_forcing_cases_match_the_reference(tmp_path, name):
         assert same_energy(a, b), (a, b)
 
 
+@pytest.mark.parametrize("name", FULL)
+def test_device_forcing_matches_the_reference_within_rounding(tmp_path, name):
+    """--device-forcing: the Gaussians' fields, injected volume and rescale
+    evaluated on the GPU (sw2g_add_gaussian). Every padded cell of every frame
+    within 1e-12 of the field's largest magnitude of the reference's (the GPU's
+    cos, acos and exp and the order of the volume sum differ in the last bits),
+    PERTURBS and the times exact, and the ENERGY lines equal to their printed
+    digits."""
+    p = gc.forcing_params(name)
+    formats.write_sw(str(tmp_path / f"{name}.sw"), p)
+    energy, frames = run(tmp_path, name, flags=("--device-forcing",))
+    ref = gc.forcing_frames(name)
+    assert sorted(frames) == list(range(len(ref)))
+    for k, rf in enumerate(ref):
+        nstep, t, nx, ny, fl = frames[k]
+        assert t == float(rf["t"])
+        assert np.array_equal(fl["perturbs"], rf["perturbs"]), k
+        for f in ("eta", "u", "v", "tracer"):
+            scale = max(float(np.max(np.abs(rf[f]))), 1e-300)
+            assert np.max(np.abs(fl[f] - rf[f])) <= 1e-12 * scale, (k, f)
+    printed = gc.manifest()[name]["energy_printed"]
+    assert len(energy) == len(printed)
+    for a, b in zip(energy, printed):
+        assert same_energy(a, b), (a, b)
+
+
+def test_device_forcing_in_the_fp32_form(tmp_path):
+    """--fp32 --device-forcing on the moving Gaussian with tracer injection:
+    the FP32 form's tolerance of the reference's frames, as with the host
+    evaluation (h relative L2 <= 1e-5, tracer within 1e-3 of its largest
+    magnitude), PERTURBS exact."""
+    name = "f02_gauss_moving_tracer"
+    p = gc.forcing_params(name)
+    formats.write_sw(str(tmp_path / f"{name}.sw"), p)
+    _, frames = run(tmp_path, name, flags=("--fp32", "--device-forcing"))
+    ref = gc.forcing_frames(name)
+    assert sorted(frames) == list(range(len(ref)))
+    inner = (slice(2, -2), slice(2, -2))
+    for k, rf in enumerate(ref):
+        fl = frames[k][4]
+        assert np.array_equal(fl["perturbs"], rf["perturbs"]), k
+        h = rf["eta"][inner] + p.depth
+        assert np.linalg.norm((fl["eta"] - rf["eta"])[inner]) <= 1e-5 * np.linalg.norm(h), k
+        tr = max(float(np.max(np.abs(rf["tracer"]))), 1e-300)
+        assert np.max(np.abs(fl["tracer"] - rf["tracer"])) <= 1e-3 * tr, k
+
+
 @pytest.mark.parametrize("name", HASHED)
 def test_reference_example_run(tmp_path, name):
     """Runs kept as hashes: the reference's examples/JupiterEnergyTest case,
