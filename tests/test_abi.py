@@ -39,6 +39,14 @@ def test_library_exports_every_declared_symbol(L):
 def test_status_strings(L):
     assert lib.status_string(lib.OK) == "ok"
     assert "CFL" in lib.status_string(lib.ERR_CFL)
+    assert "volume" in lib.status_string(lib.ERR_FORCING)
+    assert lib.status_string(99) == "unknown status"
+
+
+def test_device_gaussian_rejects_bad_arguments_before_the_gpu(L):
+    L.sw2g_add_gaussian.argtypes = [ctypes.c_void_p, ctypes.POINTER(lib.Gaussian)]
+    g = lib.Gaussian(lon=0.0, lat=0.0, amp=1.0, sigma=1e6, radius=3e6, inject=0.0, volume=1.0, images=0)
+    assert L.sw2g_add_gaussian(None, ctypes.byref(g)) == lib.ERR_BAD_ARG
 
 
 def test_create_rejects_bad_cases_without_touching_the_gpu(L):
