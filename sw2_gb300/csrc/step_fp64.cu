@@ -39,6 +39,20 @@ __device__ __forceinline__ int dexp(double x) {
   return (int)(((unsigned long long)dbits(x) >> 52) & 0x7ffULL);
 }
 
+// a / b with a zero numerator answered from the bits: IEEE division gives
+// +-0 / b the zero whose sign is the exclusive or of the operands' signs for
+// every b other than a zero or a NaN; there the hardware sequence would take
+// its special-case path (about 15 FP64 instructions). Other operands divide.
+// The literal cells use it: in a state at rest their velocities, Courant
+// numbers and differences are zeros.
+__device__ __forceinline__ double zdiv(double a, double b) {
+  const long long A = dbits(a), B = dbits(b);
+  const long long mb = B & 0x7fffffffffffffffLL;
+  if ((A & 0x7fffffffffffffffLL) == 0 && mb != 0 && mb <= 0x7ff0000000000000LL)
+    return __longlong_as_double((A ^ B) & (long long)0x8000000000000000ULL);
+  return a / b;
+}
+
 // x * 2^k for k in -2..1 (p = 2^k), the same value as the FP64 product: when
 // x and the product are normal numbers, the product only changes the exponent
 // field, done here on the integer pipe; zeros are their own product; other
@@ -162,14 +176,14 @@ __device__ __forceinline__ double limiter(double r) {
   if constexpr (SCH == 0) return MX(0.0, MN(MN((1 + r) / 2.0, 2.0 * r), 2.0));
   else if constexpr (SCH == 1) return MX(MX(0.0, MN(2.0 * r, 1.0)), MX(0.0, MN(r, 2.0)));
   else if constexpr (SCH == 2) return MN(r, 1.0);
-  else if constexpr (SCH == 3) return (r + fabs(r)) / (1.0 + r);
+  else if constexpr (SCH == 3) return zdiv(r + fabs(r), 1.0 + r);
   else if constexpr (SCH == 4) return MX(0.0, MN(2.0 * r, MN((1 + 2.0 * r) / 3.0, 2.0)));
-  else if constexpr (SCH == 5) return (1.5 * (r * r + r)) / (r * r + r + 1.0);
-  else if constexpr (SCH == 6) return (r * r + r) / (r * r + 1.0);
+  else if constexpr (SCH == 5) return zdiv(1.5 * (r * r + r), r * r + r + 1.0);
+  else if constexpr (SCH == 6) return zdiv(r * r + r, r * r + 1.0);
   else if constexpr (SCH == 7) return MX(0.0, MN(MN(2.0, 2.0 * r), MN(0.25 + 0.75 * r, 0.75 + 0.25 * r)));
   else if constexpr (SCH == 8) return 0.0;
   else if constexpr (SCH == 9) return 1.0;
-  else return (r == -1.0) ? 0.0 : (r + fabs(r)) / (1.0 + r);
+  else return (r == -1.0) ? 0.0 : zdiv(r + fabs(r), 1.0 + r);
 #undef MN
 #undef MX
 }
@@ -179,8 +193,8 @@ template <int SCH>
 __device__ __forceinline__ void tvd_face(double qm, double q0, double q1, double q2, double cP, double cM,
                                          double& BP, double& BM) {
   const double d = q1 - q0;
-  const double rP = (d != 0) ? ((q0 - qm) / d) : 0.0;
-  const double rM = (d != 0) ? ((q2 - q1) / d) : 0.0;
+  const double rP = (d != 0) ? zdiv(q0 - qm, d) : 0.0;
+  const double rM = (d != 0) ? zdiv(q2 - q1, d) : 0.0;
   BP = q0 + limiter<SCH>(rP) * 0.5 * (1 - cP) * d;
   BM = q1 - limiter<SCH>(rM) * 0.5 * (1 + cM) * d;
 }
@@ -197,13 +211,13 @@ __device__ __forceinline__ double tvd_sum(const double* qx, const double* qy, do
   return cwP * wP + cwM * wM - ceP * eP - ceM * eM + csP * sP + csM * sM - cnP * nP - cnM * nM;
 }
 
-__device__ __forceinline__ double cpos(double a, double dt, double dx) { return 0.5 * (a + fabs(a)) * dt / dx; }
-__device__ __forceinline__ double cneg(double a, double dt, double dx) { return 0.5 * (a - fabs(a)) * dt / dx; }
+__device__ __forceinline__ double cpos(double a, double dt, double dx) { return zdiv(0.5 * (a + fabs(a)) * dt, dx); }
+__device__ __forceinline__ double cneg(double a, double dt, double dx) { return zdiv(0.5 * (a - fabs(a)) * dt, dx); }
 __device__ __forceinline__ double cpos2(double a, double b, double dt, double dx) {
-  return 0.5 * (0.5 * (a + fabs(a)) + 0.5 * (b + fabs(b))) * dt / dx;
+  return zdiv(0.5 * (0.5 * (a + fabs(a)) + 0.5 * (b + fabs(b))) * dt, dx);
 }
 __device__ __forceinline__ double cneg2(double a, double b, double dt, double dx) {
-  return 0.5 * (0.5 * (a - fabs(a)) + 0.5 * (b - fabs(b))) * dt / dx;
+  return zdiv(0.5 * (0.5 * (a - fabs(a)) + 0.5 * (b - fabs(b))) * dt, dx);
 }
 
 struct F7 {
@@ -283,8 +297,8 @@ __global__ void k_tracer(DevState s, F7 f, double* out) {
   const double pv1 = tvd_sum<SCH>(qx, qy, cpos(a, Dt, dxe), cneg(a, Dt, dxe), cpos(b, Dt, dxe), cneg(b, Dt, dxe),
                                   cpos(c, Dt, dyn), cneg(c, Dt, dyn), cpos(d, Dt, dyn), cneg(d, Dt, dyn));
   const double t = qx[2];
-  double pv2 = Dt * t * (b - a) / dxe;
-  pv2 += Dt * t * (d - c) / dyn;
+  double pv2 = zdiv(Dt * t * (b - a), dxe);
+  pv2 += zdiv(Dt * t * (d - c), dyn);
   double acc = pv1 + pv2;
   const double sigma = s.polar ? PF(s, P_STR, IX(W, i, j)) : s.sigma_tr;  // calc.c:152-161
   acc -= 2.0 * Dt * (sigma) * t;
@@ -304,7 +318,7 @@ __device__ __forceinline__ double advu_cell(const DevState& s, const F7& f, int 
   const double p1 = tvd_sum<SCH>(qx, qy, cpos2(uwm, u0, Dt, dxc), cneg2(uwm, u0, Dt, dxc), cpos2(u0, uep, Dt, dxc),
                                  cneg2(u0, uep, Dt, dxc), cpos2(vs0, vs1, Dt, dyv), cneg2(vs0, vs1, Dt, dyv),
                                  cpos2(vn0, vn1, Dt, dyv), cneg2(vn0, vn1, Dt, dyv));
-  const double p2 = Dt * (u0 * (uep - uwm) / RW(s, R_DXE2, j) + u0 * ((vn0 + vn1) / 2. - (vs0 + vs1) / 2.) / dyv);
+  const double p2 = Dt * (zdiv(u0 * (uep - uwm), RW(s, R_DXE2, j)) + zdiv(u0 * ((vn0 + vn1) / 2. - (vs0 + vs1) / 2.), dyv));
   return p1 + p2;
 }
 
@@ -328,7 +342,7 @@ __device__ __forceinline__ double advv_cell(const DevState& s, const F7& f, int 
   const double p1 = tvd_sum<SCH>(qx, qy, cpos2(uw1, uw0, Dt, dxv), cneg2(uw1, uw0, Dt, dxv), cpos2(ue1, ue0, Dt, dxv),
                                  cneg2(ue1, ue0, Dt, dxv), cpos2(vsm, v0, Dt, dyc), cneg2(vsm, v0, Dt, dyc),
                                  cpos2(v0, vnp, Dt, dyc), cneg2(v0, vnp, Dt, dyc));
-  const double p2 = Dt * (v0 * ((ue0 + ue1) / 2. - (uw0 + uw1) / 2.) / dxv + v0 * (vnp - vsm) / RW(s, R_DYNS, j));
+  const double p2 = Dt * (zdiv(v0 * ((ue0 + ue1) / 2. - (uw0 + uw1) / 2.), dxv) + zdiv(v0 * (vnp - vsm), RW(s, R_DYNS, j)));
   return p1 + p2;
 }
 

@@ -279,6 +279,7 @@ def test_fast_limiters_source_matches_the_literal_limiters_on_the_host(tmp_path)
                   if ln.startswith("__device__ __forceinline__ double mn(") or
                   ln.startswith("__device__ __forceinline__ double mx(")]
     assert len(one_liners) == 2
+    one_liners.append(function_text(src, "__device__ __forceinline__ double zdiv(double a, double b) {"))
     lim = "template <int SCH>\n" + function_text(src, "__device__ __forceinline__ double limiter(double r) {")
     fast = "template <int SCH>\n" + function_text(src, "__device__ __forceinline__ double limiter_fast(double r) {")
     parts = [pw, key, "\n".join(one_liners), lim, fast]
@@ -340,3 +341,61 @@ def test_range_check_source_matches_the_reference_predicate_on_the_host(tmp_path
     subprocess.run(["g++", "-O2", "-fno-fast-math", "-o", str(exe), str(c)], check=True)
     bad, n = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     assert int(bad) == 0 and int(n) > 0
+
+
+ZDIV_HARNESS = r"""
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+static inline long long dbits(double x) { long long r; std::memcpy(&r, &x, 8); return r; }
+static inline double __longlong_as_double(long long b) { double r; std::memcpy(&r, &b, 8); return r; }
+%s
+static uint64_t st = 0x2545F4914F6CDD1DULL;
+static uint64_t next() {  // SplitMix64
+  uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+static bool isnan_bits(double x) { return (dbits(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL; }
+static bool same(double want, double got) {
+  if (isnan_bits(want)) return isnan_bits(got);
+  return dbits(want) == dbits(got);
+}
+int main(int argc, char** argv) {
+  const double edge[] = {0.0, -0.0, 1.0, -1.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.7976931348623157e308,
+                         INFINITY, -INFINITY, NAN, -NAN, 3.0, -7.5e-300};
+  long long bad = 0;
+  const int ne = sizeof(edge) / sizeof(edge[0]);
+  for (int i = 0; i < ne; i++)
+    for (int k = 0; k < ne; k++) bad += !same(edge[i] / edge[k], zdiv(edge[i], edge[k]));
+  const long long n = atoll(argv[1]);
+  for (long long t = 0; t < n; t++) {
+    const uint64_t r1 = next(), r2 = next();
+    double a = __longlong_as_double((long long)r1), b = __longlong_as_double((long long)r2);
+    if (r1 & 1) a = (r1 & 2) ? -0.0 : 0.0;  // half the numerators zero
+    bad += !same(a / b, zdiv(a, b));
+  }
+  printf("%%lld\n", bad);
+  return 0;
+}
+"""
+
+
+def test_zero_numerator_division_source_matches_ieee_on_the_host(tmp_path):
+    """zdiv (the literal cells' division, a zero numerator answered from the
+    bits) equals IEEE division bit for bit (NaNs as NaNs) on every pair of
+    edge values (zeros of both signs, subnormals, the extremes, infinities,
+    NaNs) and on random bit patterns, half of them with zero numerators."""
+    src = open(SRC).read()
+    z = function_text(src, "__device__ __forceinline__ double zdiv(double a, double b) {")
+    z = re.sub(r"__device__ __forceinline__", "static inline", z)
+    c = tmp_path / "zdiv.cpp"
+    c.write_text(ZDIV_HARNESS % z)
+    exe = tmp_path / "zdiv"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-o", str(exe), str(c)],
+                   check=True)
+    out = subprocess.run([str(exe), str(2_000_000)], check=True, capture_output=True, text=True).stdout
+    assert out.split() == ["0"]
