@@ -337,60 +337,52 @@ def metric_divisors(case):
     return np.array(out)
 
 
-def forcing_leg(n_short: int, n_long: int):
+def forcing_leg(nsteps: int = 40):
     """Per-step time of the case-file runner (sw2g-run: case reader, forcing,
-    GPU step) on a 1024x512 band with three Gaussians injected in every step
-    (cases.forcing_band with the injections kept on through the longer run),
-    in its two forcing paths: the host evaluates the cells inside the radii
-    with the reference's expressions and sends them as lists (bit for bit), or
-    the GPU evaluates the fields, the volume and its rescale from the per-step
-    scalars (--device-forcing, within rounding). Two runs of n_short and
-    n_long steps from the same start per path, each writing only its first
-    and last frame; the difference of their wall times over the difference of
-    steps is the time of a forced step. The band starts at rest, as the
-    reference's forcing cases do: the cells the waves have not reached have
-    zero fluxes, which the FP64 bodies compute with the literal per-cell code,
-    so these steps cost several times a step of a flowing state."""
+    GPU step) on a 1024x512 band with three Gaussians injected in each of its
+    40 steps (cases.forcing_band), in its two forcing paths: the host
+    evaluates the cells inside the radii with the reference's expressions and
+    sends them as lists (bit for bit), or the GPU evaluates the fields, the
+    volume and its rescale from the per-step scalars (--device-forcing, within
+    rounding). The runner times its own time loop (--timing: every step
+    forced, a frame at the first and the last); best of three runs per path.
+    The band starts at rest, as the reference's forcing cases do: the cells
+    the waves have not reached have zero fluxes, which the FP64 bodies compute
+    with the literal per-cell code, so these steps cost more than a step of a
+    flowing state."""
+    import re
     import tempfile
 
     from sw2_gb300 import cases, formats, hostlib
 
     def per_step(flags):
-        times = {}
+        best = None
         with tempfile.TemporaryDirectory() as wd:
-            for n in (n_short, n_long):
-                p = cases.forcing_band(n)
-                for gr in p.gaussians:  # injecting in every step of both runs
-                    gr[1] = (n_long + 1) * p.Dt
-                name = f"forced{n}"
-                formats.write_sw(os.path.join(wd, name + ".sw"), p)
-                os.makedirs(os.path.join(wd, "out"), exist_ok=True)
-                t0 = time.perf_counter()
-                r = subprocess.run([hostlib.RUNNER, "--quiet", *flags, "1", "1", name, "out"], cwd=wd,
+            p = cases.forcing_band(nsteps)
+            name = "forced"
+            formats.write_sw(os.path.join(wd, name + ".sw"), p)
+            os.makedirs(os.path.join(wd, "out"), exist_ok=True)
+            for _ in range(3):
+                r = subprocess.run([hostlib.RUNNER, "--quiet", "--timing", *flags, "1", "1", name, "out"], cwd=wd,
                                    capture_output=True, text=True, timeout=600)
-                times[n] = time.perf_counter() - t0
-                if r.returncode != 0:
-                    return None, {"error": r.stderr[-500:]}
-        return (times[n_long] - times[n_short]) / (n_long - n_short), times
+                m = re.search(r"LOOP (\d+) steps ([0-9.eE+-]+) s", r.stderr)
+                if r.returncode != 0 or not m:
+                    return {"error": r.stderr[-500:]}
+                t = float(m.group(2)) / int(m.group(1))
+                best = t if best is None else min(best, t)
+        return best
 
-    host, th = per_step(())
-    dev, td = per_step(("--device-forcing",))
-    if host is None:
-        return th
-    p = cases.forcing_band(n_long)
-    out = {"workload": f"{p.nx}x{p.ny} band, 3 Gaussians injected every step (ramped static, moving across "
-                       f"the seam with tracer, against the wall), minmod, nu4, FP64",
-           "ms_per_forced_step": 1e3 * host, "cell_updates_per_s": p.nx * p.ny / host,
-           "runs_s": {str(k): v for k, v in th.items()},
-           "path": "sw2g-run: host evaluation of the cells inside each radius, sw2g_set_cells + sw2g_add_cells "
-                   "between sw2g_step_open and sw2g_step_close"}
-    if dev is not None:
-        out["device_forcing"] = {"ms_per_forced_step": 1e3 * dev, "cell_updates_per_s": p.nx * p.ny / dev,
-                                 "runs_s": {str(k): v for k, v in td.items()},
-                                 "path": "sw2g-run --device-forcing: sw2g_add_gaussian (field, volume sum and "
-                                         "rescale on the GPU) between sw2g_step_open and sw2g_step_close"}
-    else:
-        out["device_forcing"] = td
+    host = per_step(())
+    dev = per_step(("--device-forcing",))
+    p = cases.forcing_band(nsteps)
+    out = {"workload": f"{p.nx}x{p.ny} band from rest, 3 Gaussians injected in each of {nsteps} steps (ramped "
+                       f"static, moving across the seam with tracer, against the wall), minmod, nu4, FP64"}
+    for key, v, path in (("host_forcing", host, "host evaluation of the cells inside each radius, sw2g_set_cells + "
+                                                  "sw2g_add_cells between sw2g_step_open and sw2g_step_close"),
+                         ("device_forcing", dev, "sw2g_add_gaussian: field, volume sum and rescale on the GPU, "
+                                                 "between sw2g_step_open and sw2g_step_close")):
+        out[key] = v if isinstance(v, dict) else {"ms_per_forced_step": 1e3 * v,
+                                                  "cell_updates_per_s": p.nx * p.ny / v, "path": path}
     return out
 
 
@@ -558,7 +550,7 @@ def main():
         accl["workload"] = args.large_config
         large = (cl.params.nx * cl.params.ny, descl, ml64, ml32, accl)
         del cl
-    forced = forcing_leg(20, 220) if args.forcing and rank == 0 else None
+    forced = forcing_leg() if args.forcing and rank == 0 else None
     # the FP64 step's division by row metrics (one Markstein correction)
     # against IEEE division: 1e10 random and near-midpoint numerators over the
     # metric factors of the headline workload, and each factor against the

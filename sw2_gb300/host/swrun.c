@@ -8,7 +8,8 @@
  * GPU (sw2g_add_gaussian: results within rounding of the reference's); by
  * default the host evaluates them with the reference's expressions and libm
  * and only the cells inside each radius cross to the GPU (bit for bit).
- * --checkpoint writes, next to each frame, an exact-restart
+ * --timing prints the time loop's step count and wall time on stderr
+ * ("LOOP n steps t s"). --checkpoint writes, next to each frame, an exact-restart
  * checkpoint (full padded state, Adams-Bashforth histories and index);
  * --resume F continues from the checkpoint of frame F bit for bit as the
  * uninterrupted run would (the reference's LoadFrom restarts with an Euler
@@ -33,6 +34,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <time.h>
 
 #include "sw2g.h"
 #include "swcase.h"
@@ -354,8 +356,14 @@ static int print_energy(sw2g_ctx *g, double t) {
   return 0;
 }
 
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, int checkpoint, int resume,
-                  int device_forcing) {
+                  int device_forcing, int timing) {
   char err[512] = {0}, path[4096];
   snprintf(path, sizeof path, "%s.sw", bname);
   swcase c;
@@ -466,6 +474,8 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
   if (!quiet)
     fprintf(stderr, "sw2g-run: %s %dx%d, steps %d..%d, Dt %g, %s%s\n", bname, nx, ny, nstart, c.N, Dt,
             fp32 ? "FP32 form" : "FP64", device_forcing ? ", Gaussians evaluated on the GPU" : "");
+  const double loop_t0 = now_s();
+  const int loop_n0 = nstart;
   for (int n = nstart; n <= c.N;) {
     /* steps without output or forcing are run in one call */
     int k = 1;
@@ -521,6 +531,8 @@ int sw2g_run_case(const char *bname, const char *outdir, int fp32, int quiet, in
       if (print_energy(g, t)) goto done;
     }
   }
+  if (timing) /* the time loop's wall time: steps, forcing, frames and ENERGY lines */
+    fprintf(stderr, "LOOP %d steps %.6f s\n", c.N - loop_n0 + 1, now_s() - loop_t0);
   rc = 0;
 done:
   if (writer_stop(&wr) && rc == 0) rc = 1;
