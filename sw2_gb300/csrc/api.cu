@@ -668,8 +668,8 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
     c32.wy = x->d_aux32[1];
     c32.hb = x->d_aux32[2];
     if (c->polar != 0) {  // the cap's per-cell factors, FP64 arithmetic rounded once
-      const int P = c32.P, R = c32.R, W = s.W, H = s.H;
-      const size_t S32 = (size_t)P * R;
+      const int P = c32.P, W = s.W, H = s.H;
+      const size_t S32 = (size_t)P * c32.R;
       std::vector<float> q32((size_t)PQ_NUM * S32, 0.f);
       auto row = [&](int t, int j) { return x->rows[(size_t)t * H + (j + 1)]; };
       const double Dt = c->Dt;
@@ -693,7 +693,6 @@ sw2g_status sw2g_create(const sw2g_case* c, int precision, int device, sw2g_ctx*
         return fail(st);
       c32.polar = c->polar;
       c32.pf = d_pf32;
-      (void)R;
     }
     fp32_tiles(c->nx, c->ny, x->run32.th, &x->run32.nbx, &x->run32.nby);
     if ((st = cuda_fail(x->run32.alloc(0), "batch")) != SW2G_OK) return fail(st);
